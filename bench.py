@@ -1,0 +1,385 @@
+#!/usr/bin/env python
+"""Benchmark of the trace-transform sinogram + circus path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+    python bench.py --impl reference ...
+
+A step is one pass of the hot path over one image: the fused rotate +
+T-functional kernel (all sinograms), the P-functional kernel (all circus
+functions) and the z-score kernel.  The metric is sinograms per second
+(sinograms = images x T-functionals).  Prints one JSON line (rank 0).
+
+* value      device-resident throughput: the image already in HBM, CUDA events
+             around each step, L2 flushed (256 MiB write) between steps
+* e2e        the same metric through the C ABI drop-in tt_transform with host
+             buffers (pinned): host->device image copy, compute, device->host
+             circus + signatures inside the timed region
+* roofline   the fused sinogram kernel: algorithmic bytes per launch
+             (4 A H W image sweeps + 4 nT N A sinogram writes) / its
+             event-timed duration, against the measured HBM copy bandwidth
+* cpu_baseline  the CPU oracle (a C restatement of the reference's float path,
+             OpenMP over angles as the reference's openmp/ port) on all host
+             cores, timed on a subset of the angles and scaled to the image
+
+--impl reference times that CPU implementation alone as the reference arm.
+Multi-GPU (torchrun): every rank transforms its own image (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sinograms/sec"
+WORKLOADS = {
+    # name: (rows, cols, n_blobs, sigma, seed, angle_step, T list, P list)
+    "single256": (256, 256, 8, (8, 40), 1, 1.0, [0, 1, 2, 3, 4, 5], [1, 2, 3]),
+    "single1024": (1024, 1024, 32, (16, 160), 2, 1.0, [0, 1, 2, 3, 4, 5, 6, 7], [1, 2, 3]),
+    "single4096": (4096, 4096, 256, (32, 640), 6, 0.5, [0, 1, 2, 3, 4, 5, 6, 7], [1, 2, 3]),
+}
+DEFAULT_WORKLOAD = "single1024"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="target CPU time of the baseline sample")
+    return ap.parse_args()
+
+
+def make_image(name):
+    from tracetransform_gb300.synthetic import blob_image
+    rows, cols, nb, sigma, seed, step, tfs, pfs = WORKLOADS[name]
+    img = blob_image(rows, cols, nb, sigma, (40, 200), seed)
+    n_ang = int(np.floor(360.0 / step))
+    angles = (np.arange(n_ang, dtype=np.float64) * step).astype(np.float32)
+    return img, angles, tfs, pfs
+
+
+def config_dict(name, n, angles, tfs, pfs, world):
+    rows, cols = WORKLOADS[name][:2]
+    return {"workload": name, "image": f"{rows}x{cols}", "padded": n, "angles": len(angles),
+            "angle_step_deg": WORKLOADS[name][5], "t_functionals": tfs,
+            "p_functionals": pfs, "images_per_step_per_gpu": 1,
+            "l2": "flushed between timed steps (256 MiB write)",
+            "parallelism": f"replicas{world}" if world > 1 else "single"}
+
+
+# ---------------------------------------------------------------------------
+# CPU side (oracle): timed baseline / reference arm
+# ---------------------------------------------------------------------------
+
+def cpu_sample(img, angles, tfs, pfs, target_s, threads=0):
+    """Time the oracle on a growing subset of angles until it takes target_s;
+    returns (seconds per full transform, sample description, threads)."""
+    from oracle import oracle as O
+    O.build()
+    padded = O.pad(img)
+    nthreads = threads or os.cpu_count() or 1
+    k = min(len(angles), max(1, nthreads))
+    while True:
+        sub = angles[:: max(1, len(angles) // k)][:k]
+        t0 = time.perf_counter()
+        sino = O.sinograms(padded, sub, tfs, threads)
+        for t in range(sino.shape[0]):
+            O.circus(sino[t], [(p, 0, 0) for p in pfs], threads)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or len(sub) >= len(angles):
+            break
+        k = min(len(angles), int(k * max(2.0, 1.2 * target_s / max(dt, 1e-3))))
+    per_image = dt * len(angles) / len(sub)
+    desc = (f"{len(sub)} of {len(angles)} angles of the same image (all T and P "
+            f"functionals), {dt:.1f} s, scaled by {len(angles) / len(sub):.2f}")
+    return per_image, desc, nthreads
+
+
+def run_reference(args, world, rank):
+    img, angles, tfs, pfs = make_image(args.workload)
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    n = O.pad_geometry(*img.shape)[0]
+    target = max(1.0, args.cpu_seconds / max(1, args.steps))
+    per = []
+    desc = ""
+    threads = os.cpu_count() or 1
+    for i in range(args.warmup + args.steps):
+        t, desc, threads = cpu_sample(img, angles, tfs, pfs, target)
+        if i >= args.warmup:
+            per.append(t)
+    sec = statistics.median(per)
+    value = len(tfs) / sec
+    line = {"metric": METRIC, "value": value, "unit": "sinograms/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded blob+noise)", "impl": "reference",
+            "config": config_dict(args.workload, n, angles, tfs, pfs, world),
+            "cpu_baseline": {"value": value, "unit": "sinograms/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "sinograms/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def committed_traffic(kernel, workload):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+def run_engine(args, world, rank, local_rank):
+    import torch
+    import tracetransform_gb300 as tt
+    from tracetransform_gb300 import _native
+    from tracetransform_gb300.device import Engine, to_colmajor
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    img, angles, tfs, pfs = make_image(args.workload)
+    rows, cols = img.shape
+    n = tt.pad_geometry(rows, cols)[0]
+    A = len(angles)
+    eng = Engine(local_rank)
+    img_dev = to_colmajor(torch.from_numpy(np.ascontiguousarray(img)).to(dev))
+    sino = torch.empty((len(tfs), A, n), dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    pf = [(p, 0, -1) for p in pfs]
+    stream = torch.cuda.current_stream(dev)
+
+    def step(ev_sino=None):
+        if ev_sino:
+            ev_sino[0].record(stream)
+        eng.sinograms(img_dev, rows, cols, angles, tfs, out=sino)
+        if ev_sino:
+            ev_sino[1].record(stream)
+        circ = eng.circus(sino, pf)
+        return eng.zscore(circ)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ks = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    barrier(world)
+    for i in range(args.steps):
+        flush.zero_()
+        starts[i].record(stream)
+        step(ks[i])
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    kern_ms = [a.elapsed_time(b) for a, b in ks]
+    ms = sum(step_ms) / len(step_ms)
+    ms = max_over_ranks(ms, world)
+    launches = 3 * args.steps
+
+    # end to end through the C ABI drop-in, pinned host buffers
+    lib = _native.lib()
+    h_img = torch.from_numpy(np.ascontiguousarray(img.ravel(order="F"))).pin_memory()
+    n_out = len(tfs) * len(pfs) * A
+    h_circ = torch.empty(n_out, dtype=torch.float32).pin_memory()
+    h_sig = torch.empty(n_out, dtype=torch.float32).pin_memory()
+    ids = np.asarray(tfs, np.int32)
+    pfa = (_native.PFunctionalC * len(pfs))()
+    for i, p in enumerate(pfs):
+        pfa[i].kind, pfa[i].order, pfa[i].center = p, -1, -1
+    fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float))
+    step_deg = WORKLOADS[args.workload][5]
+
+    def e2e_step():
+        if float(step_deg) == int(step_deg):
+            _native.check(lib.tt_transform(eng.plan.handle, fp(h_img), rows, cols, int(step_deg),
+                                           _native.iptr(ids), len(ids), pfa, len(pfs), fp(h_circ),
+                                           fp(h_sig)))
+        else:  # fractional angle steps go through the device entry points
+            d = h_img.to(dev, non_blocking=True).view(cols, rows)
+            s = eng.sinograms(d, rows, cols, angles, tfs, out=sino)
+            c = eng.circus(s, pf)
+            z = eng.zscore(c)
+            h_circ.copy_(c.view(-1), non_blocking=True)
+            h_sig.copy_(z.view(-1), non_blocking=True)
+            torch.cuda.synchronize()
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_times.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    e2e_s = max_over_ranks(sum(e2e_times) / len(e2e_times) * 1e3, world) / 1e3
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    alg_bytes = 4.0 * A * rows * cols + 4.0 * len(tfs) * n * A
+    kern_s = (sum(kern_ms) / len(kern_ms)) / 1e3
+    achieved = alg_bytes / kern_s / 1e9
+    line = {
+        "metric": METRIC, "value": world * len(tfs) / (ms / 1e3), "unit": "sinograms/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded blob+noise, the reference ships no images)",
+        "config": config_dict(args.workload, n, angles, tfs, pfs, world),
+        "e2e": {"value": world * len(tfs) / e2e_s, "unit": "sinograms/s",
+                "h2d_bytes_per_step": int(rows * cols * 4),
+                "d2h_bytes_per_step": int(2 * n_out * 4)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "sino_kernel", "achieved": achieved,
+                     "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
+                     "frac": achieved / peak,
+                     "traffic": committed_traffic("sino_kernel", args.workload),
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "kernel_ms": kern_s * 1e3},
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        per, desc, cores = cpu_sample(img, angles, tfs, pfs, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": len(tfs) / per, "unit": "sinograms/s", "cores": cores,
+                                "kind": "port", "sample": desc}
+    print(json.dumps(line), flush=True)
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if world > 1 and rank != 0:
+            return
+        run_reference(args, world, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    run_engine(args, world, rank, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+/*
+ * tracetransform.h -- C ABI of the GB300 trace-transform engine
+ * (libtt_gb300.so).
+ *
+ * The engine is a drop-in for the sinogram + circus-function path of
+ * maleadt/tracetransform's C++ implementation: a padded image is rotated over
+ * a set of angles, every rotated column is reduced by T-functionals into
+ * sinograms, every sinogram column by P-functionals into circus functions,
+ * and each circus function is z-scored into the signature matrix.
+ *
+ * Conventions (those of the reference's Eigen matrices):
+ *   - matrices are float32, column-major: element (row, col) of an R x C
+ *     matrix is at [row + col * R];
+ *   - a stack of nT sinograms is nT consecutive N x A matrices, column a
+ *     holding angle a;
+ *   - circus functions are nT x nP consecutive vectors of length A (T-major);
+ *   - the signature matrix is A x (nT * nP), column t * nP + p being the
+ *     z-scored circus function of (T t, P p) -- the same bytes as the circus
+ *     stack, z-scored.
+ *
+ * Every call returns a tt_status; on failure tt_last_error() describes the
+ * error of the calling thread.  Host-pointer calls are synchronous; *_device
+ * calls take device pointers and are ordered on the given CUDA stream (NULL:
+ * the plan's own stream) and return before the work completes.
+ */
+#ifndef TRACETRANSFORM_H
+#define TRACETRANSFORM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    TT_OK = 0,
+    TT_ERR_INVALID_ARG = 1, /* bad size, id or pointer (reference: assert /
+                               boost::program_options::validation_error) */
+    TT_ERR_UNSUPPORTED = 2, /* valid request this build does not handle */
+    TT_ERR_CUDA = 3,        /* CUDA runtime error (reference: CUDAHelper::Error) */
+    TT_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+    TT_ERR_OOM = 5          /* device or host allocation failed */
+} tt_status;
+
+/* T-functional ids: the strings "0".."7" of c++/src/sinogram.cpp:34-65
+ * (enum class TFunctional, c++/src/sinogram.hpp:22-31). */
+enum {
+    TT_T_RADON = 0,
+    TT_T1 = 1,
+    TT_T2 = 2,
+    TT_T3 = 3,
+    TT_T4 = 4,
+    TT_T5 = 5,
+    TT_T6 = 6,
+    TT_T7 = 7
+};
+
+/* P-functional kinds: "1", "2", "3" and "H<order>" of c++/src/circus.cpp:33-66
+ * (enum class PFunctional, c++/src/circus.hpp:27-32). */
+enum { TT_P_HERMITE = 0, TT_P1 = 1, TT_P2 = 2, TT_P3 = 3 };
+
+/* PFunctionalWrapper + PFunctionalArguments{order, center}
+ * (c++/src/circus.hpp:34-57).  order and center are used by TT_P_HERMITE
+ * only; center < 0 means "not set". */
+typedef struct {
+    int32_t kind;
+    int32_t order;
+    int32_t center;
+} tt_pfunctional;
+
+#define TT_MAX_TFUNCTIONALS 8
+#define TT_MAX_PFUNCTIONALS 16
+
+/* Opaque engine state: device tables (T3-T5 kernels, FFT chirps, Hermite
+ * bases), staging buffers and streams of one device.  Re-entrant per plan;
+ * one plan must not be used by two threads at once. */
+typedef struct tt_plan tt_plan;
+
+/* ---- plans and errors ------------------------------------------------ */
+tt_status tt_plan_create(tt_plan **plan, int device);
+tt_status tt_plan_destroy(tt_plan *plan);
+/* Message for the last failed call on this thread ("" if none). */
+const char *tt_last_error(void);
+/* Library version string. */
+const char *tt_version(void);
+
+/* ---- geometry (host only) -------------------------------------------- */
+/* Side N of the padded square and the offset of the image inside it:
+ * pad() of c++/src/auxiliary.cpp:257-275. */
+tt_status tt_pad_geometry(int rows, int cols, int *n, int *row_off, int *col_off);
+/* Side the orthonormal (Hermite) mode stretches the image to before padding:
+ * Transformer::Transformer, c++/src/transform.cpp:35-41. */
+tt_status tt_ortho_size(unsigned angle_stepsize, int *side);
+/* Angles a_step * step, a_step in [0, floor(360 / step)), in degrees
+ * (c++/src/sinogram.cpp:77, 112).  *count receives the number of angles;
+ * angles may be NULL to query it. */
+tt_status tt_angles_from_step(unsigned angle_stepsize, float *angles, int capacity,
+                              int *count);
+
+/* ---- drop-in entry points (host buffers, synchronous) ----------------- */
+/* Replaces getSinograms(const Eigen::MatrixXf& padded, unsigned
+ * angle_stepsize, const std::vector<TFunctionalWrapper>&)
+ * (c++/src/sinogram.hpp:57-59, c++/src/sinogram.cpp:67-178).
+ * padded: rows x cols, must be square (the reference asserts it).
+ * out: n_t x (rows x floor(360 / angle_stepsize)). plan may be NULL (the
+ * process-wide plan of the current device is used). */
+tt_status tt_sinograms(tt_plan *plan, const float *padded, int rows, int cols,
+                       unsigned angle_stepsize, const int32_t *tfuncs, int n_t,
+                       float *out);
+
+/* Replaces getCircusFunctions(const Eigen::MatrixXf& sinogram, const
+ * std::vector<PFunctionalWrapper>&) (c++/src/circus.hpp:69-71,
+ * c++/src/circus.cpp:104-177).  sinogram: rows x cols; out: n_p x cols.
+ * Hermite entries need center >= 0 (the reference dereferences the optional). */
+tt_status tt_circus(tt_plan *plan, const float *sinogram, int rows, int cols,
+                    const tt_pfunctional *pfuncs, int n_p, float *out);
+
+/* Replaces rotate(input, origin, deg2rad(angle)) with the origin
+ * ((cols-1)/2, (rows-1)/2) that getSinograms uses (c++/src/auxiliary.cpp:
+ * 223-255, c++/src/sinogram.cpp:73-74, c++/src/rottest.cpp:46-49).  The
+ * rotated image is bit-identical to the reference's; it uses the sampling
+ * code of the fused sinogram kernel, which never writes it out. */
+tt_status tt_rotate(tt_plan *plan, const float *image, int rows, int cols, float angle_deg,
+                    float *out);
+
+/* Replaces zscore(const Eigen::VectorXf&) (c++/src/auxiliary.cpp:305-318)
+ * applied to n_vec consecutive vectors of length len. */
+tt_status tt_zscore(tt_plan *plan, const float *in, int n_vec, int len, float *out);
+
+/* Replaces Transformer(image, basename, angle_step, orthonormal) +
+ * getTransform(T, P, write_data) (c++/src/transform.cpp:28-112) without the
+ * file output: image is the unpadded rows x cols image (values as gray2mat
+ * gives them).  Orthonormal mode is selected as demo.cpp:153-169 does: all P
+ * Hermite -> orthonormal, none -> regular, mixed -> TT_ERR_INVALID_ARG.
+ * circus (may be NULL): n_t x n_p x A raw circus functions.
+ * signatures (may be NULL): A x (n_t * n_p) z-scored.
+ * In orthonormal mode the Hermite centers come from the nearest orthonormal
+ * sinogram; the centers of pfuncs are ignored (the reference overwrites
+ * them). */
+tt_status tt_transform(tt_plan *plan, const float *image, int rows, int cols,
+                       unsigned angle_stepsize, const int32_t *tfuncs, int n_t,
+                       const tt_pfunctional *pfuncs, int n_p, float *circus,
+                       float *signatures);
+
+/* ---- device entry points (stream ordered) ----------------------------- */
+/* Fused rotate + T-functional sweep over an explicit angle list (degrees;
+ * the integer-step list of the reference is tt_angles_from_step).
+ * src: src_rows x src_cols image with leading dimension src_ld, placed at
+ * (row_off, col_off) inside an n x n zero frame (row_off = col_off = 0 and
+ * src_rows = src_cols = n for an already padded image).
+ * d_out: n_t x n x n_angles.  d_medians (may be NULL): n_t x n x n_angles
+ * int32, the weighted-median row each T-functional used (-1 for Radon). */
+tt_status tt_sinograms_device(tt_plan *plan, const float *d_src, int src_rows,
+                              int src_cols, int src_ld, int n, int row_off,
+                              int col_off, const float *angles_deg, int n_angles,
+                              const int32_t *tfuncs, int n_t, float *d_out,
+                              int32_t *d_medians, void *stream);
+
+/* P-functionals over n_sino stacked rows x cols sinograms.  d_out:
+ * n_sino x n_p x cols.  Hermite centers: centers[s] (host array of n_sino
+ * entries) when not NULL, else each pfunctional's own center. */
+tt_status tt_circus_device(tt_plan *plan, const float *d_sino, int rows, int cols,
+                           int n_sino, const tt_pfunctional *pfuncs, int n_p,
+                           const int32_t *centers, float *d_out, void *stream);
+
+/* z-score of n_vec consecutive vectors of length len (device). */
+tt_status tt_zscore_device(tt_plan *plan, const float *d_in, int n_vec, int len,
+                           float *d_out, void *stream);
+
+/* Synchronise the plan's stream. */
+tt_status tt_plan_synchronize(tt_plan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

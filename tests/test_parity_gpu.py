@@ -1,0 +1,198 @@
+"""GPU parity: the CUDA engine, called through its C ABI, against the CPU
+oracle (oracle/, pinned to the reference's own sources by
+tests/test_oracle_golden.py) and against the golden fixtures directly.
+
+Tolerances are in tests/parity.py: 1e-4 relative per entry with a column
+guard, bit-exact rotated samples and z-scores, weighted-median rows exact
+except counted ties.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import tracetransform_gb300 as tt
+from tracetransform_gb300.synthetic import blob_image
+
+from parity import RTOL, close_mask, median_tie, rel_err
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
+                if not p.endswith("rotate9.npz"))
+P123 = ["1", "2", "3"]
+
+
+def load(name):
+    return dict(np.load(os.path.join(HERE, "golden", name + ".npz")))
+
+
+@pytest.fixture(scope="module")
+def engine():
+    import torch
+    from tracetransform_gb300.device import Engine
+    assert torch.cuda.is_available()
+    return Engine(0)
+
+
+def test_rotation_bit_exact_golden():
+    g = load("rotate9")
+    for a, want in zip(g["angles"], g["rotated"]):
+        assert np.array_equal(tt.api.rotate(g["image"], float(a)), want), a
+
+
+@pytest.mark.parametrize("shape,seed", [((47, 47), 1), ((20, 13), 2), ((13, 31), 3), ((91, 91), 4)])
+def test_rotation_bit_exact_oracle(oracle_lib, shape, seed):
+    img = blob_image(shape[0], shape[1], 4, (2, 9), (40, 200), seed)
+    for a in (0.0, 0.5, 1.0, 13.0, 45.0, 89.0, 90.0, 91.0, 180.0, 233.5, 270.0, 359.0):
+        assert np.array_equal(tt.api.rotate(img, a), oracle_lib.rotate(img, a)), a
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_golden_sinograms(name):
+    g = load(name)
+    tfs = [str(t) for t in g["tfuncs"]]
+    sinos = tt.getSinograms(g["padded"], int(g["step"]), tfs)
+    got = np.stack(sinos)  # (nT, N, A)
+    ok = close_mask(np.swapaxes(got, 1, 2), np.swapaxes(g["sino"], 1, 2))
+    assert ok.mean() >= 0.995, f"{name}: {(~ok).sum()} entries off"
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_golden_transform(name):
+    g = load(name)
+    tfs = [str(t) for t in g["tfuncs"]]
+    pfs = [("H%d" % o) if k == 0 else str(k) for k, o in zip(g["pkinds"], g["porders"])]
+    ortho = any(k == 0 for k in g["pkinds"])
+    tr = tt.Transformer(g["image"], "golden", int(g["step"]), ortho)
+    sig = tr.getTransform(tfs, pfs, write_data=False)
+    ok_c = close_mask(tr.circus, g["circus"])
+    # z-scores amplify circus rounding by 1/std: compare at the column guard
+    ok_s = close_mask(sig.T, g["sig"].T, rtol=1e-3)
+    assert ok_c.mean() >= 0.99, f"{name}: circus {(~ok_c).sum()} entries off"
+    assert ok_s.mean() >= 0.99, f"{name}: signatures {(~ok_s).sum()} entries off"
+
+
+def _check_sinograms(oracle_lib, engine, img, step, tfs, report=None):
+    import torch
+    from tracetransform_gb300.device import to_colmajor
+    padded = oracle_lib.pad(img)
+    n = padded.shape[0]
+    ang = oracle_lib.angles_for_step(step)
+    ref, ref_med = oracle_lib.sinograms(padded, ang, tfs, with_medians=True)
+    dev = to_colmajor(torch.from_numpy(np.ascontiguousarray(img)).cuda())
+    out, med = engine.sinograms(dev, img.shape[0], img.shape[1], ang, tfs, medians=True)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().transpose(0, 2, 1)        # (nT, N, A)
+    got_med = med.cpu().numpy().transpose(0, 2, 1)
+    ties = 0
+    mism = np.argwhere(got_med != ref_med)
+    tie_cols = set()
+    rot_cache = {}
+    for t, col, a in mism:
+        f = tfs[t]
+        if a not in rot_cache:
+            rot_cache[a] = oracle_lib.rotate(padded, float(ang[a]))
+        x = rot_cache[a][:, col]
+        if f in (3, 4, 5, 6):
+            x = np.sqrt(x.astype(np.float32))
+        assert median_tie(x, int(ref_med[t, col, a]), int(got_med[t, col, a])), \
+            f"T{f} column {col} angle {a}: median {got_med[t, col, a]} vs {ref_med[t, col, a]}"
+        tie_cols.add((col, a, f in (3, 4, 5, 6)))
+        ties += 1
+    ok = close_mask(np.swapaxes(got, 1, 2), np.swapaxes(ref, 1, 2))   # per angle column
+    ok = np.swapaxes(ok, 1, 2)
+    for col, a, sq in tie_cols:
+        for t, f in enumerate(tfs):
+            if f != 0 and ((f in (3, 4, 5, 6)) == sq):
+                ok[t, col, a] = True
+    errs = rel_err(np.swapaxes(got, 1, 2), np.swapaxes(ref, 1, 2))
+    if report is not None:
+        report.update({"n": n, "ties": ties, "max_rel": float(errs.max()),
+                       "bad": int((~ok).sum()), "entries": int(ok.size)})
+    return got, ref, ok, ties
+
+
+@pytest.mark.parametrize("side,step", [(32, 2), (64, 3), (20, 1)])
+def test_sinograms_all_functionals_vs_oracle(oracle_lib, engine, side, step):
+    img = blob_image(side, side + 3, 5, (3, 12), (40, 200), 100 + side)
+    tfs = [0, 1, 2, 3, 4, 5, 6, 7]
+    rep = {}
+    got, ref, ok, ties = _check_sinograms(oracle_lib, engine, img, step, tfs, rep)
+    bad = np.argwhere(~ok)
+    assert ok.all(), f"{len(bad)} entries off, first {bad[:5].tolist()}; {rep}"
+    assert ties <= 0.01 * got[0].size
+
+
+def test_sinograms_single256_vs_oracle(oracle_lib, engine):
+    """The 256x256 workload (N = 363, 360 angles), T0-T5 as benchmarked."""
+    img = blob_image(256, 256, 8, (8, 40), (40, 200), 1)
+    rep = {}
+    got, ref, ok, ties = _check_sinograms(oracle_lib, engine, img, 1, [0, 1, 2, 3, 4, 5], rep)
+    assert ok.all(), rep
+    assert ties <= 0.002 * got[0].size, rep
+
+
+def test_circus_vs_oracle(oracle_lib):
+    img = blob_image(64, 64, 6, (3, 12), (40, 200), 7)
+    padded = oracle_lib.pad(img)
+    ang = oracle_lib.angles_for_step(2)
+    sino = oracle_lib.sinograms(padded, ang, [0, 1, 3])
+    n = padded.shape[0]
+    center = n // 2 - 3
+    pf_ref = [(1, 0, 0), (2, 0, 0), (3, 0, 0)] + [(0, o, center) for o in (1, 2, 3, 4, 5)]
+    pfs = [tt.PFunctionalWrapper.parse(s) for s in ("1", "2", "3", "H1", "H2", "H3", "H4", "H5")]
+    for p in pfs[3:]:
+        p.arguments.center = center
+    for t in range(sino.shape[0]):
+        ref = oracle_lib.circus(sino[t], pf_ref)
+        got = np.stack(tt.getCircusFunctions(sino[t], pfs))
+        ok = close_mask(got, ref)
+        assert ok.all(), (t, np.argwhere(~ok)[:5], rel_err(got, ref).max())
+
+
+def test_zscore_bit_exact(oracle_lib):
+    rng = np.random.default_rng(3)
+    for n in (2, 7, 360, 720):
+        x = (rng.random(n) * 100).astype(np.float32)
+        assert np.array_equal(tt.zscore(x), oracle_lib.zscore(x))
+
+
+@pytest.mark.parametrize("name", ["zeros", "const", "tiny3", "tiny5", "line1xN", "nonsquare"])
+def test_edge_images(oracle_lib, name):
+    imgs = {
+        "zeros": np.zeros((12, 12), np.float32, order="F"),
+        "const": np.full((9, 9), 0.5, np.float32, order="F"),
+        "tiny3": blob_image(3, 3, 1, (1, 2), (40, 200), 5),
+        "tiny5": blob_image(5, 5, 2, (1, 2), (40, 200), 6),
+        "line1xN": blob_image(1, 17, 2, (1, 3), (40, 200), 7),
+        "nonsquare": blob_image(40, 9, 3, (1, 4), (40, 200), 8),
+    }
+    img = imgs[name]
+    tfs = [0, 1, 2, 3, 4, 5, 6, 7]
+    ref = oracle_lib.transform(img, 5, tfs, [(1, 0), (2, 0), (3, 0)])
+    tr = tt.Transformer(img, name, 5, False)
+    sig = tr.getTransform([str(t) for t in tfs], P123, write_data=False)
+    ok = close_mask(tr.circus, ref["circus"])
+    assert ok.mean() >= 0.98, (name, (~ok).sum())
+    ok_s = close_mask(sig.T, ref["sig"].T, rtol=1e-3)
+    assert ok_s.mean() >= 0.98, (name, (~ok_s).sum())
+
+
+def test_orthonormal_mode_vs_oracle(oracle_lib):
+    img = blob_image(48, 48, 5, (3, 10), (40, 200), 21)
+    ref = oracle_lib.transform(img, 4, [0, 1], [(0, 1), (0, 2), (0, 3)])
+    tr = tt.Transformer(img, "ortho", 4, True)
+    tr.getTransform(["0", "1"], ["H1", "H2", "H3"], write_data=False)
+    ok = close_mask(tr.circus, ref["circus"], rtol=1e-3)
+    assert ok.mean() >= 0.97
+
+
+def test_invalid_arguments_raise():
+    with pytest.raises(ValueError):
+        tt.getSinograms(np.zeros((5, 6), np.float32), 1, ["0"])     # not square
+    with pytest.raises(tt.ValidationError):
+        tt.getSinograms(np.zeros((5, 5), np.float32), 1, ["9"])
+    with pytest.raises(tt.ValidationError):
+        tt.Transformer(np.zeros((5, 5), np.float32), "x", 1, False).getTransform(["0"], ["1", "H1"])

@@ -1,0 +1,315 @@
+"""Host API mirroring the reference's C++ interface for the sinogram + circus path.
+
+Names, argument meaning and error behaviour follow maleadt/tracetransform's
+c++/src:
+
+* ``TFunctionalWrapper.parse("0".."7")`` / ``PFunctionalWrapper.parse("1", "2",
+  "3", "H<order>")`` -- the ``operator>>`` parsers (sinogram.cpp:34-65,
+  circus.cpp:33-66); bad ids raise ``ValidationError``;
+* ``pad(image)`` -- auxiliary.cpp:257-275;
+* ``getSinograms(padded, angle_stepsize, tfunctionals)`` -- sinogram.cpp:67-178,
+  returns one N x A float32 matrix per T-functional;
+* ``getCircusFunctions(sinogram, pfunctionals)`` -- circus.cpp:104-177, returns
+  one length-A vector per P-functional;
+* ``zscore(vector)`` -- auxiliary.cpp:305-318;
+* ``Transformer(image, basename, angle_stepsize, orthonormal).getTransform(
+  tfunctionals, pfunctionals, write_data)`` -- transform.cpp:28-112, returning
+  the A x (nT * nP) signature matrix (and writing ``<basename>.csv`` when
+  ``write_data`` is true, as the reference does).
+
+Matrices are numpy float32 arrays of shape (rows, cols); they are handed to
+the engine in column-major (Eigen) order.  All compute runs on the GPU through
+libtt_gb300.so; there is no CPU implementation here.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _native
+from ._native import PFunctionalC, check, fptr, iptr, lib
+
+__all__ = [
+    "TFunctional", "PFunctional", "TFunctionalWrapper", "PFunctionalWrapper", "ValidationError",
+    "pad", "pad_geometry", "ortho_size", "angles_from_step", "getSinograms", "getCircusFunctions",
+    "zscore", "Transformer", "writecsv", "Plan",
+]
+
+
+class ValidationError(ValueError):
+    """boost::program_options::validation_error(invalid_option_value)."""
+
+
+class TFunctional(enum.IntEnum):
+    Radon = 0
+    T1 = 1
+    T2 = 2
+    T3 = 3
+    T4 = 4
+    T5 = 5
+    T6 = 6
+    T7 = 7
+
+
+class PFunctional(enum.IntEnum):
+    Hermite = 0
+    P1 = 1
+    P2 = 2
+    P3 = 3
+
+
+@dataclass
+class TFunctionalWrapper:
+    name: str
+    functional: TFunctional
+
+    @classmethod
+    def parse(cls, text: str) -> "TFunctionalWrapper":
+        """operator>>(istream, TFunctionalWrapper&) of c++/src/sinogram.cpp:34-65."""
+        names = {"0": "Radon", "1": "T1", "2": "T2", "3": "T3", "4": "T4", "5": "T5",
+                 "6": "T6", "7": "T7"}
+        if text not in names:
+            raise ValidationError(f"invalid T-functional {text!r}")
+        return cls(names[text], TFunctional(int(text)))
+
+
+@dataclass
+class PFunctionalArguments:
+    order: Optional[int] = None
+    center: Optional[int] = None
+
+
+@dataclass
+class PFunctionalWrapper:
+    name: str
+    functional: PFunctional
+    arguments: PFunctionalArguments = field(default_factory=PFunctionalArguments)
+
+    @classmethod
+    def parse(cls, text: str) -> "PFunctionalWrapper":
+        """operator>>(istream, PFunctionalWrapper&) of c++/src/circus.cpp:33-66."""
+        if text in ("1", "2", "3"):
+            return cls("P" + text, PFunctional(int(text)))
+        if text[:1] == "H":
+            if len(text) < 2:
+                raise ValidationError("Missing order parameter for Hermite P-functional")
+            digits = text[1:]
+            if not digits.isdigit():
+                raise ValidationError("Unparseable order parameter for Hermite P-functional")
+            return cls(text, PFunctional.Hermite, PFunctionalArguments(order=int(digits)))
+        raise ValidationError(f"invalid P-functional {text!r}")
+
+
+def _as_tfunctionals(tfunctionals) -> List[TFunctionalWrapper]:
+    out = []
+    for t in tfunctionals:
+        if isinstance(t, TFunctionalWrapper):
+            out.append(t)
+        elif isinstance(t, str):
+            out.append(TFunctionalWrapper.parse(t))
+        else:
+            out.append(TFunctionalWrapper.parse(str(int(t))))
+    return out
+
+
+def _as_pfunctionals(pfunctionals) -> List[PFunctionalWrapper]:
+    out = []
+    for p in pfunctionals:
+        if isinstance(p, PFunctionalWrapper):
+            out.append(p)
+        else:
+            out.append(PFunctionalWrapper.parse(str(p)))
+    return out
+
+
+class Plan:
+    """Owns one tt_plan (device tables, staging buffers, stream) of a device."""
+
+    def __init__(self, device: int = 0):
+        h = ctypes.c_void_p()
+        check(lib().tt_plan_create(ctypes.byref(h), int(device)))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            lib().tt_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synchronize(self):
+        check(lib().tt_plan_synchronize(self.handle))
+
+
+def _handle(plan: Optional[Plan]):
+    return plan.handle if plan is not None else None
+
+
+def _colmajor(a) -> np.ndarray:
+    """float32 copy of a 2-D matrix as a flat column-major buffer."""
+    a = np.asarray(a, dtype=np.float32)
+    if a.ndim != 2:
+        raise ValueError("expected a 2-D matrix")
+    return np.ascontiguousarray(a.ravel(order="F"))
+
+
+def pad_geometry(rows: int, cols: int):
+    """(N, row offset, col offset) of pad() (c++/src/auxiliary.cpp:257-275)."""
+    n, ro, co = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    check(lib().tt_pad_geometry(int(rows), int(cols), ctypes.byref(n), ctypes.byref(ro),
+                                ctypes.byref(co)))
+    return n.value, ro.value, co.value
+
+
+def pad(image) -> np.ndarray:
+    """Zero-pad to the N x N frame that holds every rotation of the image."""
+    image = np.asarray(image, dtype=np.float32)
+    n, ro, co = pad_geometry(*image.shape)
+    out = np.zeros((n, n), np.float32, order="F")
+    out[ro:ro + image.shape[0], co:co + image.shape[1]] = image
+    return out
+
+
+def ortho_size(angle_stepsize: int) -> int:
+    side = ctypes.c_int()
+    check(lib().tt_ortho_size(int(angle_stepsize), ctypes.byref(side)))
+    return side.value
+
+
+def angles_from_step(angle_stepsize: int) -> np.ndarray:
+    count = ctypes.c_int()
+    check(lib().tt_angles_from_step(int(angle_stepsize), None, 0, ctypes.byref(count)))
+    out = np.zeros(count.value, np.float32)
+    check(lib().tt_angles_from_step(int(angle_stepsize), fptr(out), count.value, ctypes.byref(count)))
+    return out
+
+
+def getSinograms(padded, angle_stepsize: int, tfunctionals: Sequence,
+                 plan: Optional[Plan] = None) -> List[np.ndarray]:
+    """One N x A sinogram per T-functional (c++/src/sinogram.cpp:67-178)."""
+    tfs = _as_tfunctionals(tfunctionals)
+    padded = np.asarray(padded, dtype=np.float32)
+    rows, cols = padded.shape
+    if int(angle_stepsize) < 1:
+        raise ValidationError("angle step must be >= 1")
+    a = 360 // int(angle_stepsize)
+    ids = np.array([int(t.functional) for t in tfs], np.int32)
+    out = np.zeros(len(tfs) * rows * a, np.float32)
+    check(lib().tt_sinograms(_handle(plan), fptr(_colmajor(padded)), rows, cols,
+                             int(angle_stepsize), iptr(ids), len(ids), fptr(out)))
+    stack = out.reshape(len(tfs), a, rows)
+    return [np.asfortranarray(stack[t].T) for t in range(len(tfs))]
+
+
+def _pf_array(pfs: List[PFunctionalWrapper]):
+    arr = (PFunctionalC * max(len(pfs), 1))()
+    for i, p in enumerate(pfs):
+        arr[i].kind = int(p.functional)
+        arr[i].order = -1 if p.arguments.order is None else int(p.arguments.order)
+        arr[i].center = -1 if p.arguments.center is None else int(p.arguments.center)
+    return arr
+
+
+def getCircusFunctions(sinogram, pfunctionals: Sequence,
+                       plan: Optional[Plan] = None) -> List[np.ndarray]:
+    """One length-A circus function per P-functional (c++/src/circus.cpp:104-177)."""
+    pfs = _as_pfunctionals(pfunctionals)
+    sinogram = np.asarray(sinogram, dtype=np.float32)
+    rows, cols = sinogram.shape
+    for p in pfs:
+        if p.functional == PFunctional.Hermite and (p.arguments.order is None or
+                                                    p.arguments.center is None):
+            raise ValidationError("Hermite P-functional needs an order and a center")
+    out = np.zeros(len(pfs) * cols, np.float32)
+    check(lib().tt_circus(_handle(plan), fptr(_colmajor(sinogram)), rows, cols, _pf_array(pfs),
+                          len(pfs), fptr(out)))
+    return [out[p * cols:(p + 1) * cols].copy() for p in range(len(pfs))]
+
+
+def rotate(image, angle_degrees: float, plan: Optional[Plan] = None) -> np.ndarray:
+    """rotate(image, ((cols-1)/2, (rows-1)/2), deg2rad(angle)) of
+    c++/src/auxiliary.cpp:223-255, bit-identical to the reference."""
+    image = np.asarray(image, dtype=np.float32)
+    rows, cols = image.shape
+    out = np.zeros(rows * cols, np.float32)
+    check(lib().tt_rotate(_handle(plan), fptr(_colmajor(image)), rows, cols,
+                          float(angle_degrees), fptr(out)))
+    return out.reshape((rows, cols), order="F")
+
+
+def zscore(vector, plan: Optional[Plan] = None) -> np.ndarray:
+    """(x - mean) / std with n - 1 (c++/src/auxiliary.cpp:305-318)."""
+    x = np.ascontiguousarray(np.asarray(vector, dtype=np.float32).ravel())
+    out = np.zeros_like(x)
+    if x.size:
+        check(lib().tt_zscore(_handle(plan), fptr(x), 1, x.size, fptr(out)))
+    return out
+
+
+def writecsv(filename: str, data) -> None:
+    """writecsv of c++/src/auxiliary.cpp:130-146: ", "-separated rows, floats
+    printed as a default C++ ostream prints them (6 significant digits)."""
+    data = np.asarray(data)
+    with open(filename, "w") as f:
+        for row in data:
+            f.write(", ".join(_ostream_float(float(v)) for v in row) + "\n")
+
+
+def _ostream_float(v: float) -> str:
+    if math.isnan(v):
+        return "-nan" if math.copysign(1.0, v) < 0 else "nan"
+    if math.isinf(v):
+        return "inf" if v > 0 else "-inf"
+    return "%g" % v
+
+
+class Transformer:
+    """Transformer of c++/src/transform.hpp:24-38 on the GPU engine."""
+
+    def __init__(self, image, basename: str, angle_stepsize: int, orthonormal: bool,
+                 plan: Optional[Plan] = None):
+        self._image = np.asarray(image, dtype=np.float32)
+        self._basename = basename
+        self._angle_stepsize = int(angle_stepsize)
+        self._orthonormal = bool(orthonormal)
+        self._plan = plan
+        if self._angle_stepsize < 1:
+            raise ValidationError("angle step must be >= 1")
+
+    def getTransform(self, tfunctionals: Sequence, pfunctionals: Sequence,
+                     write_data: bool = True) -> np.ndarray:
+        """Sinograms -> [nearest orthonormal sinogram] -> circus -> z-score.
+
+        Returns the A x (nT * nP) signature matrix; with write_data it is also
+        written to <basename>.csv.  Hermite centers of pfunctionals are
+        updated in place, as the reference does (transform.cpp:80-84)."""
+        tfs = _as_tfunctionals(tfunctionals)
+        pfs = _as_pfunctionals(pfunctionals)
+        n_h = sum(1 for p in pfs if p.functional == PFunctional.Hermite)
+        if n_h and n_h != len(pfs):
+            raise ValidationError("Cannot mix regular and orthonormal P-functionals")
+        if (n_h > 0) != self._orthonormal and pfs:
+            raise ValidationError("orthonormal mode must match the P-functionals")
+        rows, cols = self._image.shape
+        a = 360 // self._angle_stepsize
+        ids = np.array([int(t.functional) for t in tfs], np.int32)
+        circus = np.zeros(len(tfs) * len(pfs) * a, np.float32)
+        sig = np.zeros(len(tfs) * len(pfs) * a, np.float32)
+        check(lib().tt_transform(_handle(self._plan), fptr(_colmajor(self._image)), rows, cols,
+                                 self._angle_stepsize, iptr(ids), len(ids), _pf_array(pfs),
+                                 len(pfs), fptr(circus), fptr(sig)))
+        self.circus = circus.reshape(len(tfs), len(pfs), a)
+        signatures = sig.reshape(len(tfs) * len(pfs), a).T
+        if write_data and pfs:
+            writecsv(self._basename + ".csv", signatures)
+        return signatures

@@ -1,0 +1,883 @@
+// tt_api.cu -- C ABI of the trace-transform engine: plans, host-side tables,
+// and the drop-in and device entry points declared in include/tracetransform.h.
+//
+// Host-side tables are evaluated with the reference's own expressions so that
+// the device kernels see the reference's float values:
+//   rotation      cos/sin of -deg2rad(a) on a float   (c++/src/auxiliary.cpp:180, 227-237)
+//   T3, T4, T5    r^k * exp(i m log r) in double, rounded once (c++/src/functionals.cpp:136-198)
+//   P3 linspace   -1 + p * 2.0 / (N - 1) in double, rounded once (c++/src/functionals.cpp:346-355)
+//   Hermite       hermite_function with its double intermediates (c++/src/functionals.cpp:62-84, 369-386)
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "tracetransform.h"
+#include "tt_internal.h"
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+using tt::CircusArgs;
+using tt::SinoArgs;
+
+namespace {
+
+thread_local std::string g_error;
+
+tt_status fail(tt_status st, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_error = buf;
+    return st;
+}
+
+#define TT_CUDA(call)                                                          \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess)                                                 \
+            return fail(e_ == cudaErrorMemoryAllocation ? TT_ERR_OOM           \
+                                                        : TT_ERR_CUDA,         \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),       \
+                        __FILE__, __LINE__);                                   \
+    } while (0)
+
+#define TT_CHECK(expr)                                                         \
+    do {                                                                       \
+        tt_status s_ = (expr);                                                 \
+        if (s_ != TT_OK)                                                       \
+            return s_;                                                         \
+    } while (0)
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+struct FftTables {
+    int M = 0;
+    float2 *chirp = nullptr, *filt = nullptr, *twid = nullptr;
+    float *lin = nullptr;
+};
+
+// ---- host math -----------------------------------------------------------
+
+float deg2rad(float degrees) { return (float)(degrees * M_PI / 180); }
+
+void fft_pow2(std::vector<std::complex<double>> &a, int sign) {
+    const int n = (int)a.size();
+    for (int i = 1, j = 0; i < n; i++) {
+        int bit = n >> 1;
+        for (; j & bit; bit >>= 1)
+            j ^= bit;
+        j ^= bit;
+        if (i < j)
+            std::swap(a[i], a[j]);
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+        for (int i = 0; i < n; i += len) {
+            for (int k = 0; k < len / 2; k++) {
+                const double ang = sign * 2.0 * M_PI * k / len;
+                const std::complex<double> w(std::cos(ang), std::sin(ang));
+                const std::complex<double> u = a[i + k], v = a[i + k + len / 2] * w;
+                a[i + k] = u + v;
+                a[i + k + len / 2] = u - v;
+            }
+        }
+    }
+}
+
+float hermite_polynomial(unsigned order, float x) {
+    switch (order) {
+    case 0:
+        return 1.0f;
+    case 1:
+        return (float)(2.0 * x);
+    default:
+        return (float)(2.0 * x * hermite_polynomial(order - 1, x) -
+                       2.0 * (order - 1) * hermite_polynomial(order - 2, x));
+    }
+}
+
+unsigned factorial(unsigned n) { return (n == 1 || n == 0) ? 1 : factorial(n - 1) * n; }
+
+float hermite_function(unsigned order, float x) {
+    const float half_sq = x * x / 2;
+    return (float)(hermite_polynomial(order, x) /
+                   (std::sqrt(std::pow(2.0, (double)order) * factorial(order) *
+                              std::sqrt(M_PI)) *
+                    std::exp((double)half_sq)));
+}
+
+// The basis psi(order, z(p)) that PFunctionalHermite multiplies the column by.
+std::vector<float> hermite_basis(int n, unsigned order, int center) {
+    std::vector<float> b(n);
+    const float lower = (float)(10.0 / center);
+    const float upper = (float)(10.0 / (n - 1 - center));
+    for (int p = 0; p < n; p++) {
+        float z;
+        if (p < center)
+            z = p * lower - 10;
+        else
+            z = (p - center) * upper;
+        b[p] = hermite_function(order, z);
+    }
+    return b;
+}
+
+void pad_geometry(int rows, int cols, int *n, int *row_off, int *col_off) {
+    const float ox = (float)(std::floor((cols + 1) / 2.0) - 1);
+    const float oy = (float)(std::floor((rows + 1) / 2.0) - 1);
+    const float hx = (float)(cols - 1) - ox - 1;
+    const float hy = (float)(rows - 1) - oy - 1;
+    const int r_last = (int)std::ceil(std::hypot(hx, hy)) + 1;
+    const int nb = 2 * r_last + 1;
+    const float opad = (float)(std::floor((nb + 1) / 2.0) - 1);
+    *n = nb;
+    *col_off = (int)(opad - ox);
+    *row_off = (int)(opad - oy);
+}
+
+int ortho_side(unsigned step) {
+    const size_t ndiag = (int)std::ceil(360.0 / step);
+    return (int)std::ceil(ndiag / std::sqrt(2));
+}
+
+// resize() of c++/src/auxiliary.cpp:198-221 (the orthonormal mode's stretch).
+std::vector<float> resize_image(const float *in, int in_rows, int in_cols, int rows, int cols) {
+    std::vector<float> out((size_t)rows * cols, 0.f);
+    const float t00 = ((float)in_rows) / rows, t11 = ((float)in_cols) / cols;
+    for (int col = 1; col < cols - 1; col++) {
+        for (int row = 1; row < rows - 1; row++) {
+            const float px = (float)col + 0.5f, py = (float)row + 0.5f;
+            float qx = px * t00 + py * 0.0f, qy = px * 0.0f + py * t11;
+            qx = qx - 0.5f;
+            qy = qy - 0.5f;
+            if (qx < 0 || qy < 0 || qx >= in_cols - 1 || qy >= in_rows - 1)
+                continue;
+            float xi, yi;
+            const float xf = std::modf(qx, &xi), yf = std::modf(qy, &yi);
+            const size_t x0 = (size_t)xi, y0 = (size_t)yi;
+            const float s00 = in[y0 + x0 * in_rows], s01 = in[y0 + (x0 + 1) * in_rows];
+            const float s10 = in[y0 + 1 + x0 * in_rows], s11 = in[y0 + 1 + (x0 + 1) * in_rows];
+            out[(size_t)row + (size_t)col * rows] = s00 * (1 - xf) * (1 - yf) +
+                                                    s01 * xf * (1 - yf) +
+                                                    s10 * (1 - xf) * yf + s11 * xf * yf;
+        }
+    }
+    return out;
+}
+
+int find_weighted_median(const float *x, int n) {
+    float sum = 0.f;
+    for (int i = 0; i < n; i++)
+        sum += x[i];
+    float integral = 0.f;
+    for (int i = 0; i < n; i++) {
+        integral += x[i];
+        if (2 * integral >= sum)
+            return i;
+    }
+    return n - 1;
+}
+
+// Nearest orthonormal sinogram (c++/src/circus.cpp:68-102): per-column median
+// offsets, alignment into (rows + padding) x cols, then the polar factor
+// U V^T of the aligned matrix, here from a one-sided Jacobi SVD in double.
+tt_status nearest_orthonormal(const float *sino, int rows, int cols, std::vector<float> &out,
+                              int *out_rows, int *new_center) {
+    const int center = (int)std::floor((rows - 1) / 2.0);
+    std::vector<int> offset(cols);
+    for (int p = 0; p < cols; p++)
+        offset[p] = find_weighted_median(sino + (size_t)p * rows, rows) - center;
+    const int mn = *std::min_element(offset.begin(), offset.end());
+    const int mx = *std::max_element(offset.begin(), offset.end());
+    const int m = rows + std::abs(mx) + std::abs(mn);
+    if (m < cols)
+        return fail(TT_ERR_UNSUPPORTED,
+                    "nearest orthonormal sinogram needs at least as many rows (%d) as angles (%d)",
+                    m, cols);
+    *new_center = center + mx;
+    *out_rows = m;
+    std::vector<double> a((size_t)m * cols, 0.0), v((size_t)cols * cols, 0.0);
+    for (int col = 0; col < cols; col++)
+        for (int row = 0; row < rows; row++)
+            a[(size_t)(mx + row - offset[col]) + (size_t)col * m] = sino[(size_t)row + (size_t)col * rows];
+    for (int i = 0; i < cols; i++)
+        v[(size_t)i * cols + i] = 1.0;
+    for (int sweep = 0; sweep < 60; sweep++) {
+        double off = 0.0;
+        for (int p = 0; p < cols - 1; p++) {
+            for (int q = p + 1; q < cols; q++) {
+                double *ap = &a[(size_t)p * m], *aq = &a[(size_t)q * m];
+                double al = 0, be = 0, ga = 0;
+                for (int i = 0; i < m; i++) {
+                    al += ap[i] * ap[i];
+                    be += aq[i] * aq[i];
+                    ga += ap[i] * aq[i];
+                }
+                if (ga == 0 || std::fabs(ga) <= 1e-15 * std::sqrt(al * be))
+                    continue;
+                off = std::max(off, std::fabs(ga) / std::sqrt(al * be));
+                const double zeta = (be - al) / (2 * ga);
+                const double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1 + zeta * zeta));
+                const double c = 1 / std::sqrt(1 + t * t), s = c * t;
+                for (int i = 0; i < m; i++) {
+                    const double x = ap[i], y = aq[i];
+                    ap[i] = c * x - s * y;
+                    aq[i] = s * x + c * y;
+                }
+                double *vp = &v[(size_t)p * cols], *vq = &v[(size_t)q * cols];
+                for (int i = 0; i < cols; i++) {
+                    const double x = vp[i], y = vq[i];
+                    vp[i] = c * x - s * y;
+                    vq[i] = s * x + c * y;
+                }
+            }
+        }
+        if (off < 1e-15)
+            break;
+    }
+    for (int k = 0; k < cols; k++) {
+        double nrm = 0;
+        double *ak = &a[(size_t)k * m];
+        for (int i = 0; i < m; i++)
+            nrm += ak[i] * ak[i];
+        nrm = std::sqrt(nrm);
+        for (int i = 0; i < m; i++)
+            ak[i] = nrm > 0 ? ak[i] / nrm : 0.0;
+    }
+    out.assign((size_t)m * cols, 0.f);
+    for (int j = 0; j < cols; j++)
+        for (int i = 0; i < m; i++) {
+            double acc = 0;
+            for (int k = 0; k < cols; k++)
+                acc += a[i + (size_t)k * m] * v[j + (size_t)k * cols];
+            out[i + (size_t)j * m] = (float)acc;
+        }
+    return TT_OK;
+}
+
+} // namespace
+
+// ---- the plan ----------------------------------------------------------------
+
+struct tt_plan {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::map<int, float2 *> t345;                       // n -> 3 x n
+    std::map<int, FftTables> fft;                       // n -> P3 tables
+    std::map<std::tuple<int, int, int>, float *> herm;  // (n, order, center)
+    std::map<std::vector<float>, float2 *> trig;        // angle list -> (c, s)
+    std::map<std::vector<long>, const float **> herm_ptrs;
+    DevBuf in, sino, circ, sig, region, nos;
+    std::vector<void *> owned;
+
+    ~tt_plan() {
+        int prev = 0;
+        cudaGetDevice(&prev);
+        cudaSetDevice(device);
+        if (stream)
+            cudaStreamSynchronize(stream);
+        for (void *p : owned)
+            cudaFree(p);
+        for (DevBuf *b : {&in, &sino, &circ, &sig, &region, &nos})
+            cudaFree(b->p);
+        if (stream)
+            cudaStreamDestroy(stream);
+        cudaSetDevice(prev);
+    }
+
+    tt_status alloc(void **p, size_t bytes) {
+        TT_CUDA(cudaMalloc(p, bytes > 0 ? bytes : 1));
+        owned.push_back(*p);
+        return TT_OK;
+    }
+    tt_status ensure(DevBuf &b, size_t bytes) {
+        if (b.bytes >= bytes && b.p)
+            return TT_OK;
+        if (b.p) {
+            TT_CUDA(cudaStreamSynchronize(stream));
+            cudaFree(b.p);
+            b.p = nullptr;
+            b.bytes = 0;
+        }
+        TT_CUDA(cudaMalloc(&b.p, bytes > 0 ? bytes : 1));
+        b.bytes = bytes;
+        return TT_OK;
+    }
+    // Tables are created once and read by kernels on any stream, so the copy
+    // completes before the table is handed out.
+    template <typename T> tt_status upload(T **dst, const std::vector<T> &h) {
+        TT_CHECK(alloc((void **)dst, sizeof(T) * h.size()));
+        TT_CUDA(cudaMemcpyAsync(*dst, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, stream));
+        TT_CUDA(cudaStreamSynchronize(stream));
+        return TT_OK;
+    }
+
+    tt_status get_trig(const float *angles, int n_angles, const float2 **out) {
+        std::vector<float> key(angles, angles + n_angles);
+        auto it = trig.find(key);
+        if (it != trig.end()) {
+            *out = it->second;
+            return TT_OK;
+        }
+        std::vector<float2> h(n_angles);
+        for (int a = 0; a < n_angles; a++) {
+            const float ang = deg2rad(angles[a]);
+            h[a] = make_float2(std::cos(-ang), std::sin(-ang));
+        }
+        float2 *d;
+        TT_CHECK(upload(&d, h));
+        trig[key] = d;
+        *out = d;
+        return TT_OK;
+    }
+
+    tt_status get_t345(int n, const float2 **out) {
+        auto it = t345.find(n);
+        if (it != t345.end()) {
+            *out = it->second;
+            return TT_OK;
+        }
+        std::vector<float2> h((size_t)3 * n, make_float2(0.f, 0.f));
+        for (int r = 1; r < n; r++) {
+            h[r] = make_float2((float)(r * std::cos(5.0 * std::log((double)r))),
+                               (float)(r * std::sin(5.0 * std::log((double)r))));
+            h[n + r] = make_float2((float)std::cos(3.0 * std::log((double)r)),
+                                   (float)std::sin(3.0 * std::log((double)r)));
+            h[2 * n + r] = make_float2((float)(std::sqrt((double)r) * std::cos(4.0 * std::log((double)r))),
+                                       (float)(std::sqrt((double)r) * std::sin(4.0 * std::log((double)r))));
+        }
+        float2 *d;
+        TT_CHECK(upload(&d, h));
+        t345[n] = d;
+        *out = d;
+        return TT_OK;
+    }
+
+    tt_status get_fft(int n, const FftTables **out) {
+        auto it = fft.find(n);
+        if (it != fft.end()) {
+            *out = &it->second;
+            return TT_OK;
+        }
+        FftTables t;
+        int M = 2;
+        while (M < 2 * n - 1)
+            M <<= 1;
+        t.M = M;
+        std::vector<float2> chirp(n), filt(M), twid(M / 2);
+        std::vector<std::complex<double>> w(n), b(M, 0.0);
+        for (int j = 0; j < n; j++) {
+            const long q = ((long)j * j) % (2L * n);
+            w[j] = std::complex<double>(std::cos(M_PI * q / n), -std::sin(M_PI * q / n));
+            chirp[j] = make_float2((float)w[j].real(), (float)w[j].imag());
+        }
+        b[0] = std::conj(w[0]);
+        for (int j = 1; j < n; j++)
+            b[j] = b[M - j] = std::conj(w[j]);
+        fft_pow2(b, -1);
+        for (int i = 0; i < M; i++)
+            filt[i] = make_float2((float)(b[i].real() / M), (float)(b[i].imag() / M));
+        for (int k = 0; k < M / 2; k++)
+            twid[k] = make_float2((float)std::cos(-2.0 * M_PI * k / M), (float)std::sin(-2.0 * M_PI * k / M));
+        std::vector<float> lin(n);
+        for (int p = 0; p < n; p++)
+            lin[p] = (float)(-1 + p * 2.0 / (n - 1));
+        TT_CHECK(upload(&t.chirp, chirp));
+        TT_CHECK(upload(&t.filt, filt));
+        TT_CHECK(upload(&t.twid, twid));
+        TT_CHECK(upload(&t.lin, lin));
+        fft[n] = t;
+        *out = &fft[n];
+        return TT_OK;
+    }
+
+    tt_status get_herm(int n, int order, int center, const float **out) {
+        auto key = std::make_tuple(n, order, center);
+        auto it = herm.find(key);
+        if (it != herm.end()) {
+            *out = it->second;
+            return TT_OK;
+        }
+        float *d;
+        TT_CHECK(upload(&d, hermite_basis(n, (unsigned)order, center)));
+        herm[key] = d;
+        *out = d;
+        return TT_OK;
+    }
+};
+
+namespace {
+
+std::mutex g_default_mu;
+std::map<int, tt_plan *> g_default;
+
+tt_status resolve_plan(tt_plan *plan, tt_plan **out) {
+    if (plan) {
+        *out = plan;
+        TT_CUDA(cudaSetDevice(plan->device));
+        return TT_OK;
+    }
+    int dev = 0;
+    TT_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_default_mu);
+    auto it = g_default.find(dev);
+    if (it == g_default.end()) {
+        tt_plan *p = nullptr;
+        TT_CHECK(tt_plan_create(&p, dev));
+        g_default[dev] = p;
+        *out = p;
+    } else {
+        *out = it->second;
+    }
+    return TT_OK;
+}
+
+cudaStream_t pick_stream(tt_plan *p, void *stream) {
+    return stream ? (cudaStream_t)stream : p->stream;
+}
+
+tt_status check_tfuncs(const int32_t *tfuncs, int n_t, unsigned *need) {
+    if (n_t < 0 || n_t > tt::kMaxT)
+        return fail(TT_ERR_INVALID_ARG, "between 0 and %d T-functionals are supported, got %d",
+                    tt::kMaxT, n_t);
+    if (n_t > 0 && !tfuncs)
+        return fail(TT_ERR_INVALID_ARG, "tfuncs is NULL");
+    *need = 0;
+    for (int t = 0; t < n_t; t++) {
+        if (tfuncs[t] < 0 || tfuncs[t] > 7)
+            return fail(TT_ERR_INVALID_ARG, "invalid T-functional id %d (valid: 0..7)", tfuncs[t]);
+        *need |= 1u << tfuncs[t];
+    }
+    return TT_OK;
+}
+
+tt_status check_pfuncs(const tt_pfunctional *pf, int n_p, bool need_center, unsigned *need) {
+    if (n_p < 0 || n_p > tt::kMaxP)
+        return fail(TT_ERR_INVALID_ARG, "between 0 and %d P-functionals are supported, got %d",
+                    tt::kMaxP, n_p);
+    if (n_p > 0 && !pf)
+        return fail(TT_ERR_INVALID_ARG, "pfuncs is NULL");
+    *need = 0;
+    for (int p = 0; p < n_p; p++) {
+        if (pf[p].kind < 0 || pf[p].kind > 3)
+            return fail(TT_ERR_INVALID_ARG, "invalid P-functional kind %d", pf[p].kind);
+        if (pf[p].kind == TT_P_HERMITE) {
+            if (pf[p].order < 0)
+                return fail(TT_ERR_INVALID_ARG, "Hermite P-functional needs an order >= 0");
+            if (need_center && pf[p].center < 0)
+                return fail(TT_ERR_INVALID_ARG, "Hermite P-functional needs a center");
+        }
+        *need |= 1u << pf[p].kind;
+    }
+    return TT_OK;
+}
+
+std::vector<float> step_angles(unsigned step) {
+    const int k = (int)std::floor(360 / step);
+    std::vector<float> a(k);
+    for (int i = 0; i < k; i++)
+        a[i] = (float)(i * step);
+    return a;
+}
+
+// Sinograms of a region placed in an n x n frame (device pointers).
+tt_status run_sinograms(tt_plan *p, const float *d_src, int src_rows, int src_cols, int src_ld,
+                        int n, int row_off, int col_off, const int *d_region,
+                        const float *angles, int n_angles, const int32_t *tfuncs, int n_t,
+                        unsigned need, float *d_out, int32_t *d_medians, cudaStream_t st) {
+    if (n_angles == 0 || n_t == 0 || n == 0)
+        return TT_OK;
+    SinoArgs a{};
+    a.src = d_src;
+    a.src_rows = src_rows;
+    a.src_cols = src_cols;
+    a.src_ld = src_ld;
+    a.row_off = row_off;
+    a.col_off = col_off;
+    a.dyn_region = d_region;
+    a.n = n;
+    a.n_angles = n_angles;
+    TT_CHECK(p->get_trig(angles, n_angles, &a.trig));
+    a.tab = nullptr;
+    if (need & ((1u << 3) | (1u << 4) | (1u << 5)))
+        TT_CHECK(p->get_t345(n, &a.tab));
+    a.out = d_out;
+    a.medians = d_medians;
+    a.n_t = n_t;
+    for (int t = 0; t < n_t; t++)
+        a.tf[t] = tfuncs[t];
+    a.need = need;
+    const int L = tt::sino_lines_per_block();
+    a.stride = tt::sino_stride(n, L);
+    if (tt::sino_smem_bytes(n, L) > 227 * 1024)
+        return fail(TT_ERR_UNSUPPORTED, "padded side %d exceeds the shared-memory line buffer", n);
+    TT_CUDA(tt::launch_sinograms(a, st));
+    return TT_OK;
+}
+
+tt_status run_circus(tt_plan *p, const float *d_sino, int rows, int cols, int n_sino,
+                     const tt_pfunctional *pf, int n_p, const int32_t *centers, unsigned need,
+                     float *d_out, cudaStream_t st) {
+    if (n_p == 0 || cols == 0 || n_sino == 0)
+        return TT_OK;
+    if (rows <= 0)
+        return fail(TT_ERR_INVALID_ARG, "sinograms need at least one row");
+    CircusArgs a{};
+    a.sino = d_sino;
+    a.rows = rows;
+    a.cols = cols;
+    a.n_sino = n_sino;
+    a.n_p = n_p;
+    for (int i = 0; i < n_p; i++)
+        a.kind[i] = pf[i].kind;
+    a.need = need;
+    a.out = d_out;
+    int sl = 1;
+    while (sl < rows)
+        sl <<= 1;
+    a.sort_len = sl;
+    if (need & (1u << 3)) {
+        const FftTables *f;
+        TT_CHECK(p->get_fft(rows, &f));
+        a.M = f->M;
+        a.chirp = f->chirp;
+        a.filt = f->filt;
+        a.twid = f->twid;
+        a.lin = f->lin;
+    }
+    if (need & 1u) {
+        std::vector<long> key;
+        key.push_back(rows);
+        std::vector<const float *> ptrs((size_t)n_sino * n_p, nullptr);
+        for (int s = 0; s < n_sino; s++)
+            for (int i = 0; i < n_p; i++) {
+                if (pf[i].kind != TT_P_HERMITE)
+                    continue;
+                const int center = centers ? centers[s] : pf[i].center;
+                if (center < 0)
+                    return fail(TT_ERR_INVALID_ARG, "Hermite P-functional needs a center");
+                const float *b;
+                TT_CHECK(p->get_herm(rows, pf[i].order, center, &b));
+                ptrs[(size_t)s * n_p + i] = b;
+                key.push_back(((long)s * n_p + i) * 1000003L + pf[i].order * 100003L + center);
+            }
+        auto it = p->herm_ptrs.find(key);
+        if (it == p->herm_ptrs.end()) {
+            const float **d;
+            TT_CHECK(p->upload(&d, ptrs));
+            p->herm_ptrs[key] = d;
+            a.herm = d;
+        } else {
+            a.herm = it->second;
+        }
+    }
+    if (tt::circus_smem_bytes(a) > 227 * 1024)
+        return fail(TT_ERR_UNSUPPORTED, "sinogram length %d exceeds the shared-memory column buffers",
+                    rows);
+    TT_CUDA(tt::launch_circus(a, st));
+    return TT_OK;
+}
+
+} // namespace
+
+// ---- C ABI ---------------------------------------------------------------------
+
+extern "C" {
+
+const char *tt_last_error(void) { return g_error.c_str(); }
+
+const char *tt_version(void) { return "tracetransform-gb300 0.1 (sm_103a)"; }
+
+tt_status tt_plan_create(tt_plan **plan, int device) {
+    if (!plan)
+        return fail(TT_ERR_INVALID_ARG, "plan is NULL");
+    int count = 0;
+    TT_CUDA(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count)
+        return fail(TT_ERR_INVALID_ARG, "device %d out of range (%d devices)", device, count);
+    TT_CUDA(cudaSetDevice(device));
+    tt_plan *p = new tt_plan();
+    p->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete p;
+        return fail(TT_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    *plan = p;
+    return TT_OK;
+}
+
+tt_status tt_plan_destroy(tt_plan *plan) {
+    if (!plan)
+        return TT_OK;
+    {
+        std::lock_guard<std::mutex> lock(g_default_mu);
+        for (auto it = g_default.begin(); it != g_default.end(); ++it)
+            if (it->second == plan) {
+                g_default.erase(it);
+                break;
+            }
+    }
+    delete plan;
+    return TT_OK;
+}
+
+tt_status tt_plan_synchronize(tt_plan *plan) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    TT_CUDA(cudaStreamSynchronize(p->stream));
+    return TT_OK;
+}
+
+tt_status tt_pad_geometry(int rows, int cols, int *n, int *row_off, int *col_off) {
+    if (rows <= 0 || cols <= 0 || !n || !row_off || !col_off)
+        return fail(TT_ERR_INVALID_ARG, "pad geometry needs a non-empty image and output pointers");
+    pad_geometry(rows, cols, n, row_off, col_off);
+    return TT_OK;
+}
+
+tt_status tt_ortho_size(unsigned step, int *side) {
+    if (step == 0 || !side)
+        return fail(TT_ERR_INVALID_ARG, "angle step must be >= 1");
+    *side = ortho_side(step);
+    return TT_OK;
+}
+
+tt_status tt_angles_from_step(unsigned step, float *angles, int capacity, int *count) {
+    if (step == 0 || !count)
+        return fail(TT_ERR_INVALID_ARG, "angle step must be >= 1");
+    std::vector<float> a = step_angles(step);
+    *count = (int)a.size();
+    if (angles) {
+        if (capacity < (int)a.size())
+            return fail(TT_ERR_INVALID_ARG, "angle buffer holds %d, need %d", capacity, (int)a.size());
+        std::copy(a.begin(), a.end(), angles);
+    }
+    return TT_OK;
+}
+
+tt_status tt_sinograms_device(tt_plan *plan, const float *d_src, int src_rows, int src_cols,
+                              int src_ld, int n, int row_off, int col_off,
+                              const float *angles_deg, int n_angles, const int32_t *tfuncs,
+                              int n_t, float *d_out, int32_t *d_medians, void *stream) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    unsigned need;
+    TT_CHECK(check_tfuncs(tfuncs, n_t, &need));
+    if (n <= 0 || src_rows < 0 || src_cols < 0 || src_ld < src_rows || row_off < 0 || col_off < 0 ||
+        row_off + src_rows > n || col_off + src_cols > n)
+        return fail(TT_ERR_INVALID_ARG, "source region %dx%d at (%d,%d) does not fit a %dx%d frame",
+                    src_rows, src_cols, row_off, col_off, n, n);
+    if (n_angles < 0 || (n_angles > 0 && !angles_deg))
+        return fail(TT_ERR_INVALID_ARG, "bad angle list");
+    if (!d_out || (src_rows * src_cols > 0 && !d_src))
+        return fail(TT_ERR_INVALID_ARG, "NULL device buffer");
+    return run_sinograms(p, d_src, src_rows, src_cols, src_ld, n, row_off, col_off, nullptr,
+                         angles_deg, n_angles, tfuncs, n_t, need, d_out, d_medians,
+                         pick_stream(p, stream));
+}
+
+tt_status tt_circus_device(tt_plan *plan, const float *d_sino, int rows, int cols, int n_sino,
+                           const tt_pfunctional *pfuncs, int n_p, const int32_t *centers,
+                           float *d_out, void *stream) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    unsigned need;
+    TT_CHECK(check_pfuncs(pfuncs, n_p, centers == nullptr, &need));
+    if (rows <= 0 || cols < 0 || n_sino < 0 || !d_sino || !d_out)
+        return fail(TT_ERR_INVALID_ARG, "bad sinogram stack %dx%dx%d", n_sino, rows, cols);
+    return run_circus(p, d_sino, rows, cols, n_sino, pfuncs, n_p, centers, need, d_out,
+                      pick_stream(p, stream));
+}
+
+tt_status tt_zscore_device(tt_plan *plan, const float *d_in, int n_vec, int len, float *d_out,
+                           void *stream) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    if (n_vec < 0 || len < 0 || (n_vec * len > 0 && (!d_in || !d_out)))
+        return fail(TT_ERR_INVALID_ARG, "bad z-score arguments");
+    TT_CUDA(tt::launch_zscore(d_in, n_vec, len, d_out, pick_stream(p, stream)));
+    return TT_OK;
+}
+
+tt_status tt_sinograms(tt_plan *plan, const float *padded, int rows, int cols,
+                       unsigned angle_stepsize, const int32_t *tfuncs, int n_t, float *out) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    if (rows != cols)
+        return fail(TT_ERR_INVALID_ARG, "getSinograms needs a square (padded) image, got %dx%d",
+                    rows, cols);
+    if (rows <= 0 || !padded || !out)
+        return fail(TT_ERR_INVALID_ARG, "empty image or NULL buffer");
+    if (angle_stepsize == 0)
+        return fail(TT_ERR_INVALID_ARG, "angle step must be >= 1");
+    unsigned need;
+    TT_CHECK(check_tfuncs(tfuncs, n_t, &need));
+    const int n = rows;
+    std::vector<float> ang = step_angles(angle_stepsize);
+    const size_t out_elems = (size_t)n_t * n * ang.size();
+    TT_CHECK(p->ensure(p->in, sizeof(float) * (size_t)n * n));
+    TT_CHECK(p->ensure(p->sino, sizeof(float) * std::max<size_t>(out_elems, 1)));
+    TT_CHECK(p->ensure(p->region, 4 * sizeof(int)));
+    cudaStream_t st = p->stream;
+    TT_CUDA(cudaMemcpyAsync(p->in.p, padded, sizeof(float) * (size_t)n * n, cudaMemcpyHostToDevice, st));
+    // sample only where the padded frame holds non-zero pixels
+    TT_CUDA(tt::launch_region_bbox((const float *)p->in.p, n, (int *)p->region.p, st));
+    TT_CHECK(run_sinograms(p, (const float *)p->in.p, n, n, n, n, 0, 0, (const int *)p->region.p,
+                           ang.data(), (int)ang.size(), tfuncs, n_t, need, (float *)p->sino.p,
+                           nullptr, st));
+    TT_CUDA(cudaMemcpyAsync(out, p->sino.p, sizeof(float) * out_elems, cudaMemcpyDeviceToHost, st));
+    TT_CUDA(cudaStreamSynchronize(st));
+    return TT_OK;
+}
+
+tt_status tt_circus(tt_plan *plan, const float *sinogram, int rows, int cols,
+                    const tt_pfunctional *pfuncs, int n_p, float *out) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    unsigned need;
+    TT_CHECK(check_pfuncs(pfuncs, n_p, true, &need));
+    if (rows <= 0 || cols < 0 || !sinogram || !out)
+        return fail(TT_ERR_INVALID_ARG, "bad sinogram %dx%d", rows, cols);
+    cudaStream_t st = p->stream;
+    TT_CHECK(p->ensure(p->sino, sizeof(float) * std::max<size_t>((size_t)rows * cols, 1)));
+    TT_CHECK(p->ensure(p->circ, sizeof(float) * std::max<size_t>((size_t)n_p * cols, 1)));
+    TT_CUDA(cudaMemcpyAsync(p->sino.p, sinogram, sizeof(float) * (size_t)rows * cols,
+                            cudaMemcpyHostToDevice, st));
+    TT_CHECK(run_circus(p, (const float *)p->sino.p, rows, cols, 1, pfuncs, n_p, nullptr, need,
+                        (float *)p->circ.p, st));
+    TT_CUDA(cudaMemcpyAsync(out, p->circ.p, sizeof(float) * (size_t)n_p * cols, cudaMemcpyDeviceToHost, st));
+    TT_CUDA(cudaStreamSynchronize(st));
+    return TT_OK;
+}
+
+tt_status tt_rotate(tt_plan *plan, const float *image, int rows, int cols, float angle_deg,
+                    float *out) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    if (rows <= 0 || cols <= 0 || !image || !out)
+        return fail(TT_ERR_INVALID_ARG, "bad image %dx%d", rows, cols);
+    const size_t elems = (size_t)rows * cols;
+    cudaStream_t st = p->stream;
+    TT_CHECK(p->ensure(p->in, sizeof(float) * elems));
+    TT_CHECK(p->ensure(p->sino, sizeof(float) * elems));
+    TT_CUDA(cudaMemcpyAsync(p->in.p, image, sizeof(float) * elems, cudaMemcpyHostToDevice, st));
+    const float ang = deg2rad(angle_deg);
+    TT_CUDA(tt::launch_rotate((const float *)p->in.p, rows, cols, std::cos(-ang), std::sin(-ang),
+                              (float *)p->sino.p, st));
+    TT_CUDA(cudaMemcpyAsync(out, p->sino.p, sizeof(float) * elems, cudaMemcpyDeviceToHost, st));
+    TT_CUDA(cudaStreamSynchronize(st));
+    return TT_OK;
+}
+
+tt_status tt_zscore(tt_plan *plan, const float *in, int n_vec, int len, float *out) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    if (n_vec < 0 || len < 0 || (n_vec * len > 0 && (!in || !out)))
+        return fail(TT_ERR_INVALID_ARG, "bad z-score arguments");
+    const size_t elems = (size_t)n_vec * len;
+    if (elems == 0)
+        return TT_OK;
+    cudaStream_t st = p->stream;
+    TT_CHECK(p->ensure(p->circ, sizeof(float) * elems));
+    TT_CHECK(p->ensure(p->sig, sizeof(float) * elems));
+    TT_CUDA(cudaMemcpyAsync(p->circ.p, in, sizeof(float) * elems, cudaMemcpyHostToDevice, st));
+    TT_CUDA(tt::launch_zscore((const float *)p->circ.p, n_vec, len, (float *)p->sig.p, st));
+    TT_CUDA(cudaMemcpyAsync(out, p->sig.p, sizeof(float) * elems, cudaMemcpyDeviceToHost, st));
+    TT_CUDA(cudaStreamSynchronize(st));
+    return TT_OK;
+}
+
+tt_status tt_transform(tt_plan *plan, const float *image, int rows, int cols,
+                       unsigned angle_stepsize, const int32_t *tfuncs, int n_t,
+                       const tt_pfunctional *pfuncs, int n_p, float *circus, float *signatures) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    if (rows <= 0 || cols <= 0 || !image)
+        return fail(TT_ERR_INVALID_ARG, "empty image");
+    if (angle_stepsize == 0)
+        return fail(TT_ERR_INVALID_ARG, "angle step must be >= 1");
+    unsigned tneed, pneed;
+    TT_CHECK(check_tfuncs(tfuncs, n_t, &tneed));
+    TT_CHECK(check_pfuncs(pfuncs, n_p, false, &pneed));
+    int n_herm = 0;
+    for (int i = 0; i < n_p; i++)
+        n_herm += pfuncs[i].kind == TT_P_HERMITE;
+    if (n_herm != 0 && n_herm != n_p)
+        return fail(TT_ERR_INVALID_ARG, "Cannot mix regular and orthonormal P-functionals");
+    const bool ortho = n_herm > 0;
+
+    // Transformer::Transformer: optional stretch, then padding (implicit here)
+    std::vector<float> stretched;
+    const float *img = image;
+    int ir = rows, ic = cols;
+    if (ortho) {
+        const int side = ortho_side(angle_stepsize);
+        stretched = resize_image(image, rows, cols, side, side);
+        img = stretched.data();
+        ir = ic = side;
+    }
+    int n, ro, co;
+    pad_geometry(ir, ic, &n, &ro, &co);
+    std::vector<float> ang = step_angles(angle_stepsize);
+    const int A = (int)ang.size();
+    const size_t sino_elems = (size_t)n_t * n * A, circ_elems = (size_t)n_t * n_p * A;
+    cudaStream_t st = p->stream;
+    TT_CHECK(p->ensure(p->in, sizeof(float) * (size_t)ir * ic));
+    TT_CHECK(p->ensure(p->sino, sizeof(float) * std::max<size_t>(sino_elems, 1)));
+    TT_CHECK(p->ensure(p->circ, sizeof(float) * std::max<size_t>(circ_elems, 1)));
+    TT_CHECK(p->ensure(p->sig, sizeof(float) * std::max<size_t>(circ_elems, 1)));
+    TT_CUDA(cudaMemcpyAsync(p->in.p, img, sizeof(float) * (size_t)ir * ic, cudaMemcpyHostToDevice, st));
+    TT_CHECK(run_sinograms(p, (const float *)p->in.p, ir, ic, ir, n, ro, co, nullptr, ang.data(), A,
+                           tfuncs, n_t, tneed, (float *)p->sino.p, nullptr, st));
+    if (n_p == 0 || A == 0) {
+        TT_CUDA(cudaStreamSynchronize(st));
+        return TT_OK;
+    }
+    if (!ortho) {
+        TT_CHECK(run_circus(p, (const float *)p->sino.p, n, A, n_t, pfuncs, n_p, nullptr, pneed,
+                            (float *)p->circ.p, st));
+    } else {
+        // nearest orthonormal sinogram per T (host), then Hermite circus
+        std::vector<float> h_sino(sino_elems);
+        TT_CUDA(cudaMemcpyAsync(h_sino.data(), p->sino.p, sizeof(float) * sino_elems,
+                                cudaMemcpyDeviceToHost, st));
+        TT_CUDA(cudaStreamSynchronize(st));
+        for (int t = 0; t < n_t; t++) {
+            std::vector<float> nos;
+            int m = 0, center = 0;
+            TT_CHECK(nearest_orthonormal(h_sino.data() + (size_t)t * n * A, n, A, nos, &m, &center));
+            TT_CHECK(p->ensure(p->nos, sizeof(float) * nos.size()));
+            TT_CUDA(cudaMemcpyAsync(p->nos.p, nos.data(), sizeof(float) * nos.size(),
+                                    cudaMemcpyHostToDevice, st));
+            const int32_t c32 = center;
+            TT_CHECK(run_circus(p, (const float *)p->nos.p, m, A, 1, pfuncs, n_p, &c32, pneed,
+                                (float *)p->circ.p + (size_t)t * n_p * A, st));
+            TT_CUDA(cudaStreamSynchronize(st));
+        }
+    }
+    if (signatures)
+        TT_CUDA(tt::launch_zscore((const float *)p->circ.p, n_t * n_p, A, (float *)p->sig.p, st));
+    if (circus)
+        TT_CUDA(cudaMemcpyAsync(circus, p->circ.p, sizeof(float) * circ_elems, cudaMemcpyDeviceToHost, st));
+    if (signatures)
+        TT_CUDA(cudaMemcpyAsync(signatures, p->sig.p, sizeof(float) * circ_elems, cudaMemcpyDeviceToHost, st));
+    TT_CUDA(cudaStreamSynchronize(st));
+    return TT_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,124 @@
+"""Device-resident entry points on torch CUDA tensors (stream ordered).
+
+Layouts (torch tensors are row-major, the engine is column-major):
+
+* an image of R rows and C columns is a (C, R) contiguous tensor holding the
+  column-major matrix -- ``to_colmajor`` / ``from_colmajor`` convert;
+* a sinogram stack is (nT, A, N): ``sino[t, a]`` is column a (angle a) of
+  sinogram t, i.e. the engine's nT x N x A column-major stack;
+* circus functions are (nT, nP, A); signatures the same shape, z-scored.
+
+Work is enqueued on torch's current CUDA stream of the tensor's device.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from ._native import PFunctionalC, check, lib
+from .api import Plan, angles_from_step, pad_geometry
+
+
+def to_colmajor(image: torch.Tensor) -> torch.Tensor:
+    """(R, C) tensor -> (C, R) contiguous tensor holding it column-major."""
+    return image.t().contiguous()
+
+
+def from_colmajor(buf: torch.Tensor) -> torch.Tensor:
+    """(C, R) column-major storage -> (R, C) view."""
+    return buf.t()
+
+
+_CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy: the NULL stream's explicit handle
+
+
+def _stream(t: torch.Tensor):
+    """Handle of torch's current stream.  torch's default stream is the legacy
+    NULL stream (handle 0), which the C ABI would read as "the plan's own
+    stream", so it is passed as cudaStreamLegacy."""
+    h = torch.cuda.current_stream(t.device).cuda_stream
+    return ctypes.c_void_p(h if h else _CUDA_STREAM_LEGACY)
+
+
+def _ptr(t: Optional[torch.Tensor]):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _pf(pfuncs):
+    arr = (PFunctionalC * max(len(pfuncs), 1))()
+    for i, p in enumerate(pfuncs):
+        kind, order, center = (tuple(p) + (-1, -1))[:3]
+        arr[i].kind, arr[i].order, arr[i].center = int(kind), int(order), int(center)
+    return arr
+
+
+class Engine:
+    """One device's plan plus tensor-level calls of the C ABI."""
+
+    def __init__(self, device: int = 0):
+        self.device = torch.device("cuda", device)
+        self.plan = Plan(device)
+
+    def sinograms(self, image_cm: torch.Tensor, rows: int, cols: int, angles_deg, tfuncs,
+                  padded: bool = False, medians: bool = False,
+                  out: Optional[torch.Tensor] = None):
+        """Sinograms of a column-major image (see module doc).
+
+        padded=False: image_cm is the unpadded R x C image, placed in its pad()
+        frame implicitly; padded=True: it already is the N x N frame."""
+        if padded:
+            n, ro, co = rows, 0, 0
+            if rows != cols:
+                raise ValueError("a padded image must be square")
+        else:
+            n, ro, co = pad_geometry(rows, cols)
+        ang = np.ascontiguousarray(np.asarray(angles_deg, np.float32))
+        ids = np.ascontiguousarray(np.asarray([int(t) for t in tfuncs], np.int32))
+        if out is None:
+            out = torch.empty((len(ids), len(ang), n), dtype=torch.float32, device=image_cm.device)
+        med = torch.empty_like(out, dtype=torch.int32) if medians else None
+        check(lib().tt_sinograms_device(
+            self.plan.handle, _ptr(image_cm), rows, cols, rows, n, ro, co,
+            ang.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(ang),
+            ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), len(ids), _ptr(out), _ptr(med),
+            _stream(image_cm)))
+        return (out, med) if medians else out
+
+    def circus(self, sino: torch.Tensor, pfuncs: Sequence, centers=None,
+               out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """P-functionals of a (nS, A, N) sinogram stack -> (nS, nP, A).
+        pfuncs: (kind, order, center) tuples; centers: per-sinogram Hermite
+        centers overriding theirs."""
+        ns, a, n = sino.shape
+        if out is None:
+            out = torch.empty((ns, len(pfuncs), a), dtype=torch.float32, device=sino.device)
+        cptr = None
+        if centers is not None:
+            c = np.ascontiguousarray(np.asarray(centers, np.int32))
+            cptr = c.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        check(lib().tt_circus_device(self.plan.handle, _ptr(sino), n, a, ns, _pf(pfuncs),
+                                     len(pfuncs), cptr, _ptr(out), _stream(sino)))
+        return out
+
+    def zscore(self, circus: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        length = circus.shape[-1]
+        nvec = circus.numel() // max(length, 1)
+        if out is None:
+            out = torch.empty_like(circus)
+        check(lib().tt_zscore_device(self.plan.handle, _ptr(circus), nvec, length, _ptr(out),
+                                     _stream(circus)))
+        return out
+
+    def transform(self, image_cm: torch.Tensor, rows: int, cols: int, angles_deg, tfuncs,
+                  pfuncs, out_sino=None):
+        """Regular (non-orthonormal) transform on the device: returns
+        (sinograms, circus, signatures) tensors."""
+        sino = self.sinograms(image_cm, rows, cols, angles_deg, tfuncs, out=out_sino)
+        circ = self.circus(sino, [(k, o, -1) for k, o in pfuncs])
+        return sino, circ, self.zscore(circ)
+
+
+__all__ = ["Engine", "to_colmajor", "from_colmajor", "angles_from_step"]
