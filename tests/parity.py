@@ -40,6 +40,35 @@ def rel_err(got, ref, eps_frac=EPS_FRAC, axis=-1):
     return np.where(got == ref, 0.0, np.abs(got - ref) / scale)
 
 
+def selection_tie(keys: np.ndarray, weights: np.ndarray, got: float) -> bool:
+    """Is `got` the key at which the reference's weighted median of `keys`
+    could cross within float rounding?
+
+    TFunctional6/7 and PFunctional2 sort the keys, sum the weights in sorted
+    order in float and take the key at the first k with 2 C_k >= W
+    (c++/src/functionals.cpp:226-311).  A different summation order may move
+    the crossing across the boundary between two adjacent distinct keys when
+    |2 C - W| there is within N ulp(W)."""
+    keys = np.asarray(keys, np.float32)
+    w = np.asarray(weights, np.float32)
+    order = np.argsort(keys, kind="stable")
+    k, w = keys[order], w[order]
+    c = np.cumsum(w, dtype=np.float32)
+    total = c[-1] if len(c) else np.float32(0)
+    bound = len(k) * np.spacing(np.float32(abs(total))) + np.spacing(np.float32(0))
+    idx = np.nonzero(2.0 * c.astype(np.float64) >= float(total))[0]
+    i_ref = int(idx[0]) if len(idx) else len(k) - 1
+    if k[i_ref] == np.float32(got):
+        return True
+    where = np.nonzero(k == np.float32(got))[0]
+    if not len(where):
+        return False
+    lo_i, hi_i = (int(where[0]), i_ref) if where[0] < i_ref else (i_ref, int(where[-1]))
+    # every cumulative sum between the two keys must sit at the threshold
+    gap = np.abs(2.0 * c[lo_i:hi_i].astype(np.float64) - float(total))
+    return bool(np.all(gap <= bound))
+
+
 def median_tie(x: np.ndarray, m_ref: int, m_gpu: int) -> bool:
     """Is the reference's weighted-median crossing of column x ambiguous
     between rows m_ref and m_gpu at float precision?

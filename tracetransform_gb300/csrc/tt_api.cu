@@ -71,6 +71,24 @@ struct FftTables {
     float *lin = nullptr;
 };
 
+// A gather-capable CUDA array holding a source image (texel (u, v) = image
+// row u, column v) and its border-mode texture object.
+struct SourceTexture {
+    cudaArray_t arr = nullptr;
+    cudaTextureObject_t tex = 0;
+    int rows = 0, cols = 0;
+
+    void release() {
+        if (tex)
+            cudaDestroyTextureObject(tex);
+        if (arr)
+            cudaFreeArray(arr);
+        tex = 0;
+        arr = nullptr;
+        rows = cols = 0;
+    }
+};
+
 // ---- host math -----------------------------------------------------------
 
 float deg2rad(float degrees) { return (float)(degrees * M_PI / 180); }
@@ -282,6 +300,7 @@ struct tt_plan {
     std::map<std::vector<float>, float2 *> trig;        // angle list -> (c, s)
     std::map<std::vector<long>, const float **> herm_ptrs;
     DevBuf in, sino, circ, sig, region, nos;
+    SourceTexture src;
     std::vector<void *> owned;
 
     ~tt_plan() {
@@ -290,6 +309,8 @@ struct tt_plan {
         cudaSetDevice(device);
         if (stream)
             cudaStreamSynchronize(stream);
+        cudaDeviceSynchronize();
+        src.release();
         for (void *p : owned)
             cudaFree(p);
         for (DevBuf *b : {&in, &sino, &circ, &sig, &region, &nos})
@@ -323,6 +344,41 @@ struct tt_plan {
         TT_CHECK(alloc((void **)dst, sizeof(T) * h.size()));
         TT_CUDA(cudaMemcpyAsync(*dst, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, stream));
         TT_CUDA(cudaStreamSynchronize(stream));
+        return TT_OK;
+    }
+
+    // Copy a rows x cols column-major device image (leading dimension ld)
+    // into the source texture, stream ordered.  The array is reallocated only
+    // when the size changes (after the device has drained: kernels in flight
+    // may still read the old texture).
+    tt_status load_source(const float *d_img, int rows, int cols, int ld, cudaStream_t st,
+                          cudaTextureObject_t *tex) {
+        if (rows > 32768 || cols > 32768)
+            return fail(TT_ERR_UNSUPPORTED, "image %dx%d exceeds the 32768 texture-gather limit",
+                        rows, cols);
+        if (src.rows != rows || src.cols != cols) {
+            TT_CUDA(cudaDeviceSynchronize());
+            src.release();
+            cudaChannelFormatDesc desc = cudaCreateChannelDesc<float>();
+            TT_CUDA(cudaMallocArray(&src.arr, &desc, rows, cols, cudaArrayTextureGather));
+            cudaResourceDesc res{};
+            res.resType = cudaResourceTypeArray;
+            res.res.array.array = src.arr;
+            cudaTextureDesc td{};
+            td.addressMode[0] = cudaAddressModeBorder;
+            td.addressMode[1] = cudaAddressModeBorder;
+            td.filterMode = cudaFilterModePoint;
+            td.readMode = cudaReadModeElementType;
+            td.normalizedCoords = 0;
+            TT_CUDA(cudaCreateTextureObject(&src.tex, &res, &td, nullptr));
+            src.rows = rows;
+            src.cols = cols;
+        }
+        if (d_img)
+            TT_CUDA(cudaMemcpy2DToArrayAsync(src.arr, 0, 0, d_img, sizeof(float) * (size_t)ld,
+                                             sizeof(float) * (size_t)rows, cols,
+                                             cudaMemcpyDeviceToDevice, st));
+        *tex = src.tex;
         return TT_OK;
     }
 
@@ -502,10 +558,16 @@ tt_status run_sinograms(tt_plan *p, const float *d_src, int src_rows, int src_co
     if (n_angles == 0 || n_t == 0 || n == 0)
         return TT_OK;
     SinoArgs a{};
-    a.src = d_src;
+    if (src_rows > 0 && src_cols > 0) {
+        TT_CHECK(p->load_source(d_src, src_rows, src_cols, src_ld, st, &a.tex));
+    } else {
+        src_rows = src_cols = 0; // nothing to sample: every line is zero
+        TT_CHECK(p->load_source(nullptr, 1, 1, 1, st, &a.tex));
+    }
+    a.tex_row_off = row_off;
+    a.tex_col_off = col_off;
     a.src_rows = src_rows;
     a.src_cols = src_cols;
-    a.src_ld = src_ld;
     a.row_off = row_off;
     a.col_off = col_off;
     a.dyn_region = d_region;
@@ -521,11 +583,11 @@ tt_status run_sinograms(tt_plan *p, const float *d_src, int src_rows, int src_co
     for (int t = 0; t < n_t; t++)
         a.tf[t] = tfuncs[t];
     a.need = need;
-    const int L = tt::sino_lines_per_block();
+    const int L = tt::sino_lines_per_block(n, need);
     a.stride = tt::sino_stride(n, L);
-    if (tt::sino_smem_bytes(n, L) > 227 * 1024)
+    if (tt::sino_smem_bytes(n, L, need) > 227 * 1024)
         return fail(TT_ERR_UNSUPPORTED, "padded side %d exceeds the shared-memory line buffer", n);
-    TT_CUDA(tt::launch_sinograms(a, st));
+    TT_CUDA(tt::launch_sinograms(a, L, st));
     return TT_OK;
 }
 
@@ -777,8 +839,10 @@ tt_status tt_rotate(tt_plan *plan, const float *image, int rows, int cols, float
     TT_CHECK(p->ensure(p->sino, sizeof(float) * elems));
     TT_CUDA(cudaMemcpyAsync(p->in.p, image, sizeof(float) * elems, cudaMemcpyHostToDevice, st));
     const float ang = deg2rad(angle_deg);
-    TT_CUDA(tt::launch_rotate((const float *)p->in.p, rows, cols, std::cos(-ang), std::sin(-ang),
-                              (float *)p->sino.p, st));
+    cudaTextureObject_t tex;
+    TT_CHECK(p->load_source((const float *)p->in.p, rows, cols, rows, st, &tex));
+    TT_CUDA(tt::launch_rotate(tex, rows, cols, std::cos(-ang), std::sin(-ang), (float *)p->sino.p,
+                              st));
     TT_CUDA(cudaMemcpyAsync(out, p->sino.p, sizeof(float) * elems, cudaMemcpyDeviceToHost, st));
     TT_CUDA(cudaStreamSynchronize(st));
     return TT_OK;

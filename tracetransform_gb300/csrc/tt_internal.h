@@ -12,12 +12,12 @@ constexpr int kMaxP = 16; // P-functional entries per call
 
 // Fused rotate + T-functional sweep over one image.
 struct SinoArgs {
-    const float *src;   // element (0, 0) of the source region
-    int src_rows, src_cols, src_ld;
-    int row_off, col_off; // region origin inside the n x n padded frame
+    cudaTextureObject_t tex; // source pixels (border mode: 0 outside)
+    int tex_row_off, tex_col_off; // frame position of texel (0, 0)
+    int src_rows, src_cols;       // support region: rows x cols at
+    int row_off, col_off;         // (row_off, col_off) of the frame
     const int *dyn_region; // optional device int4 {row0, col0, rows, cols}
-                           // overriding the region (src then points at the
-                           // frame origin and src_ld is the frame's)
+                           // replacing the support region
     int n;                 // padded side N
     int n_angles;
     const float2 *trig; // per angle (cos(-theta), sin(-theta)), host-rounded
@@ -49,12 +49,12 @@ struct CircusArgs {
 // Opt-in shared memory per block minus the kernel's static shared memory.
 size_t dynamic_smem_limit(const void *kernel);
 
-int sino_lines_per_block();
-size_t sino_smem_bytes(int n, int lines);
+int sino_lines_per_block(int n, unsigned need);
+size_t sino_smem_bytes(int n, int lines, unsigned need);
 int sino_stride(int n, int lines);
-cudaError_t launch_sinograms(const SinoArgs &a, cudaStream_t stream);
-cudaError_t launch_rotate(const float *src, int rows, int cols, float c, float s, float *out,
-                          cudaStream_t stream);
+cudaError_t launch_sinograms(const SinoArgs &a, int lines, cudaStream_t stream);
+cudaError_t launch_rotate(cudaTextureObject_t tex, int rows, int cols, float c, float s,
+                          float *out, cudaStream_t stream);
 cudaError_t launch_region_bbox(const float *frame, int n, int *d_region,
                                cudaStream_t stream);
 cudaError_t launch_circus(const CircusArgs &a, cudaStream_t stream);

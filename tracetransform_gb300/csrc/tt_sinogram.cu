@@ -7,53 +7,31 @@
 // requested T-functional (c++/src/sinogram.cpp:67-178 with the functionals of
 // c++/src/functionals.cpp:21-276).
 //
-// Rotated samples are bit-identical to the reference's rotate()/interpolate()
-// (c++/src/auxiliary.cpp:182-196, 223-255): the host rounds cos/sin exactly as
-// the reference does, and the coordinate transform and bilinear expression
-// are evaluated with explicit round-to-nearest intrinsics in the reference's
-// order, so no multiply-add is fused.  Only rows whose 2x2 stencil can touch
-// the image are sampled; all others are exact zeros in the reference too.
+// Sampling.  The source region sits in a block-linear CUDA array read through
+// a texture object in border mode (texels outside the region read 0, which
+// is exactly the reference's zero padding).  One 2x2 gather (tld4) fetches
+// the bilinear stencil; coordinates and weights are then combined in the
+// reference's order with scalar round-to-nearest operations, so every
+// rotated sample is bit-identical to rotate()/interpolate()
+// (c++/src/auxiliary.cpp:182-196, 223-255): the host rounds cos/sin as the
+// reference does and no multiply-add is fused.  (Packed f32x2 multiply + add
+// measured fused on this part, so they are not used here.)  Each thread keeps
+// four gathers in flight.  Only rows whose stencil can touch the image are
+// sampled; all others are exact zeros in the reference too.
 //
 // Reductions run in warp order rather than the reference's sequential order,
 // so sums agree to rounding and a weighted median can move by one row where
 // the reference's cumulative sum ties the half-total to within rounding.
+// T6 and T7 need no sort: their weighted medians come from a histogram
+// selection with exact fixed-point weights (tt_select.cuh).
 #include <climits>
 
 #include "tt_common.cuh"
 #include "tt_internal.h"
+#include "tt_select.cuh"
 
 namespace tt {
 namespace {
-
-constexpr int kLines = 8; // lines (warps) per CTA
-
-// Bilinear sample at frame coordinates (qx, qy), reference order.  The
-// reference samples only where 0 <= qx < xmax and 0 <= qy < ymax (frame
-// columns - 1, rows - 1); the source region is rr x rc at (roff, coff).
-__device__ __forceinline__ float sample(const float *__restrict__ src, int ld,
-                                        int rr, int rc, int roff, int coff,
-                                        float xmax, float ymax, float qx, float qy) {
-    if (!(qx >= 0.f && qx < xmax && qy >= 0.f && qy < ymax))
-        return 0.f;
-    const float xi = truncf(qx), yi = truncf(qy);
-    const float xf = __fsub_rn(qx, xi), yf = __fsub_rn(qy, yi);
-    const int cx = (int)xi - coff, cy = (int)yi - roff;
-    const bool x0 = (unsigned)cx < (unsigned)rc;
-    const bool x1 = (unsigned)(cx + 1) < (unsigned)rc;
-    const bool y0 = (unsigned)cy < (unsigned)rr;
-    const bool y1 = (unsigned)(cy + 1) < (unsigned)rr;
-    const long long o00 = (long long)cx * ld + cy;
-    const float s00 = (x0 && y0) ? __ldg(src + o00) : 0.f;
-    const float s10 = (x0 && y1) ? __ldg(src + o00 + 1) : 0.f;
-    const float s01 = (x1 && y0) ? __ldg(src + o00 + ld) : 0.f;
-    const float s11 = (x1 && y1) ? __ldg(src + o00 + ld + 1) : 0.f;
-    const float omx = __fsub_rn(1.f, xf), omy = __fsub_rn(1.f, yf);
-    const float t0 = __fmul_rn(__fmul_rn(s00, omx), omy);
-    const float t1 = __fmul_rn(__fmul_rn(s01, xf), omy);
-    const float t2 = __fmul_rn(__fmul_rn(s10, omx), yf);
-    const float t3 = __fmul_rn(__fmul_rn(s11, xf), yf);
-    return __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
-}
 
 // Rows [lo, hi) of a line whose samples can be non-zero: the reference's
 // bounds test 0 <= q < n-1 intersected with the band where the 2x2 stencil
@@ -104,52 +82,65 @@ __device__ __forceinline__ int resolve_median(int found, float total, int jlo,
     return n - 1;
 }
 
-// Smallest key k (a non-negative float) with 2 * sum(weights of keys <= k) >=
-// sum(weights): the weighted median of a sorted sequence as TFunctional6 /
-// TFunctional7 take it (c++/src/functionals.cpp:226-276), found by bisection
-// on the key's bit pattern.  Elements are the stored rows [b, jhi) of a line.
-template <bool kT6>
-__device__ float weighted_select(const float *x, int jlo, int jhi, int b,
-                                 int m, int lane) {
-    float wt = 0.f;
-    for (int j = b + lane; j < jhi; j += 32)
-        wt += __fsqrt_rn(x[j - jlo]);
-    wt = warp_sum(wt);
-    unsigned lo = 0u, hi = 0x7f800000u;
-    while (lo < hi) {
-        const unsigned mid = lo + ((hi - lo) >> 1);
-        float f = 0.f;
-        for (int j = b + lane; j < jhi; j += 32) {
-            const float v = x[j - jlo];
-            const float key = kT6 ? __fmul_rn((float)(j - m), v) : v;
-            if (__float_as_uint(key) <= mid)
-                f += __fsqrt_rn(v);
-        }
-        f = warp_sum(f);
-        if (2.f * f >= wt)
-            hi = mid;
-        else
-            lo = mid + 1u;
-    }
-    return __uint_as_float(lo);
+template <bool kSqrt>
+__device__ __forceinline__ float elem(const float *x, int i) {
+    return kSqrt ? __fsqrt_rn(x[i]) : x[i];
 }
 
-template <int L>
+// First element i (of the chunked line) with 2 * prefix_i >= total, given the
+// per-lane chunk sums: the warp jumps to the first chunk whose inclusive sum
+// crosses and scans that chunk cooperatively (continuing into the next chunk
+// if rounding put the crossing there).  Valid for non-negative data.
+template <bool kSqrt>
+__device__ int find_crossing(const float *x, int C, float inc, float exc, float total, int lane) {
+    const unsigned ball = __ballot_sync(TT_FULL_MASK, 2.f * inc >= total);
+    if (!ball)
+        return INT_MAX;
+    for (int ln = __ffs(ball) - 1; ln < 32; ln++) {
+        float basev = __shfl_sync(TT_FULL_MASK, exc, ln);
+        for (int t0 = 0; t0 < C; t0 += 32) {
+            const int t = t0 + lane;
+            const float v = t < C ? elem<kSqrt>(x, ln * C + t) : 0.f;
+            const float p = warp_incl_scan(v, lane) + basev;
+            const unsigned b = __ballot_sync(TT_FULL_MASK, t < C && 2.f * p >= total);
+            if (b)
+                return ln * C + t0 + __ffs(b) - 1;
+            basev = __shfl_sync(TT_FULL_MASK, p, 31);
+        }
+    }
+    return INT_MAX;
+}
+
+// Sequential per-lane walk (any sign): the first crossing as the reference
+// defines it even when the prefix is not monotone.
+__device__ int find_crossing_walk(const float *x, int C, float exc, float total, int lane) {
+    float run = exc;
+    int f = INT_MAX;
+    for (int k = 0; k < C; k++) {
+        run += x[lane * C + k];
+        if (f == INT_MAX && 2.f * run >= total)
+            f = lane * C + k;
+    }
+    return warp_min(f);
+}
+
+template <int L, bool kSel>
 __global__ void __launch_bounds__(32 * L)
     sino_kernel(const SinoArgs a) {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ int s_range[2];
     __shared__ int s_region[4];
+    float *sm = reinterpret_cast<float *>(smraw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int angle = blockIdx.y;
     const int col0 = blockIdx.x * L;
     const int n = a.n;
     const float2 cs = a.trig[angle];
-    const float c = cs.x, s = cs.y, ms = -cs.y;
+    const float c = cs.x, s = cs.y;
     const float o = (float)(n - 1) * 0.5f;
     const float nm1 = (float)(n - 1);
 
-    // Source region (static or computed on the device).
+    // Support region (static, or the non-zero box found on the device).
     if (threadIdx.x == 0) {
         if (a.dyn_region) {
             s_region[0] = a.dyn_region[0];
@@ -166,7 +157,6 @@ __global__ void __launch_bounds__(32 * L)
     __syncthreads();
     const int roff = s_region[0], coff = s_region[1];
     const int rr = max(s_region[2], 0), rc = max(s_region[3], 0);
-    const float *src = a.dyn_region ? a.src + (long long)coff * a.src_ld + roff : a.src;
 
     // 1. Row range shared by the CTA's lines.
     if (warp == 0) {
@@ -191,26 +181,49 @@ __global__ void __launch_bounds__(32 * L)
     const int jlo = s_range[0], jhi = s_range[1];
     const int len = jhi - jlo;
     const int C = max((len + 31) >> 5, 1) | 1; // odd: conflict-free chunks
-    const int span = 32 * C;
+
 
     // 2. Sample the lines into shared memory (zeros past len).
     {
         constexpr int RPW = 32 / L;
         const int l = lane % L, r = lane / L;
         const int col = col0 + l;
+        const bool colok = col < n;
         const float X = (float)col - o;
-        const float Xc = __fmul_rn(X, c), Xms = __fmul_rn(X, ms);
+        const float Xc = __fmul_rn(X, c), Xms = __fmul_rn(X, -s);
+        const float tu = 1.f - (float)a.tex_row_off, tv = 1.f - (float)a.tex_col_off;
         float *dst = sm + l * a.stride;
-#pragma unroll 4
-        for (int jr = warp * RPW + r; jr < span; jr += 32) {
-            float v = 0.f;
-            if (jr < len && col < n) {
+        const int first = warp * RPW + r; // this thread's rows: first + 32 i, i < C
+        constexpr int U = 4;              // gathers in flight per thread
+        for (int i0 = 0; i0 < C; i0 += U) {
+            float4 g[U];
+            float xf[U], yf[U];
+            bool ok[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int jr = first + 32 * (i0 + u);
                 const float Y = (float)(jlo + jr) - o;
+                // (x c + y s) + o and (x (-s) + y c) + o, each operation rounded
                 const float qx = __fadd_rn(__fadd_rn(Xc, __fmul_rn(Y, s)), o);
                 const float qy = __fadd_rn(__fadd_rn(Xms, __fmul_rn(Y, c)), o);
-                v = sample(src, a.src_ld, rr, rc, roff, coff, nm1, nm1, qx, qy);
+                ok[u] = colok && jr < len && qx >= 0.f && qx < nm1 && qy >= 0.f && qy < nm1;
+                const float xi = truncf(qx), yi = truncf(qy);
+                xf[u] = __fsub_rn(qx, xi);
+                yf[u] = __fsub_rn(qy, yi);
+                // texel (u, v) = image (row, col); w/z/x/y = s00, s10, s01, s11
+                g[u] = tex2Dgather<float4>(a.tex, yi + tu, xi + tv, 0);
             }
-            dst[jr] = v;
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const float omx = __fsub_rn(1.f, xf[u]), omy = __fsub_rn(1.f, yf[u]);
+                const float t0 = __fmul_rn(__fmul_rn(g[u].w, omx), omy);
+                const float t1 = __fmul_rn(__fmul_rn(g[u].x, xf[u]), omy);
+                const float t2 = __fmul_rn(__fmul_rn(g[u].z, omx), yf[u]);
+                const float t3 = __fmul_rn(__fmul_rn(g[u].y, xf[u]), yf[u]);
+                const float v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
+                if (i0 + u < C)
+                    dst[first + 32 * (i0 + u)] = ok[u] ? v : 0.f;
+            }
         }
     }
     __syncthreads();
@@ -219,64 +232,57 @@ __global__ void __launch_bounds__(32 * L)
     const int col = col0 + warp;
     if (col >= n)
         return;
-    const float *x = sm + warp * a.stride;
+    float *x = sm + warp * a.stride;
     const unsigned need = a.need;
     const bool need_m1 = need & ((1u << 1) | (1u << 2) | (1u << 7));
     const bool need_m2 = need & ((1u << 3) | (1u << 4) | (1u << 5) | (1u << 6));
+    const bool need_sq = need_m2 || (need & (1u << 7)); // sum of sqrt(x) wanted
     const int base = lane * C;
 
-    float tot = 0.f, totq = 0.f;
+    float tot = 0.f, totq = 0.f, lmax = 0.f;
+    bool neg = false;
     for (int k = 0; k < C; k++) {
         const float v = x[base + k];
         tot += v;
-        if (need_m2)
+        neg |= v < 0.f;
+        if (kSel)
+            lmax = fmaxf(lmax, v);
+        if (need_sq)
             totq += __fsqrt_rn(v);
     }
     const float inc = warp_incl_scan(tot, lane);
     const float S = __shfl_sync(TT_FULL_MASK, inc, 31);
-    float ps = __shfl_up_sync(TT_FULL_MASK, inc, 1);
-    float Q = 0.f, pq = 0.f;
-    if (need_m2) {
-        const float incq = warp_incl_scan(totq, lane);
+    float exc = __shfl_up_sync(TT_FULL_MASK, inc, 1);
+    float Q = 0.f, incq = 0.f, excq = 0.f;
+    if (need_sq) {
+        incq = warp_incl_scan(totq, lane);
         Q = __shfl_sync(TT_FULL_MASK, incq, 31);
-        pq = __shfl_up_sync(TT_FULL_MASK, incq, 1);
+        excq = __shfl_up_sync(TT_FULL_MASK, incq, 1);
     }
     if (lane == 0) {
-        ps = 0.f;
-        pq = 0.f;
+        exc = 0.f;
+        excq = 0.f;
     }
+    const bool any_neg = __any_sync(TT_FULL_MASK, neg);
 
     int m1 = 0, m2 = 0;
-    if (need_m1 || need_m2) {
-        int f1 = INT_MAX, f2 = INT_MAX;
-        for (int k = 0; k < C; k++) {
-            const float v = x[base + k];
-            ps += v;
-            if (f1 == INT_MAX && 2.f * ps >= S)
-                f1 = base + k;
-            if (need_m2) {
-                pq += __fsqrt_rn(v);
-                if (f2 == INT_MAX && 2.f * pq >= Q)
-                    f2 = base + k;
-            }
-        }
-        m1 = resolve_median(warp_min(f1), S, jlo, jhi, len, n);
-        if (need_m2)
-            m2 = resolve_median(warp_min(f2), Q, jlo, jhi, len, n);
+    if (need_m1) {
+        const int f = any_neg ? find_crossing_walk(x, C, exc, S, lane)
+                              : find_crossing<false>(x, C, inc, exc, S, lane);
+        m1 = resolve_median(f, S, jlo, jhi, len, n);
     }
+    if (need_m2)
+        m2 = resolve_median(find_crossing<true>(x, C, incq, excq, Q, lane), Q, jlo, jhi, len, n);
 
     float r1v = 0.f, r2v = 0.f;
     if (need & ((1u << 1) | (1u << 2))) {
         float t1 = 0.f, t2 = 0.f;
-        for (int k = 0; k < C; k++) {
-            const int j = jlo + base + k;
-            const float v = x[base + k];
-            if (j >= m1) {
-                const float r = (float)(j - m1);
-                const float vr = v * r;
-                t1 += vr;
-                t2 += vr * r;
-            }
+        for (int j = max(m1, jlo) + lane; j < jhi; j += 32) {
+            const float v = x[j - jlo];
+            const float r = (float)(j - m1);
+            const float vr = v * r;
+            t1 += vr;
+            t2 = fmaf(vr, r, t2);
         }
         r1v = warp_sum(t1);
         r2v = warp_sum(t2);
@@ -292,18 +298,18 @@ __global__ void __launch_bounds__(32 * L)
             const float v = x[m2 + q - jlo];
             if (w3) {
                 const float2 w = __ldg(tab3 + q);
-                re3 += w.x * v;
-                im3 += w.y * v;
+                re3 = fmaf(w.x, v, re3);
+                im3 = fmaf(w.y, v, im3);
             }
             if (w4) {
                 const float2 w = __ldg(tab4 + q);
-                re4 += w.x * v;
-                im4 += w.y * v;
+                re4 = fmaf(w.x, v, re4);
+                im4 = fmaf(w.y, v, im4);
             }
             if (w5) {
                 const float2 w = __ldg(tab5 + q);
-                re5 += w.x * v;
-                im5 += w.y * v;
+                re5 = fmaf(w.x, v, re5);
+                im5 = fmaf(w.y, v, im5);
             }
         }
         // hypot of the two float integrals in double, as C's hypot does
@@ -322,10 +328,13 @@ __global__ void __launch_bounds__(32 * L)
     }
 
     float r6v = 0.f, r7v = 0.f;
-    if (need & (1u << 6))
-        r6v = weighted_select<true>(x, jlo, jhi, max(m2, jlo), m2, lane);
-    if (need & (1u << 7))
-        r7v = weighted_select<false>(x, jlo, jhi, max(m1, jlo), m1, lane);
+    if (kSel) {
+        SelScratch *scr = reinterpret_cast<SelScratch *>(sm + L * a.stride) + 2 * warp;
+        const float xmax = __int_as_float(warp_max(__float_as_int(lmax)));
+        // T6: keys r1 * x[m2 + r1], r1 in [0, N - m2); T7: keys x[m1 ..]
+        select_t67(x, jlo, jhi, m1, m2, need & (1u << 6), need & (1u << 7), xmax, Q, scr,
+                   scr + 1, lane, &r6v, &r7v);
+    }
 
     if (lane == 0) {
         const size_t plane = (size_t)a.n_angles * n;
@@ -353,8 +362,8 @@ __global__ void __launch_bounds__(32 * L)
 
 // rotate() of c++/src/auxiliary.cpp:223-255 about ((cols-1)/2, (rows-1)/2),
 // writing the rotated image (used to check the sampling arithmetic; the
-// fused kernel never materialises it).
-__global__ void rotate_kernel(const float *__restrict__ src, int rows, int cols, float2 cs,
+// fused kernel never materialises it).  Same texture path as the fused kernel.
+__global__ void rotate_kernel(cudaTextureObject_t tex, int rows, int cols, float2 cs,
                               float *__restrict__ out) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= (long long)rows * cols)
@@ -364,7 +373,19 @@ __global__ void rotate_kernel(const float *__restrict__ src, int rows, int cols,
     const float X = (float)col - ox, Y = (float)row - oy;
     const float qx = __fadd_rn(__fadd_rn(__fmul_rn(X, cs.x), __fmul_rn(Y, cs.y)), ox);
     const float qy = __fadd_rn(__fadd_rn(__fmul_rn(X, -cs.y), __fmul_rn(Y, cs.x)), oy);
-    out[i] = sample(src, rows, rows, cols, 0, 0, (float)(cols - 1), (float)(rows - 1), qx, qy);
+    float v = 0.f;
+    if (qx >= 0.f && qx < (float)(cols - 1) && qy >= 0.f && qy < (float)(rows - 1)) {
+        const float xi = truncf(qx), yi = truncf(qy);
+        const float xf = __fsub_rn(qx, xi), yf = __fsub_rn(qy, yi);
+        const float4 g = tex2Dgather<float4>(tex, yi + 1.f, xi + 1.f, 0);
+        const float omx = __fsub_rn(1.f, xf), omy = __fsub_rn(1.f, yf);
+        const float t0 = __fmul_rn(__fmul_rn(g.w, omx), omy);
+        const float t1 = __fmul_rn(__fmul_rn(g.x, xf), omy);
+        const float t2 = __fmul_rn(__fmul_rn(g.z, omx), yf);
+        const float t3 = __fmul_rn(__fmul_rn(g.y, xf), yf);
+        v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
+    }
+    out[i] = v;
 }
 
 // Bounding box of the non-zero pixels of an n x n frame.
@@ -413,18 +434,25 @@ __global__ void bbox_finish(int *r) {
     }
 }
 
+template <int L, bool kSel>
+cudaError_t launch_one(const SinoArgs &a, size_t smem, cudaStream_t stream) {
+    static size_t limit = 0;
+    if (limit == 0) {
+        limit = dynamic_smem_limit((const void *)sino_kernel<L, kSel>);
+        cudaError_t e = cudaFuncSetAttribute(sino_kernel<L, kSel>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)limit);
+        if (e != cudaSuccess)
+            return e;
+    }
+    if (smem > limit)
+        return cudaErrorInvalidValue;
+    dim3 grid((a.n + L - 1) / L, a.n_angles);
+    sino_kernel<L, kSel><<<grid, 32 * L, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
 } // namespace
-
-int sino_lines_per_block() { return kLines; }
-
-int sino_stride(int n, int lines) {
-    const int cmax = (((n + 31) >> 5) | 1);
-    return 32 * cmax + 32 / lines;
-}
-
-size_t sino_smem_bytes(int n, int lines) {
-    return sizeof(float) * (size_t)lines * sino_stride(n, lines);
-}
 
 size_t dynamic_smem_limit(const void *kernel) {
     int dev = 0, optin = 0;
@@ -435,31 +463,38 @@ size_t dynamic_smem_limit(const void *kernel) {
     return optin > (int)fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
 }
 
-cudaError_t launch_sinograms(const SinoArgs &a, cudaStream_t stream) {
-    const int L = kLines;
-    const size_t smem = sino_smem_bytes(a.n, L);
-    static size_t limit = 0;
-    if (limit == 0) {
-        limit = dynamic_smem_limit((const void *)sino_kernel<kLines>);
-        cudaError_t e = cudaFuncSetAttribute(sino_kernel<kLines>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)limit);
-        if (e != cudaSuccess)
-            return e;
-    }
-    if (smem > limit)
-        return cudaErrorInvalidValue;
-    dim3 grid((a.n + L - 1) / L, a.n_angles);
-    sino_kernel<kLines><<<grid, 32 * L, smem, stream>>>(a);
-    return cudaGetLastError();
+int sino_lines_per_block(int n, unsigned need) {
+    // eight lines per CTA unless the line buffers (+ T6/T7 histograms) would
+    // leave room for a single CTA per SM
+    return sino_smem_bytes(n, 8, need) > 110 * 1024 ? 4 : 8;
 }
 
-cudaError_t launch_rotate(const float *src, int rows, int cols, float c, float s, float *out,
-                          cudaStream_t stream) {
+int sino_stride(int n, int lines) {
+    const int cmax = (((n + 31) >> 5) | 1);
+    return 32 * cmax + 32 / lines;
+}
+
+size_t sino_smem_bytes(int n, int lines, unsigned need) {
+    size_t bytes = sizeof(float) * (size_t)lines * sino_stride(n, lines);
+    if (need & ((1u << 6) | (1u << 7)))
+        bytes = ((bytes + 15) & ~size_t(15)) + 2 * sizeof(SelScratch) * lines;
+    return bytes;
+}
+
+cudaError_t launch_sinograms(const SinoArgs &a, int lines, cudaStream_t stream) {
+    const size_t smem = sino_smem_bytes(a.n, lines, a.need);
+    const bool sel = a.need & ((1u << 6) | (1u << 7));
+    if (lines == 8)
+        return sel ? launch_one<8, true>(a, smem, stream) : launch_one<8, false>(a, smem, stream);
+    return sel ? launch_one<4, true>(a, smem, stream) : launch_one<4, false>(a, smem, stream);
+}
+
+cudaError_t launch_rotate(cudaTextureObject_t tex, int rows, int cols, float c, float s,
+                          float *out, cudaStream_t stream) {
     const long long total = (long long)rows * cols;
     if (total == 0)
         return cudaSuccess;
-    rotate_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(src, rows, cols,
+    rotate_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(tex, rows, cols,
                                                                        make_float2(c, s), out);
     return cudaGetLastError();
 }
