@@ -93,29 +93,6 @@ struct SourceTexture {
 
 float deg2rad(float degrees) { return (float)(degrees * M_PI / 180); }
 
-void fft_pow2(std::vector<std::complex<double>> &a, int sign) {
-    const int n = (int)a.size();
-    for (int i = 1, j = 0; i < n; i++) {
-        int bit = n >> 1;
-        for (; j & bit; bit >>= 1)
-            j ^= bit;
-        j ^= bit;
-        if (i < j)
-            std::swap(a[i], a[j]);
-    }
-    for (int len = 2; len <= n; len <<= 1) {
-        for (int i = 0; i < n; i += len) {
-            for (int k = 0; k < len / 2; k++) {
-                const double ang = sign * 2.0 * M_PI * k / len;
-                const std::complex<double> w(std::cos(ang), std::sin(ang));
-                const std::complex<double> u = a[i + k], v = a[i + k + len / 2] * w;
-                a[i + k] = u + v;
-                a[i + k + len / 2] = u - v;
-            }
-        }
-    }
-}
-
 float hermite_polynomial(unsigned order, float x) {
     switch (order) {
     case 0:
@@ -430,28 +407,12 @@ struct tt_plan {
             return TT_OK;
         }
         FftTables t;
-        int M = 2;
-        while (M < 2 * n - 1)
-            M <<= 1;
+        const int M = tt::p3_fft_length(n);
         t.M = M;
         std::vector<float2> chirp(n), filt(M), twid(M / 2);
-        std::vector<std::complex<double>> w(n), b(M, 0.0);
-        for (int j = 0; j < n; j++) {
-            const long q = ((long)j * j) % (2L * n);
-            w[j] = std::complex<double>(std::cos(M_PI * q / n), -std::sin(M_PI * q / n));
-            chirp[j] = make_float2((float)w[j].real(), (float)w[j].imag());
-        }
-        b[0] = std::conj(w[0]);
-        for (int j = 1; j < n; j++)
-            b[j] = b[M - j] = std::conj(w[j]);
-        fft_pow2(b, -1);
-        for (int i = 0; i < M; i++)
-            filt[i] = make_float2((float)(b[i].real() / M), (float)(b[i].imag() / M));
-        for (int k = 0; k < M / 2; k++)
-            twid[k] = make_float2((float)std::cos(-2.0 * M_PI * k / M), (float)std::sin(-2.0 * M_PI * k / M));
         std::vector<float> lin(n);
-        for (int p = 0; p < n; p++)
-            lin[p] = (float)(-1 + p * 2.0 / (n - 1));
+        std::vector<std::complex<double>> work(M);
+        tt::p3_tables(n, chirp.data(), filt.data(), twid.data(), lin.data(), work.data());
         TT_CHECK(upload(&t.chirp, chirp));
         TT_CHECK(upload(&t.filt, filt));
         TT_CHECK(upload(&t.twid, twid));

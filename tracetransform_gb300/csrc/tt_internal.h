@@ -2,6 +2,8 @@
 // translation units (not part of the public ABI).
 #pragma once
 
+#include <complex>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -45,6 +47,12 @@ struct CircusArgs {
     unsigned need;        // bit k set when P kind k is requested
     float *out;           // n_sino x n_p x cols
 };
+
+// P3 tables (tt_tables.cu): FFT length M for a column of n samples, and the
+// chirp (n), filter (M), twiddles (M / 2) and linspace (n); work holds M.
+int p3_fft_length(int n);
+void p3_tables(int n, float2 *chirp, float2 *filt, float2 *twid, float *lin,
+               std::complex<double> *work);
 
 // Opt-in shared memory per block minus the kernel's static shared memory.
 size_t dynamic_smem_limit(const void *kernel);
