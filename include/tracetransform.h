@@ -171,6 +171,27 @@ tt_status tt_zscore_device(tt_plan *plan, const float *d_in, int n_vec, int len,
 /* Synchronise the plan's stream. */
 tt_status tt_plan_synchronize(tt_plan *plan);
 
+/* ---- allocation-free entry point ---------------------------------------- */
+/* No counterpart in the reference.  P1 / P2 / P3 circus functions of n_sino
+ * stacked rows x cols sinograms (device), z-scored into d_signatures
+ * (n_sino x n_p x cols, the layout of tt_circus_device + tt_zscore_device),
+ * for callers that cannot allocate device memory while they run -- a plugin
+ * whose host application's allocator owns all device memory, or a loop that
+ * cannot afford cudaMalloc/cudaFree stalls.  It allocates nothing: the raw
+ * circus values and the P3 tables live in one file-scope device array of
+ * 1048576 floats (4 MiB) that every GPU loading the library holds until the
+ * process exits; larger requests (n_sino * n_p * cols plus, with P3, about
+ * 5 * rows floats of tables) fail with TT_ERR_INVALID_ARG, P3 needs
+ * rows <= 8192, and Hermite is TT_ERR_UNSUPPORTED (use tt_circus_device).
+ * The first call on a device looks up the array's device address (set-up);
+ * make that first call before any stream capture.  Every call shares the
+ * array and it keeps the last call's contents (nothing in it needs to start
+ * at zero); calls that overlap on the GPU race on it.  stream: a CUDA stream
+ * handle, NULL for the legacy default stream. */
+tt_status tt_circus_zscore_noalloc(const float *d_sino, int rows, int cols, int n_sino,
+                                   const tt_pfunctional *pfuncs, int n_p, float *d_signatures,
+                                   void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,6 +22,7 @@ EXPORTS = (
     "tt_plan_create", "tt_plan_destroy", "tt_plan_synchronize", "tt_last_error", "tt_version",
     "tt_pad_geometry", "tt_ortho_size", "tt_angles_from_step", "tt_sinograms", "tt_circus",
     "tt_zscore", "tt_rotate", "tt_transform", "tt_sinograms_device", "tt_circus_device", "tt_zscore_device",
+    "tt_circus_zscore_noalloc",
 )
 
 
@@ -76,6 +77,8 @@ def lib():
         "tt_circus_device": [_P, _P, _int, _int, _int, ctypes.POINTER(PFunctionalC), _int, _I32,
                              _P, _P],
         "tt_zscore_device": [_P, _P, _int, _int, _P, _P],
+        "tt_circus_zscore_noalloc": [_P, _int, _int, _int, ctypes.POINTER(PFunctionalC), _int,
+                                     _P, _P],
     }
     for name, args in sig.items():
         fn = getattr(l, name)

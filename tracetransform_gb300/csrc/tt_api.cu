@@ -617,6 +617,11 @@ tt_status run_circus(tt_plan *p, const float *d_sino, int rows, int cols, int n_
 
 } // namespace
 
+int tt::record_error(int status, const char *message) {
+    g_error = message;
+    return status;
+}
+
 // ---- C ABI ---------------------------------------------------------------------
 
 extern "C" {

@@ -54,6 +54,9 @@ int p3_fft_length(int n);
 void p3_tables(int n, float2 *chirp, float2 *filt, float2 *twid, float *lin,
                std::complex<double> *work);
 
+// Record a failure for tt_last_error() on this thread; returns status.
+int record_error(int status, const char *message);
+
 // Opt-in shared memory per block minus the kernel's static shared memory.
 size_t dynamic_smem_limit(const void *kernel);
 
