@@ -31,6 +31,16 @@ __device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
     return d;
 }
 
+// Correctly rounded sqrt of a non-negative sample.  Zero (frequent: the
+// zero samples at the ends of every line) would send the IEEE square root
+// down its divergent special-case path; it is answered directly instead, and
+// the result is the same as sqrtf's.
+__device__ __forceinline__ float sqrt_nn(float v) {
+    const bool pos = v > 0.f;
+    const float r = __fsqrt_rn(pos ? v : 1.f);
+    return pos ? r : (v == 0.f ? 0.f : __fsqrt_rn(v));
+}
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1)

@@ -169,7 +169,7 @@ __device__ float sel_list_sqrt(float *keys, int count, float klo, float khi, flo
         __syncwarp();
         for (int i = lane; i < count; i += 32) {
             const float k = keys[i];
-            atomicAdd(sc->hist + sel_bin(k, klo, bs), __float2uint_rn(__fsqrt_rn(k) * qs));
+            atomicAdd(sc->hist + sel_bin(k, klo, bs), __float2uint_rn(sqrt_nn(k) * qs));
         }
         __syncwarp();
         const int d = sel_pick_bin(sc->hist, &below, total, lane);
@@ -198,7 +198,7 @@ __device__ float sel_list_sqrt(float *keys, int count, float klo, float khi, flo
         return klo;
     for (int i = lane; i < count; i += 32) {
         sc->key[i] = __float_as_uint(keys[i]);
-        sc->w[i] = __float2uint_rn(__fsqrt_rn(keys[i]) * qs);
+        sc->w[i] = __float2uint_rn(sqrt_nn(keys[i]) * qs);
     }
     __syncwarp();
     return sel_finish(sc, count, below, total, khi, lane);
@@ -221,7 +221,7 @@ __device__ float sel_refine(const float *x, int jlo, int j0, int j1, int per, Ke
             const float v = x[j - jlo];
             const float k = keyfn(j, v);
             if (k >= klo && k <= khi)
-                atomicAdd(sc->hist + sel_bin(k, klo, bs), __float2uint_rn(__fsqrt_rn(v) * qs));
+                atomicAdd(sc->hist + sel_bin(k, klo, bs), __float2uint_rn(sqrt_nn(v) * qs));
         }
         __syncwarp();
         const int d = sel_pick_bin(sc->hist, &below, total, lane);
@@ -238,7 +238,7 @@ __device__ float sel_refine(const float *x, int jlo, int j0, int j1, int per, Ke
                 k = keyfn(j, v);
                 if (k >= klo && k <= khi && sel_bin(k, klo, bs) == d) {
                     in = true;
-                    wq = __float2uint_rn(__fsqrt_rn(v) * qs);
+                    wq = __float2uint_rn(sqrt_nn(v) * qs);
                     bmin = fminf(bmin, k);
                     bmax = fmaxf(bmax, k);
                 }
@@ -292,16 +292,26 @@ __device__ void select_t67(float *x, int jlo, int jhi, int m1, int m2, bool want
     }
     __syncwarp();
     unsigned l6 = 0, l7 = 0;
-    for (int j = j0; j < j1; j++) {
-        const float v = x[j - jlo];
-        const unsigned wq = __float2uint_rn(__fsqrt_rn(v) * qs);
-        if (want7 && j >= b7) {
-            l7 += wq;
-            atomicAdd(s7->hist + sel_bin(v, 0.f, bs7), wq);
-        }
-        if (want6 && j >= b6) {
-            l6 += wq;
-            atomicAdd(s6->hist + sel_bin(key6(j, v), 0.f, bs6), wq);
+    for (int jb = j0; jb < j1; jb += 4) {
+        float vb[4]; // four loads in flight before the atomics
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            vb[u] = jb + u < j1 ? x[jb + u - jlo] : 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int j = jb + u;
+            if (j >= j1)
+                break;
+            const float v = vb[u];
+            const unsigned wq = __float2uint_rn(sqrt_nn(v) * qs);
+            if (want7 && j >= b7) {
+                l7 += wq;
+                atomicAdd(s7->hist + sel_bin(v, 0.f, bs7), wq);
+            }
+            if (want6 && j >= b6) {
+                l6 += wq;
+                atomicAdd(s6->hist + sel_bin(key6(j, v), 0.f, bs6), wq);
+            }
         }
     }
     const unsigned long long W7 = __reduce_add_sync(TT_FULL_MASK, l7);
@@ -324,7 +334,7 @@ __device__ void select_t67(float *x, int jlo, int jhi, int m1, int m2, bool want
                 k = key6(j, v);
                 if (j >= b6 && sel_bin(k, 0.f, bs6) == d) {
                     in = true;
-                    wq = __float2uint_rn(__fsqrt_rn(v) * qs);
+                    wq = __float2uint_rn(sqrt_nn(v) * qs);
                     mn = fminf(mn, k);
                     mx = fmaxf(mx, k);
                 }

@@ -84,7 +84,7 @@ __device__ __forceinline__ int resolve_median(int found, float total, int jlo,
 
 template <bool kSqrt>
 __device__ __forceinline__ float elem(const float *x, int i) {
-    return kSqrt ? __fsqrt_rn(x[i]) : x[i];
+    return kSqrt ? sqrt_nn(x[i]) : x[i];
 }
 
 // First element i (of the chunked line) with 2 * prefix_i >= total, given the
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(32 * L)
         if (kSel)
             lmax = fmaxf(lmax, v);
         if (need_sq)
-            totq += __fsqrt_rn(v);
+            totq += sqrt_nn(v);
     }
     const float inc = warp_incl_scan(tot, lane);
     const float S = __shfl_sync(TT_FULL_MASK, inc, 31);
