@@ -61,6 +61,11 @@ def parse_args():
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel-only", type=int, default=0, metavar="CALLS",
+                    help="for profiler captures: run only the fused sinogram kernel CALLS "
+                         "times on the workload and exit (prints no bench line)")
+    ap.add_argument("--tfuncs", default=None,
+                    help="comma-separated T-functional ids overriding the workload's")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="target CPU time of the baseline sample")
     return ap.parse_args()
@@ -360,8 +365,24 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
+def run_kernel_only(args):
+    import torch
+    from tracetransform_gb300.device import Engine, to_colmajor
+    img, angles, tfs, _ = make_image(args.workload)
+    if args.tfuncs:
+        tfs = [int(t) for t in args.tfuncs.split(",")]
+    eng = Engine(0)
+    dev = to_colmajor(torch.from_numpy(np.ascontiguousarray(img)).cuda())
+    for _ in range(args.kernel_only):
+        eng.sinograms(dev, img.shape[0], img.shape[1], angles, tfs)
+    torch.cuda.synchronize()
+
+
 def main():
     args = parse_args()
+    if args.kernel_only:
+        run_kernel_only(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
