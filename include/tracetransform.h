@@ -171,6 +171,36 @@ tt_status tt_zscore_device(tt_plan *plan, const float *d_in, int n_vec, int len,
 /* Synchronise the plan's stream. */
 tt_status tt_plan_synchronize(tt_plan *plan);
 
+/* ---- batched engine ------------------------------------------------------ */
+/* Many images of uneven sizes and angle counts in one pass: the reference
+ * transforms its inputs one after another (the demo's loop over files and
+ * components, c++/src/demo.cpp:179-254, each a Transformer::getTransform,
+ * c++/src/transform.cpp:49-112; the CUDA port gives each GPU thread one
+ * image, cuda/src/demo.cpp:258-266).  Image i is rows[i] x cols[i],
+ * column-major, at images + offsets[i] (elements); it is transformed with
+ * 360 / angle_steps[i] angles (integer degrees), the T- and P-functionals
+ * given (P1-P3; Hermite is TT_ERR_UNSUPPORTED here).  circus and signatures
+ * receive, image after image, each image's n_t x n_p x A_i block (the layout
+ * of tt_transform).  The first call for a batch shape (sizes, steps,
+ * functionals, input pointer) builds per-image textures and per-size tables,
+ * times the persistent kernel's tile shapes on the batch (the choice is kept
+ * in $TT_AUTOTUNE_CACHE, default ~/.cache/tracetransform_gb300_autotune.json)
+ * and captures one CUDA graph: work-counter reset, image copies, a persistent
+ * sinogram kernel, the batched P-functional kernel and the batched z-score;
+ * later calls of that shape replay the graph. */
+tt_status tt_transform_batch(tt_plan *plan, const float *images, const int64_t *offsets,
+                             const int32_t *rows, const int32_t *cols, const int32_t *angle_steps,
+                             int n_images, const int32_t *tfuncs, int n_t,
+                             const tt_pfunctional *pfuncs, int n_p, float *circus,
+                             float *signatures);
+/* The same on device buffers, ordered on stream (NULL: the plan's stream);
+ * d_circus / d_signatures may be NULL. */
+tt_status tt_transform_batch_device(tt_plan *plan, const float *d_images, const int64_t *offsets,
+                                    const int32_t *rows, const int32_t *cols,
+                                    const int32_t *angle_steps, int n_images,
+                                    const int32_t *tfuncs, int n_t, const tt_pfunctional *pfuncs,
+                                    int n_p, float *d_circus, float *d_signatures, void *stream);
+
 /* ---- allocation-free entry point ---------------------------------------- */
 /* No counterpart in the reference.  P1 / P2 / P3 circus functions of n_sino
  * stacked rows x cols sinograms (device), z-scored into d_signatures

@@ -5,13 +5,15 @@ Transformer: hand-written sm_103a CUDA kernels behind the C ABI of
 include/tracetransform.h (libtt_gb300.so), with this package as the Python
 host side.  Build the library with ``python -m tracetransform_gb300.build``.
 """
+from . import api
 from .api import (PFunctional, PFunctionalWrapper, Plan, TFunctional, TFunctionalWrapper,
                   Transformer, ValidationError, angles_from_step, getCircusFunctions,
-                  getSinograms, ortho_size, pad, pad_geometry, writecsv, zscore)
+                  getSinograms, ortho_size, pad, pad_geometry, rotate, transform_batch,
+                  writecsv, zscore)
 
 __all__ = [
     "PFunctional", "PFunctionalWrapper", "Plan", "TFunctional", "TFunctionalWrapper",
     "Transformer", "ValidationError", "angles_from_step", "getCircusFunctions", "getSinograms",
-    "ortho_size", "pad", "pad_geometry", "writecsv", "zscore",
+    "ortho_size", "pad", "pad_geometry", "rotate", "transform_batch", "writecsv", "zscore",
 ]
 __version__ = "0.1.0"

@@ -22,7 +22,7 @@ EXPORTS = (
     "tt_plan_create", "tt_plan_destroy", "tt_plan_synchronize", "tt_last_error", "tt_version",
     "tt_pad_geometry", "tt_ortho_size", "tt_angles_from_step", "tt_sinograms", "tt_circus",
     "tt_zscore", "tt_rotate", "tt_transform", "tt_sinograms_device", "tt_circus_device", "tt_zscore_device",
-    "tt_circus_zscore_noalloc",
+    "tt_circus_zscore_noalloc", "tt_transform_batch", "tt_transform_batch_device",
 )
 
 
@@ -45,6 +45,7 @@ class PFunctionalC(ctypes.Structure):
 _lib = None
 _F = ctypes.POINTER(ctypes.c_float)
 _I32 = ctypes.POINTER(ctypes.c_int32)
+_I64 = ctypes.POINTER(ctypes.c_int64)
 _P = ctypes.c_void_p
 _int = ctypes.c_int
 
@@ -79,6 +80,10 @@ def lib():
         "tt_zscore_device": [_P, _P, _int, _int, _P, _P],
         "tt_circus_zscore_noalloc": [_P, _int, _int, _int, ctypes.POINTER(PFunctionalC), _int,
                                      _P, _P],
+        "tt_transform_batch": [_P, _F, _I64, _I32, _I32, _I32, _int, _I32, _int,
+                               ctypes.POINTER(PFunctionalC), _int, _F, _F],
+        "tt_transform_batch_device": [_P, _P, _I64, _I32, _I32, _I32, _int, _I32, _int,
+                                      ctypes.POINTER(PFunctionalC), _int, _P, _P, _P],
     }
     for name, args in sig.items():
         fn = getattr(l, name)

@@ -37,7 +37,7 @@ from ._native import PFunctionalC, check, fptr, iptr, lib
 __all__ = [
     "TFunctional", "PFunctional", "TFunctionalWrapper", "PFunctionalWrapper", "ValidationError",
     "pad", "pad_geometry", "ortho_size", "angles_from_step", "getSinograms", "getCircusFunctions",
-    "zscore", "Transformer", "writecsv", "Plan",
+    "zscore", "Transformer", "writecsv", "Plan", "transform_batch", "rotate",
 ]
 
 
@@ -271,6 +271,44 @@ def _ostream_float(v: float) -> str:
     if math.isinf(v):
         return "inf" if v > 0 else "-inf"
     return "%g" % v
+
+
+def transform_batch(images: Sequence, angle_stepsizes: Sequence[int], tfunctionals: Sequence,
+                    pfunctionals: Sequence, plan: Optional[Plan] = None):
+    """Transform many images of uneven sizes in one pass of the batched engine
+    (tt_transform_batch): returns, per image, (circus, signatures) with circus
+    of shape (nT, nP, A) and signatures the A x (nT * nP) matrix
+    Transformer.getTransform returns.  P1-P3 only."""
+    tfs = _as_tfunctionals(tfunctionals)
+    pfs = _as_pfunctionals(pfunctionals)
+    imgs = [np.asarray(im, dtype=np.float32) for im in images]
+    if len(angle_stepsizes) != len(imgs):
+        raise ValueError("one angle step per image")
+    bufs = [_colmajor(im) for im in imgs]
+    offsets = np.zeros(len(bufs), np.int64)
+    if bufs:
+        offsets[1:] = np.cumsum([b.size for b in bufs])[:-1]
+    flat = np.concatenate(bufs) if bufs else np.zeros(1, np.float32)
+    rows = np.array([im.shape[0] for im in imgs], np.int32)
+    cols = np.array([im.shape[1] for im in imgs], np.int32)
+    steps = np.array([int(s) for s in angle_stepsizes], np.int32)
+    ids = np.array([int(t.functional) for t in tfs], np.int32)
+    na = [360 // int(s) for s in steps]
+    total = sum(len(ids) * len(pfs) * a for a in na)
+    circus = np.zeros(max(total, 1), np.float32)
+    sig = np.zeros(max(total, 1), np.float32)
+    check(lib().tt_transform_batch(
+        _handle(plan), fptr(flat), offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+        iptr(rows), iptr(cols), iptr(steps), len(imgs), iptr(ids), len(ids), _pf_array(pfs),
+        len(pfs), fptr(circus), fptr(sig)))
+    out, at = [], 0
+    for a in na:
+        k = len(ids) * len(pfs) * a
+        c = circus[at:at + k].reshape(len(ids), len(pfs), a)
+        s = sig[at:at + k].reshape(len(ids) * len(pfs), a).T
+        out.append((c, s))
+        at += k
+    return out
 
 
 class Transformer:

@@ -131,18 +131,7 @@ std::vector<float> hermite_basis(int n, unsigned order, int center) {
     return b;
 }
 
-void pad_geometry(int rows, int cols, int *n, int *row_off, int *col_off) {
-    const float ox = (float)(std::floor((cols + 1) / 2.0) - 1);
-    const float oy = (float)(std::floor((rows + 1) / 2.0) - 1);
-    const float hx = (float)(cols - 1) - ox - 1;
-    const float hy = (float)(rows - 1) - oy - 1;
-    const int r_last = (int)std::ceil(std::hypot(hx, hy)) + 1;
-    const int nb = 2 * r_last + 1;
-    const float opad = (float)(std::floor((nb + 1) / 2.0) - 1);
-    *n = nb;
-    *col_off = (int)(opad - ox);
-    *row_off = (int)(opad - oy);
-}
+using tt::pad_geometry;
 
 int ortho_side(unsigned step) {
     const size_t ndiag = (int)std::ceil(360.0 / step);
@@ -276,8 +265,9 @@ struct tt_plan {
     std::map<std::tuple<int, int, int>, float *> herm;  // (n, order, center)
     std::map<std::vector<float>, float2 *> trig;        // angle list -> (c, s)
     std::map<std::vector<long>, const float **> herm_ptrs;
-    DevBuf in, sino, circ, sig, region, nos;
+    DevBuf in, sino, circ, sig, region, nos, batch_in, batch_out;
     SourceTexture src;
+    tt::BatchEngine *batch = nullptr;
     std::vector<void *> owned;
 
     ~tt_plan() {
@@ -287,10 +277,11 @@ struct tt_plan {
         if (stream)
             cudaStreamSynchronize(stream);
         cudaDeviceSynchronize();
+        tt::batch_destroy(batch);
         src.release();
         for (void *p : owned)
             cudaFree(p);
-        for (DevBuf *b : {&in, &sino, &circ, &sig, &region, &nos})
+        for (DevBuf *b : {&in, &sino, &circ, &sig, &region, &nos, &batch_in, &batch_out})
             cudaFree(b->p);
         if (stream)
             cudaStreamDestroy(stream);
@@ -368,8 +359,7 @@ struct tt_plan {
         }
         std::vector<float2> h(n_angles);
         for (int a = 0; a < n_angles; a++) {
-            const float ang = deg2rad(angles[a]);
-            h[a] = make_float2(std::cos(-ang), std::sin(-ang));
+            h[a] = tt::rotation(angles[a]);
         }
         float2 *d;
         TT_CHECK(upload(&d, h));
@@ -384,15 +374,8 @@ struct tt_plan {
             *out = it->second;
             return TT_OK;
         }
-        std::vector<float2> h((size_t)3 * n, make_float2(0.f, 0.f));
-        for (int r = 1; r < n; r++) {
-            h[r] = make_float2((float)(r * std::cos(5.0 * std::log((double)r))),
-                               (float)(r * std::sin(5.0 * std::log((double)r))));
-            h[n + r] = make_float2((float)std::cos(3.0 * std::log((double)r)),
-                                   (float)std::sin(3.0 * std::log((double)r)));
-            h[2 * n + r] = make_float2((float)(std::sqrt((double)r) * std::cos(4.0 * std::log((double)r))),
-                                       (float)(std::sqrt((double)r) * std::sin(4.0 * std::log((double)r))));
-        }
+        std::vector<float2> h((size_t)3 * n);
+        tt::t345_tables(n, h.data());
         float2 *d;
         TT_CHECK(upload(&d, h));
         t345[n] = d;
@@ -661,6 +644,88 @@ tt_status tt_plan_destroy(tt_plan *plan) {
             }
     }
     delete plan;
+    return TT_OK;
+}
+
+static tt_status check_batch(const int64_t *offsets, const int32_t *rows, const int32_t *cols,
+                             const int32_t *steps, int n_images, const int32_t *tfuncs, int n_t,
+                             const tt_pfunctional *pfuncs, int n_p, size_t *in_elems,
+                             size_t *out_elems) {
+    if (n_images < 0 || (n_images > 0 && (!offsets || !rows || !cols || !steps)))
+        return fail(TT_ERR_INVALID_ARG, "bad batch description");
+    unsigned need;
+    TT_CHECK(check_tfuncs(tfuncs, n_t, &need));
+    TT_CHECK(check_pfuncs(pfuncs, n_p, false, &need));
+    for (int p = 0; p < n_p; p++)
+        if (pfuncs[p].kind == TT_P_HERMITE)
+            return fail(TT_ERR_UNSUPPORTED,
+                        "the batched engine computes P1-P3; Hermite needs tt_transform");
+    size_t in = 0, out = 0;
+    for (int i = 0; i < n_images; i++) {
+        if (rows[i] <= 0 || cols[i] <= 0 || offsets[i] < 0 || steps[i] <= 0 || steps[i] > 360)
+            return fail(TT_ERR_INVALID_ARG, "batch image %d: %dx%d at %lld, step %d", i, rows[i],
+                        cols[i], (long long)offsets[i], steps[i]);
+        in = std::max(in, (size_t)offsets[i] + (size_t)rows[i] * cols[i]);
+        out += (size_t)n_t * n_p * (360 / steps[i]);
+    }
+    *in_elems = in;
+    *out_elems = out;
+    return TT_OK;
+}
+
+tt_status tt_transform_batch_device(tt_plan *plan, const float *d_images, const int64_t *offsets,
+                                    const int32_t *rows, const int32_t *cols,
+                                    const int32_t *angle_steps, int n_images,
+                                    const int32_t *tfuncs, int n_t, const tt_pfunctional *pfuncs,
+                                    int n_p, float *d_circus, float *d_signatures, void *stream) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    size_t in_elems, out_elems;
+    TT_CHECK(check_batch(offsets, rows, cols, angle_steps, n_images, tfuncs, n_t, pfuncs, n_p,
+                         &in_elems, &out_elems));
+    if (n_images == 0 || out_elems == 0)
+        return TT_OK;
+    if (!d_images)
+        return fail(TT_ERR_INVALID_ARG, "NULL image buffer");
+    if (!p->batch)
+        p->batch = tt::batch_create(p->device);
+    std::vector<long long> off(offsets, offsets + n_images);
+    const int st = tt::batch_run(p->batch, d_images, off.data(), rows, cols, angle_steps,
+                                 n_images, tfuncs, n_t, pfuncs, n_p, d_circus, d_signatures,
+                                 pick_stream(p, stream));
+    return (tt_status)st;
+}
+
+tt_status tt_transform_batch(tt_plan *plan, const float *images, const int64_t *offsets,
+                             const int32_t *rows, const int32_t *cols, const int32_t *angle_steps,
+                             int n_images, const int32_t *tfuncs, int n_t,
+                             const tt_pfunctional *pfuncs, int n_p, float *circus,
+                             float *signatures) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    size_t in_elems, out_elems;
+    TT_CHECK(check_batch(offsets, rows, cols, angle_steps, n_images, tfuncs, n_t, pfuncs, n_p,
+                         &in_elems, &out_elems));
+    if (n_images == 0 || out_elems == 0)
+        return TT_OK;
+    if (!images)
+        return fail(TT_ERR_INVALID_ARG, "NULL image buffer");
+    cudaStream_t st = p->stream;
+    TT_CHECK(p->ensure(p->batch_in, sizeof(float) * in_elems));
+    TT_CHECK(p->ensure(p->batch_out, sizeof(float) * 2 * out_elems));
+    TT_CUDA(cudaMemcpyAsync(p->batch_in.p, images, sizeof(float) * in_elems,
+                            cudaMemcpyHostToDevice, st));
+    float *d_circ = (float *)p->batch_out.p, *d_sig = d_circ + out_elems;
+    TT_CHECK(tt_transform_batch_device(p, (const float *)p->batch_in.p, offsets, rows, cols,
+                                       angle_steps, n_images, tfuncs, n_t, pfuncs, n_p, d_circ,
+                                       d_sig, st));
+    if (circus)
+        TT_CUDA(cudaMemcpyAsync(circus, d_circ, sizeof(float) * out_elems, cudaMemcpyDeviceToHost,
+                                st));
+    if (signatures)
+        TT_CUDA(cudaMemcpyAsync(signatures, d_sig, sizeof(float) * out_elems,
+                                cudaMemcpyDeviceToHost, st));
+    TT_CUDA(cudaStreamSynchronize(st));
     return TT_OK;
 }
 

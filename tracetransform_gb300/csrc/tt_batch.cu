@@ -1,0 +1,572 @@
+// tt_batch.cu -- batched engine: many images of uneven sizes and angle
+// counts transformed by one persistent sinogram launch, one batched
+// P-functional launch and one batched z-score launch, replayed as a CUDA
+// graph.
+//
+// Per batch shape (image sizes, angle steps, functionals) the engine builds
+// once: a gather-capable CUDA array and texture per image, the rotation and
+// T3-T5 tables of every distinct angle step and padded size, the P3 tables of
+// every distinct size, the work-item and column descriptors, and scratch for
+// the sinograms.  An autotuner times the persistent kernel's tile shapes
+// (lines per CTA, resident CTAs per SM) on the batch itself and remembers the
+// winner in a JSON file.  The graph holds the image copies into the texture
+// arrays, the three kernels and the work-counter reset; each call replays it.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include <sys/stat.h>
+
+#include "tracetransform.h"
+#include "tt_internal.h"
+
+namespace tt {
+namespace {
+
+int berr(int status, const char *msg) { return record_error(status, msg); }
+
+int cuda_err(cudaError_t e, const char *what) {
+    char buf[320];
+    snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+    return record_error(e == cudaErrorMemoryAllocation ? TT_ERR_OOM : TT_ERR_CUDA, buf);
+}
+
+#define B_CUDA(call)                                                           \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess)                                                 \
+            return cuda_err(e_, #call);                                        \
+    } while (0)
+
+#define B_CHECK(expr)                                                          \
+    do {                                                                       \
+        int s_ = (expr);                                                       \
+        if (s_ != TT_OK)                                                       \
+            return s_;                                                         \
+    } while (0)
+
+template <typename T> struct DevArray {
+    T *p = nullptr;
+    size_t n = 0;
+    ~DevArray() { cudaFree(p); }
+    int resize(size_t count) {
+        if (count <= n && p)
+            return TT_OK;
+        cudaFree(p);
+        p = nullptr;
+        n = 0;
+        B_CUDA(cudaMalloc(&p, sizeof(T) * std::max<size_t>(count, 1)));
+        n = count;
+        return TT_OK;
+    }
+    int upload(const std::vector<T> &h, cudaStream_t st) {
+        B_CHECK(resize(h.size()));
+        if (!h.empty()) {
+            B_CUDA(cudaMemcpyAsync(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, st));
+            B_CUDA(cudaStreamSynchronize(st));
+        }
+        return TT_OK;
+    }
+};
+
+struct ImageTexture {
+    cudaArray_t arr = nullptr;
+    cudaTextureObject_t tex = 0;
+    void release() {
+        if (tex)
+            cudaDestroyTextureObject(tex);
+        if (arr)
+            cudaFreeArray(arr);
+        tex = 0;
+        arr = nullptr;
+    }
+};
+
+// The shape a captured graph was built for.
+struct Shape {
+    std::vector<int> rows, cols, steps;
+    std::vector<long long> offsets;
+    std::vector<int> tf, pk;
+    const float *src = nullptr;
+    bool operator==(const Shape &o) const {
+        return rows == o.rows && cols == o.cols && steps == o.steps && offsets == o.offsets &&
+               tf == o.tf && pk == o.pk && src == o.src;
+    }
+};
+
+struct Tune {
+    int lines = 8, ctas_per_sm = 0;
+};
+
+std::string tune_cache_path() {
+    if (const char *p = getenv("TT_AUTOTUNE_CACHE"))
+        return p;
+    const char *home = getenv("HOME");
+    return std::string(home ? home : "/tmp") + "/.cache/tracetransform_gb300_autotune.json";
+}
+
+// The cache is a flat JSON object {"key": [lines, ctas_per_sm], ...}.
+std::map<std::string, Tune> load_tune_cache() {
+    std::map<std::string, Tune> m;
+    std::ifstream f(tune_cache_path());
+    if (!f)
+        return m;
+    std::stringstream ss;
+    ss << f.rdbuf();
+    const std::string s = ss.str();
+    size_t pos = 0;
+    while ((pos = s.find('"', pos)) != std::string::npos) {
+        const size_t end = s.find('"', pos + 1);
+        if (end == std::string::npos)
+            break;
+        const std::string key = s.substr(pos + 1, end - pos - 1);
+        Tune t;
+        if (sscanf(s.c_str() + end + 1, " : [ %d , %d ]", &t.lines, &t.ctas_per_sm) == 2)
+            m[key] = t;
+        pos = end + 1;
+    }
+    return m;
+}
+
+void save_tune_cache(const std::map<std::string, Tune> &m) {
+    const std::string path = tune_cache_path();
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos)
+        mkdir(path.substr(0, slash).c_str(), 0755); // the cache's folder, if missing
+    std::ofstream f(path);
+    if (!f)
+        return;
+    f << "{\n";
+    size_t i = 0;
+    for (const auto &kv : m)
+        f << "  \"" << kv.first << "\": [" << kv.second.lines << ", " << kv.second.ctas_per_sm
+          << "]" << (++i < m.size() ? ",\n" : "\n");
+    f << "}\n";
+}
+
+} // namespace
+
+class BatchEngine {
+  public:
+    explicit BatchEngine(int device) : device_(device) {}
+    ~BatchEngine() { release(); }
+
+    int run(const float *d_images, const long long *offsets, const int *rows, const int *cols,
+            const int *steps, int n_img, const int32_t *tfuncs, int n_t,
+            const tt_pfunctional *pf, int n_p, float *d_circus, float *d_sig, cudaStream_t st);
+
+  private:
+    int build(cudaStream_t st);
+    int make_desc(int lines, std::vector<BatchImage> &desc, int *total_items) const;
+    int set_tile(int lines, cudaStream_t st);
+    int autotune(cudaStream_t st);
+    int capture(cudaStream_t st);
+    void release();
+
+    int device_;
+    Shape shape_;
+    bool built_ = false;
+    std::vector<ImageTexture> tex_;
+    std::vector<int> n_, ro_, co_, na_, order_;
+    std::vector<long long> sino_off_, out_off_;
+    DevArray<BatchImage> img_;
+    DevArray<BatchCircusImage> cimg_;
+    DevArray<float2> trig_, tab_, tables_;
+    DevArray<float> lin_, sino_, circ_, sig_;
+    DevArray<unsigned> counter_;
+    DevArray<long long> voff_;
+    DevArray<int> vlen_;
+    BatchSinoArgs sargs_{};
+    BatchCircusArgs cargs_{};
+    size_t circ_smem_ = 0;
+    int circ_blocks_ = 0, n_vec_ = 0, n_max_ = 0;
+    size_t out_floats_ = 0;
+    std::vector<int> trig_off_, tab_off_;
+    Tune tune_;
+    size_t sino_smem_ = 0;
+    cudaGraphExec_t exec_ = nullptr;
+};
+
+void BatchEngine::release() {
+    if (exec_)
+        cudaGraphExecDestroy(exec_);
+    exec_ = nullptr;
+    for (auto &t : tex_)
+        t.release();
+    tex_.clear();
+    built_ = false;
+}
+
+// Work-item descriptors for a tile of `lines` lines per CTA, largest image first.
+int BatchEngine::make_desc(int lines, std::vector<BatchImage> &desc, int *total_items) const {
+    const int n_img = (int)shape_.rows.size();
+    desc.resize(n_img);
+    long long items = 0;
+    for (int k = 0; k < n_img; k++) {
+        const int i = order_[k];
+        BatchImage &d = desc[k];
+        d.tex = tex_[i].tex;
+        d.rows = shape_.rows[i];
+        d.cols = shape_.cols[i];
+        d.n = n_[i];
+        d.row_off = ro_[i];
+        d.col_off = co_[i];
+        d.n_angles = na_[i];
+        d.blocks = (n_[i] + lines - 1) / lines;
+        d.items_begin = (int)items;
+        d.trig_off = trig_off_[i];
+        d.tab_off = tab_off_[i];
+        d.sino_off = sino_off_[i];
+        items += (long long)d.blocks * d.n_angles;
+    }
+    if (items > 0x7fffffffLL)
+        return berr(TT_ERR_UNSUPPORTED, "batch has more than 2^31 work items");
+    *total_items = (int)items;
+    return TT_OK;
+}
+
+int BatchEngine::set_tile(int lines, cudaStream_t st) {
+    std::vector<BatchImage> desc;
+    int total = 0;
+    B_CHECK(make_desc(lines, desc, &total));
+    B_CHECK(img_.upload(desc, st));
+    sino_smem_ = sino_smem_bytes(n_max_, lines, sargs_.need);
+    B_CUDA(prepare_sino_batch(lines, sargs_.need & ((1u << 6) | (1u << 7)), sino_smem_));
+    sargs_.img = img_.p;
+    sargs_.total_items = total;
+    sargs_.stride = sino_stride(n_max_, lines);
+    return TT_OK;
+}
+
+int BatchEngine::build(cudaStream_t st) {
+    const int n_img = (int)shape_.rows.size();
+    const int n_t = (int)shape_.tf.size(), n_p = (int)shape_.pk.size();
+    n_.resize(n_img);
+    ro_.resize(n_img);
+    co_.resize(n_img);
+    na_.resize(n_img);
+    trig_off_.resize(n_img);
+    tab_off_.resize(n_img);
+    sino_off_.resize(n_img);
+    out_off_.resize(n_img);
+    n_max_ = 0;
+    long long sino_total = 0, out_total = 0;
+    for (int i = 0; i < n_img; i++) {
+        pad_geometry(shape_.rows[i], shape_.cols[i], &n_[i], &ro_[i], &co_[i]);
+        na_[i] = 360 / shape_.steps[i];
+        n_max_ = std::max(n_max_, n_[i]);
+        sino_off_[i] = sino_total;
+        out_off_[i] = out_total;
+        sino_total += (long long)n_t * na_[i] * n_[i];
+        out_total += (long long)n_t * n_p * na_[i];
+    }
+    out_floats_ = (size_t)out_total;
+    // textures (texel (u, v) = image row u, column v; border reads 0)
+    tex_.resize(n_img);
+    for (int i = 0; i < n_img; i++) {
+        if (shape_.rows[i] > 32768 || shape_.cols[i] > 32768)
+            return berr(TT_ERR_UNSUPPORTED, "batch image exceeds the 32768 texture-gather limit");
+        cudaChannelFormatDesc desc = cudaCreateChannelDesc<float>();
+        B_CUDA(cudaMallocArray(&tex_[i].arr, &desc, shape_.rows[i], shape_.cols[i],
+                               cudaArrayTextureGather));
+        cudaResourceDesc res{};
+        res.resType = cudaResourceTypeArray;
+        res.res.array.array = tex_[i].arr;
+        cudaTextureDesc td{};
+        td.addressMode[0] = cudaAddressModeBorder;
+        td.addressMode[1] = cudaAddressModeBorder;
+        td.filterMode = cudaFilterModePoint;
+        td.readMode = cudaReadModeElementType;
+        B_CUDA(cudaCreateTextureObject(&tex_[i].tex, &res, &td, nullptr));
+    }
+    // rotation tables per distinct step, T3-T5 and P3 tables per distinct size
+    std::vector<float2> trig, tab, tables;
+    std::vector<float> lin;
+    std::map<int, int> step_at, tab_at;
+    std::map<int, long long> chirp_at;
+    std::vector<BatchCircusImage> cimg(n_img);
+    int col_begin = 0;
+    size_t circ_smem = 0;
+    const bool p3 = std::find(shape_.pk.begin(), shape_.pk.end(), (int)TT_P3) != shape_.pk.end();
+    unsigned pneed = 0;
+    for (int k : shape_.pk)
+        pneed |= 1u << k;
+    for (int i = 0; i < n_img; i++) {
+        const int step = shape_.steps[i], n = n_[i];
+        if (!step_at.count(step)) {
+            step_at[step] = (int)trig.size();
+            for (int a = 0; a < 360 / step; a++)
+                trig.push_back(rotation((float)(a * step)));
+        }
+        trig_off_[i] = step_at[step];
+        if (!tab_at.count(n)) {
+            tab_at[n] = (int)tab.size();
+            tab.resize(tab.size() + 3 * (size_t)n);
+            t345_tables(n, tab.data() + tab_at[n]);
+        }
+        tab_off_[i] = tab_at[n];
+        BatchCircusImage &c = cimg[i];
+        c.rows = n;
+        c.cols = na_[i];
+        c.col_begin = col_begin;
+        col_begin += n_t * na_[i];
+        c.M = p3 ? p3_fft_length(n) : 2;
+        int sl = 1;
+        while (sl < n)
+            sl <<= 1;
+        c.sort_len = sl;
+        c.sino_off = sino_off_[i];
+        c.out_off = out_off_[i];
+        if (p3) {
+            if (!chirp_at.count(n)) {
+                const int M = c.M;
+                chirp_at[n] = (long long)tables.size();
+                const size_t base = tables.size();
+                tables.resize(base + n + M + M / 2);
+                const size_t lbase = lin.size();
+                lin.resize(lbase + n);
+                std::vector<std::complex<double>> work(M);
+                p3_tables(n, tables.data() + base, tables.data() + base + n,
+                          tables.data() + base + n + M, lin.data() + lbase, work.data());
+                tab_at[-n] = (int)lbase; // linspace offset, keyed by -n
+            }
+            c.chirp_off = chirp_at[n];
+            c.filt_off = c.chirp_off + n;
+            c.twid_off = c.filt_off + c.M;
+            c.lin_off = tab_at[-n];
+        } else {
+            c.chirp_off = c.filt_off = c.twid_off = c.lin_off = 0;
+        }
+        CircusArgs probe{};
+        probe.rows = n;
+        probe.M = c.M;
+        probe.sort_len = sl;
+        probe.need = pneed;
+        circ_smem = std::max(circ_smem, circus_smem_bytes(probe));
+    }
+    if (tables.empty())
+        tables.push_back(make_float2(0.f, 0.f));
+    if (lin.empty())
+        lin.push_back(0.f);
+    B_CHECK(trig_.upload(trig, st));
+    B_CHECK(tab_.upload(tab, st));
+    B_CHECK(tables_.upload(tables, st));
+    B_CHECK(lin_.upload(lin, st));
+    B_CHECK(cimg_.upload(cimg, st));
+    B_CHECK(sino_.resize((size_t)std::max<long long>(sino_total, 1)));
+    B_CHECK(circ_.resize(std::max<size_t>(out_floats_, 1)));
+    B_CHECK(sig_.resize(std::max<size_t>(out_floats_, 1)));
+    B_CHECK(counter_.resize(1));
+    // z-score vectors: n_t x n_p per image, length = its angle count
+    std::vector<long long> voff;
+    std::vector<int> vlen;
+    for (int i = 0; i < n_img; i++)
+        for (int v = 0; v < n_t * n_p; v++) {
+            voff.push_back(out_off_[i] + (long long)v * na_[i]);
+            vlen.push_back(na_[i]);
+        }
+    n_vec_ = (int)voff.size();
+    if (voff.empty()) {
+        voff.push_back(0);
+        vlen.push_back(0);
+    }
+    B_CHECK(voff_.upload(voff, st));
+    B_CHECK(vlen_.upload(vlen, st));
+    // work order: largest image first, for a short tail
+    order_.resize(n_img);
+    for (int i = 0; i < n_img; i++)
+        order_[i] = i;
+    std::stable_sort(order_.begin(), order_.end(), [&](int a, int b) {
+        return (double)n_[a] * n_[a] * na_[a] > (double)n_[b] * n_[b] * na_[b];
+    });
+    // kernel arguments (the work-item descriptors depend on the tile: set_tile)
+    unsigned tneed = 0;
+    unsigned long long code = 0;
+    for (int t = 0; t < n_t; t++) {
+        tneed |= 1u << shape_.tf[t];
+        code |= (unsigned long long)shape_.tf[t] << (3 * t);
+    }
+    sargs_ = BatchSinoArgs{};
+    sargs_.n_img = n_img;
+    sargs_.trig = trig_.p;
+    sargs_.tab = tab_.p;
+    sargs_.sino = sino_.p;
+    sargs_.counter = counter_.p;
+    sargs_.tf_code = code;
+    sargs_.n_t = n_t;
+    sargs_.need = tneed;
+    cargs_ = BatchCircusArgs{};
+    cargs_.img = cimg_.p;
+    cargs_.n_img = n_img;
+    cargs_.n_sino = n_t;
+    cargs_.n_p = n_p;
+    for (int p = 0; p < n_p; p++)
+        cargs_.kind[p] = shape_.pk[p];
+    cargs_.need = pneed;
+    cargs_.sino = sino_.p;
+    cargs_.tables = tables_.p;
+    cargs_.lin = lin_.p;
+    cargs_.out = circ_.p;
+    circ_blocks_ = col_begin;
+    circ_smem_ = circ_smem;
+    B_CUDA(prepare_circus_batch(circ_smem_));
+    built_ = true;
+    return TT_OK;
+}
+
+// Tile shapes: lines per CTA (columns per warp group) in {8, 4} and resident
+// CTAs per SM for the persistent grid; each candidate is timed on the batch.
+int BatchEngine::autotune(cudaStream_t st) {
+    int dev_sms = 0;
+    B_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device_));
+    cudaDeviceProp prop;
+    B_CUDA(cudaGetDeviceProperties(&prop, device_));
+    int n_min = n_max_;
+    long long angles = 0;
+    for (int i = 0; i < (int)n_.size(); i++) {
+        n_min = std::min(n_min, n_[i]);
+        angles += na_[i];
+    }
+    std::ostringstream key;
+    key << prop.name << "|n" << n_min << "-" << n_max_ << "|imgs" << n_.size() << "|angles"
+        << angles << "|need" << sargs_.need;
+    std::map<std::string, Tune> cache = load_tune_cache();
+    auto hit = cache.find(key.str());
+    if (hit != cache.end()) {
+        tune_ = hit->second;
+        return set_tile(tune_.lines, st);
+    }
+    // load the images once so the timed runs see real data
+    for (int i = 0; i < (int)n_.size(); i++)
+        B_CUDA(cudaMemcpy2DToArrayAsync(tex_[i].arr, 0, 0, shape_.src + shape_.offsets[i],
+                                        sizeof(float) * shape_.rows[i],
+                                        sizeof(float) * shape_.rows[i], shape_.cols[i],
+                                        cudaMemcpyDeviceToDevice, st));
+    cudaEvent_t e0, e1;
+    B_CUDA(cudaEventCreate(&e0));
+    B_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    Tune best_t;
+    const bool sel = sargs_.need & ((1u << 6) | (1u << 7));
+    for (int lines : {8, 4}) {
+        const size_t smem = sino_smem_bytes(n_max_, lines, sargs_.need);
+        const int occ = sino_batch_occupancy(lines, sel, smem);
+        if (occ <= 0)
+            continue;
+        B_CHECK(set_tile(lines, st));
+        for (int per_sm : {occ, std::max(1, occ / 2)}) {
+            float ms = 0.f;
+            for (int rep = 0; rep < 2; rep++) { // first run warms up
+                B_CUDA(cudaMemsetAsync(counter_.p, 0, sizeof(unsigned), st));
+                B_CUDA(cudaEventRecord(e0, st));
+                B_CUDA(launch_sino_batch(sargs_, lines, per_sm * dev_sms, sino_smem_, st));
+                B_CUDA(cudaEventRecord(e1, st));
+                B_CUDA(cudaEventSynchronize(e1));
+                B_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            }
+            if (ms < best) {
+                best = ms;
+                best_t.lines = lines;
+                best_t.ctas_per_sm = per_sm;
+            }
+            if (per_sm == 1)
+                break;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best_t.ctas_per_sm == 0)
+        return berr(TT_ERR_UNSUPPORTED, "no tile shape fits the batch's largest image");
+    tune_ = best_t;
+    cache[key.str()] = tune_;
+    save_tune_cache(cache);
+    return set_tile(tune_.lines, st);
+}
+
+int BatchEngine::capture(cudaStream_t st) {
+    if (exec_) {
+        cudaGraphExecDestroy(exec_);
+        exec_ = nullptr;
+    }
+    int dev_sms = 0;
+    B_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device_));
+    cudaGraph_t graph = nullptr;
+    B_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemsetAsync(counter_.p, 0, sizeof(unsigned), st);
+    for (int i = 0; e == cudaSuccess && i < (int)n_.size(); i++)
+        e = cudaMemcpy2DToArrayAsync(tex_[i].arr, 0, 0, shape_.src + shape_.offsets[i],
+                                     sizeof(float) * shape_.rows[i],
+                                     sizeof(float) * shape_.rows[i], shape_.cols[i],
+                                     cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+        e = launch_sino_batch(sargs_, tune_.lines, tune_.ctas_per_sm * dev_sms, sino_smem_, st);
+    if (e == cudaSuccess)
+        e = launch_circus_batch(cargs_, circ_blocks_, circ_smem_, st);
+    if (e == cudaSuccess)
+        e = launch_zscore_batch(circ_.p, voff_.p, vlen_.p, n_vec_, sig_.p, st);
+    const cudaError_t e_end = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess) {
+        if (graph)
+            cudaGraphDestroy(graph);
+        return cuda_err(e, "batch graph capture");
+    }
+    B_CUDA(e_end);
+    e = cudaGraphInstantiate(&exec_, graph, 0);
+    cudaGraphDestroy(graph);
+    B_CUDA(e);
+    return TT_OK;
+}
+
+int BatchEngine::run(const float *d_images, const long long *offsets, const int *rows,
+                     const int *cols, const int *steps, int n_img, const int32_t *tfuncs,
+                     int n_t, const tt_pfunctional *pf, int n_p, float *d_circus, float *d_sig,
+                     cudaStream_t st) {
+    Shape s;
+    s.rows.assign(rows, rows + n_img);
+    s.cols.assign(cols, cols + n_img);
+    s.steps.assign(steps, steps + n_img);
+    s.offsets.assign(offsets, offsets + n_img);
+    for (int t = 0; t < n_t; t++)
+        s.tf.push_back(tfuncs[t]);
+    for (int p = 0; p < n_p; p++)
+        s.pk.push_back(pf[p].kind);
+    s.src = d_images;
+    if (!built_ || !(s == shape_)) {
+        B_CUDA(cudaDeviceSynchronize()); // kernels of the old shape may still read its arrays
+        release();
+        shape_ = s;
+        B_CHECK(build(st));
+        B_CHECK(autotune(st));
+        B_CHECK(capture(st));
+    }
+    B_CUDA(cudaGraphLaunch(exec_, st));
+    if (d_circus)
+        B_CUDA(cudaMemcpyAsync(d_circus, circ_.p, sizeof(float) * out_floats_,
+                               cudaMemcpyDeviceToDevice, st));
+    if (d_sig)
+        B_CUDA(cudaMemcpyAsync(d_sig, sig_.p, sizeof(float) * out_floats_,
+                               cudaMemcpyDeviceToDevice, st));
+    return TT_OK;
+}
+
+BatchEngine *batch_create(int device) { return new BatchEngine(device); }
+
+void batch_destroy(BatchEngine *b) { delete b; }
+
+int batch_run(BatchEngine *b, const float *d_images, const long long *offsets, const int *rows,
+              const int *cols, const int *steps, int n_img, const int32_t *tfuncs, int n_t,
+              const tt_pfunctional *pf, int n_p, float *d_circus, float *d_sig,
+              cudaStream_t st) {
+    return b->run(d_images, offsets, rows, cols, steps, n_img, tfuncs, n_t, pf, n_p, d_circus,
+                  d_sig, st);
+}
+
+} // namespace tt

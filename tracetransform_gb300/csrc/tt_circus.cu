@@ -27,12 +27,34 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-__global__ void __launch_bounds__(kThreads) circus_kernel(const CircusArgs a) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ float red[kThreads / 32];
-    __shared__ int redi[kThreads / 32];
+// z-score of one vector by one block, in the reference's order.
+__device__ __forceinline__ void zscore_vector(const float *__restrict__ x, int len,
+                                              float *__restrict__ z) {
+    __shared__ float s_mean, s_std;
+    if (threadIdx.x == 0) {
+        float sum = 0.f;
+        for (int i = 0; i < len; i++)
+            sum = __fadd_rn(sum, x[i]);
+        const float mean = __fdiv_rn(sum, (float)len);
+        double acc = 0.0;
+        for (int i = 0; i < len; i++) {
+            const double d = (double)__fsub_rn(x[i], mean);
+            acc = __dadd_rn(acc, __dmul_rn(d, d));
+        }
+        s_mean = mean;
+        s_std = (float)sqrt(acc / (double)(len - 1));
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < len; i += blockDim.x)
+        z[i] = __fdiv_rn(__fsub_rn(x[i], s_mean), s_std);
+}
+
+// All requested P-functionals of column colidx of sinogram sidx.  Every thread
+// of the block calls it (it synchronises the block); smraw is the dynamic
+// shared memory sized by circus_smem_bytes.
+__device__ __forceinline__ void circus_column(const CircusArgs &a, int sidx, int colidx,
+                                              unsigned char *smraw, float *red, int *redi) {
     const int tid = threadIdx.x, bd = blockDim.x;
-    const int colidx = blockIdx.x, sidx = blockIdx.y;
     const int rows = a.rows, M = a.M, P = a.sort_len;
     const bool need_p2 = a.need & (1u << 2), need_p3 = a.need & (1u << 3);
 
@@ -190,27 +212,59 @@ __global__ void __launch_bounds__(kThreads) circus_kernel(const CircusArgs a) {
     }
 }
 
+__global__ void __launch_bounds__(kThreads) circus_kernel(const CircusArgs a) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ float red[kThreads / 32];
+    __shared__ int redi[kThreads / 32];
+    circus_column(a, blockIdx.y, blockIdx.x, smraw, red, redi);
+}
+
+// Batched P-stage: block b handles one column of one sinogram of one image;
+// images differ in sinogram length (rows), angle count (cols) and tables.
+__global__ void __launch_bounds__(kThreads) circus_batch_kernel(const BatchCircusArgs b) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ float red[kThreads / 32];
+    __shared__ int redi[kThreads / 32];
+    const int blk = blockIdx.x;
+    int lo = 0, hi = b.n_img - 1; // image whose column range holds blk
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (b.img[mid].col_begin <= blk)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const BatchCircusImage im = b.img[lo];
+    const int k = blk - im.col_begin; // = sinogram * cols + column
+    CircusArgs a{};
+    a.sino = b.sino + im.sino_off;
+    a.rows = im.rows;
+    a.cols = im.cols;
+    a.n_sino = b.n_sino;
+    a.n_p = b.n_p;
+    for (int p = 0; p < b.n_p; p++)
+        a.kind[p] = b.kind[p];
+    a.chirp = b.tables + im.chirp_off;
+    a.filt = b.tables + im.filt_off;
+    a.twid = b.tables + im.twid_off;
+    a.lin = b.lin + im.lin_off;
+    a.M = im.M;
+    a.sort_len = im.sort_len;
+    a.need = b.need;
+    a.out = b.out + im.out_off;
+    circus_column(a, k / im.cols, k % im.cols, smraw, red, redi);
+}
+
+// z-score of vectors of varying length: vector v is in[off[v] .. off[v] + len[v]).
+__global__ void zscore_batch_kernel(const float *__restrict__ in, const long long *__restrict__ off,
+                                    const int *__restrict__ len, float *__restrict__ out) {
+    const long long o = off[blockIdx.x];
+    zscore_vector(in + o, len[blockIdx.x], out + o);
+}
+
 __global__ void zscore_kernel(const float *__restrict__ in, int len,
                               float *__restrict__ out) {
-    __shared__ float s_mean, s_std;
-    const float *x = in + (size_t)blockIdx.x * len;
-    float *z = out + (size_t)blockIdx.x * len;
-    if (threadIdx.x == 0) {
-        float sum = 0.f;
-        for (int i = 0; i < len; i++)
-            sum = __fadd_rn(sum, x[i]);
-        const float mean = __fdiv_rn(sum, (float)len);
-        double acc = 0.0;
-        for (int i = 0; i < len; i++) {
-            const double d = (double)__fsub_rn(x[i], mean);
-            acc = __dadd_rn(acc, __dmul_rn(d, d));
-        }
-        s_mean = mean;
-        s_std = (float)sqrt(acc / (double)(len - 1));
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < len; i += blockDim.x)
-        z[i] = __fdiv_rn(__fsub_rn(x[i], s_mean), s_std);
+    zscore_vector(in + (size_t)blockIdx.x * len, len, out + (size_t)blockIdx.x * len);
 }
 
 } // namespace
@@ -247,6 +301,35 @@ cudaError_t launch_zscore(const float *in, int n_vec, int len, float *out,
     if (n_vec <= 0 || len <= 0)
         return cudaSuccess;
     zscore_kernel<<<n_vec, 128, 0, stream>>>(in, len, out);
+    return cudaGetLastError();
+}
+
+cudaError_t prepare_circus_batch(size_t smem) {
+    static size_t limit = 0;
+    if (limit == 0) {
+        limit = dynamic_smem_limit((const void *)circus_batch_kernel);
+        cudaError_t e = cudaFuncSetAttribute(circus_batch_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)limit);
+        if (e != cudaSuccess)
+            return e;
+    }
+    return smem > limit ? cudaErrorInvalidValue : cudaSuccess;
+}
+
+cudaError_t launch_circus_batch(const BatchCircusArgs &a, int blocks, size_t smem,
+                                cudaStream_t stream) {
+    if (blocks <= 0)
+        return cudaSuccess;
+    circus_batch_kernel<<<blocks, kThreads, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zscore_batch(const float *in, const long long *off, const int *len,
+                                int n_vec, float *out, cudaStream_t stream) {
+    if (n_vec <= 0)
+        return cudaSuccess;
+    zscore_batch_kernel<<<n_vec, 128, 0, stream>>>(in, off, len, out);
     return cudaGetLastError();
 }
 

@@ -7,6 +7,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "tracetransform.h"
+
 namespace tt {
 
 constexpr int kMaxT = 16; // T-functional entries per call
@@ -54,11 +56,73 @@ int p3_fft_length(int n);
 void p3_tables(int n, float2 *chirp, float2 *filt, float2 *twid, float *lin,
                std::complex<double> *work);
 
+// Rotation (cos(-theta), sin(-theta)) of an angle in degrees and the T3-T5
+// kernels (3 n entries) as the reference rounds them (tt_tables.cu).
+float2 rotation(float degrees);
+void t345_tables(int n, float2 *out);
+
+// pad() geometry of c++/src/auxiliary.cpp:257-275 (tt_tables.cu).
+void pad_geometry(int rows, int cols, int *n, int *row_off, int *col_off);
+
+// The batched engine (tt_batch.cu): one per plan, rebuilt when the batch shape
+// changes.  batch_run returns a tt_status.
+class BatchEngine;
+BatchEngine *batch_create(int device);
+void batch_destroy(BatchEngine *b);
+int batch_run(BatchEngine *b, const float *d_images, const long long *offsets, const int *rows,
+              const int *cols, const int *steps, int n_img, const int32_t *tfuncs, int n_t,
+              const tt_pfunctional *pf, int n_p, float *d_circus, float *d_sig,
+              cudaStream_t st);
+
 // Record a failure for tt_last_error() on this thread; returns status.
 int record_error(int status, const char *message);
 
 // Opt-in shared memory per block minus the kernel's static shared memory.
 size_t dynamic_smem_limit(const void *kernel);
+
+// Batched P-stage: one image's sinogram stack and tables.
+struct BatchCircusImage {
+    int rows, cols;        // sinogram length N and angle count A
+    int col_begin;         // first block index: blocks are n_sino * cols per image
+    int M, sort_len;       // P3 FFT length, power-of-two sort length
+    long long sino_off;    // into sino (n_sino x cols x rows floats)
+    long long out_off;     // into out (n_sino x n_p x cols floats)
+    long long chirp_off, filt_off, twid_off; // into tables (float2)
+    long long lin_off;     // into lin (float)
+};
+
+struct BatchCircusArgs {
+    const BatchCircusImage *img;
+    int n_img, n_sino, n_p;
+    int kind[kMaxP];
+    unsigned need;
+    const float *sino;
+    const float2 *tables;
+    const float *lin;
+    float *out;
+};
+
+// Batched sinograms: one image of a batch (device descriptor).
+struct BatchImage {
+    cudaTextureObject_t tex; // the image, texel (u, v) = (row, col)
+    int rows, cols, n, row_off, col_off;
+    int n_angles, blocks;    // angles; CTA line blocks per angle, ceil(n / L)
+    int items_begin;         // first work item (angle * blocks + block)
+    int trig_off, tab_off;   // into trig (per angle) and tab (3 n)
+    long long sino_off;      // into sino (n_t x n_angles x n floats)
+};
+
+struct BatchSinoArgs {
+    const BatchImage *img;
+    int n_img, total_items;
+    const float2 *trig, *tab;
+    float *sino;
+    unsigned *counter;       // work counter, zero before the launch
+    unsigned long long tf_code; // T id of output t in bits [3t, 3t + 3)
+    int n_t;
+    unsigned need;
+    int stride;              // floats per line buffer (for the largest n)
+};
 
 int sino_lines_per_block(int n, unsigned need);
 size_t sino_smem_bytes(int n, int lines, unsigned need);
@@ -72,5 +136,17 @@ cudaError_t launch_circus(const CircusArgs &a, cudaStream_t stream);
 size_t circus_smem_bytes(const CircusArgs &a);
 cudaError_t launch_zscore(const float *in, int n_vec, int len, float *out,
                           cudaStream_t stream);
+
+// Batched engine kernels.  The persistent sinogram kernel runs `grid` CTAs
+// that claim work items from *counter; lines = 4 or 8.
+cudaError_t prepare_sino_batch(int lines, bool sel, size_t smem);
+int sino_batch_occupancy(int lines, bool sel, size_t smem);
+cudaError_t launch_sino_batch(const BatchSinoArgs &a, int lines, int grid, size_t smem,
+                              cudaStream_t stream);
+cudaError_t prepare_circus_batch(size_t smem);
+cudaError_t launch_circus_batch(const BatchCircusArgs &a, int blocks, size_t smem,
+                                cudaStream_t stream);
+cudaError_t launch_zscore_batch(const float *in, const long long *off, const int *len,
+                                int n_vec, float *out, cudaStream_t stream);
 
 } // namespace tt

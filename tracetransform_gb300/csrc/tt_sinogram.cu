@@ -124,39 +124,36 @@ __device__ int find_crossing_walk(const float *x, int C, float exc, float total,
     return warp_min(f);
 }
 
+// One CTA's unit of work: L adjacent lines (columns col0 ..) of one angle of
+// one image.
+struct BlockJob {
+    cudaTextureObject_t tex;
+    float tu, tv;     // texel coordinate = frame coordinate + (tu, tv)
+    int n, col0, angle;
+    float c, s;       // cos(-theta), sin(-theta) as the host rounded them
+    int roff, coff, rr, rc; // support region inside the frame
+    const float2 *tab;      // T3, T4, T5 kernels of this n
+    float *out;             // this image's n_t x n_angles x n sinogram stack
+    int32_t *medians;       // optional, same shape
+    size_t plane;           // n_angles * n
+};
+
+// The fused body: support, sampling, T-functionals of one BlockJob.  Every
+// thread of the CTA calls it; it synchronises the CTA but never returns early.
+// tf_code holds the T-functional id of output t in bits [3t, 3t + 3).
 template <int L, bool kSel>
-__global__ void __launch_bounds__(32 * L)
-    sino_kernel(const SinoArgs a) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ int s_range[2];
-    __shared__ int s_region[4];
-    float *sm = reinterpret_cast<float *>(smraw);
+__device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long tf_code,
+                                           int n_t, unsigned need, int stride, float *sm,
+                                           int *s_range) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int angle = blockIdx.y;
-    const int col0 = blockIdx.x * L;
-    const int n = a.n;
-    const float2 cs = a.trig[angle];
-    const float c = cs.x, s = cs.y;
+    const int angle = J.angle;
+    const int col0 = J.col0;
+    const int n = J.n;
+    const float c = J.c, s = J.s;
     const float o = (float)(n - 1) * 0.5f;
     const float nm1 = (float)(n - 1);
-
-    // Support region (static, or the non-zero box found on the device).
-    if (threadIdx.x == 0) {
-        if (a.dyn_region) {
-            s_region[0] = a.dyn_region[0];
-            s_region[1] = a.dyn_region[1];
-            s_region[2] = a.dyn_region[2];
-            s_region[3] = a.dyn_region[3];
-        } else {
-            s_region[0] = a.row_off;
-            s_region[1] = a.col_off;
-            s_region[2] = a.src_rows;
-            s_region[3] = a.src_cols;
-        }
-    }
-    __syncthreads();
-    const int roff = s_region[0], coff = s_region[1];
-    const int rr = max(s_region[2], 0), rc = max(s_region[3], 0);
+    const int roff = J.roff, coff = J.coff;
+    const int rr = max(J.rr, 0), rc = max(J.rc, 0);
 
     // 1. Row range shared by the CTA's lines.
     if (warp == 0) {
@@ -191,8 +188,8 @@ __global__ void __launch_bounds__(32 * L)
         const bool colok = col < n;
         const float X = (float)col - o;
         const float Xc = __fmul_rn(X, c), Xms = __fmul_rn(X, -s);
-        const float tu = 1.f - (float)a.tex_row_off, tv = 1.f - (float)a.tex_col_off;
-        float *dst = sm + l * a.stride;
+        const float tu = J.tu, tv = J.tv;
+        float *dst = sm + l * stride;
         const int first = warp * RPW + r; // this thread's rows: first + 32 i, i < C
         constexpr int U = 4;              // gathers in flight per thread
         for (int i0 = 0; i0 < C; i0 += U) {
@@ -211,7 +208,7 @@ __global__ void __launch_bounds__(32 * L)
                 xf[u] = __fsub_rn(qx, xi);
                 yf[u] = __fsub_rn(qy, yi);
                 // texel (u, v) = image (row, col); w/z/x/y = s00, s10, s01, s11
-                g[u] = tex2Dgather<float4>(a.tex, yi + tu, xi + tv, 0);
+                g[u] = tex2Dgather<float4>(J.tex, yi + tu, xi + tv, 0);
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
@@ -230,10 +227,8 @@ __global__ void __launch_bounds__(32 * L)
 
     // 3. One warp per line: T-functionals.
     const int col = col0 + warp;
-    if (col >= n)
-        return;
-    float *x = sm + warp * a.stride;
-    const unsigned need = a.need;
+    if (col < n) {
+    float *x = sm + warp * stride;
     const bool need_m1 = need & ((1u << 1) | (1u << 2) | (1u << 7));
     const bool need_m2 = need & ((1u << 3) | (1u << 4) | (1u << 5) | (1u << 6));
     const bool need_sq = need_m2 || (need & (1u << 7)); // sum of sqrt(x) wanted
@@ -291,7 +286,7 @@ __global__ void __launch_bounds__(32 * L)
     float r345[3] = {0.f, 0.f, 0.f};
     if (need & ((1u << 3) | (1u << 4) | (1u << 5))) {
         const bool w3 = need & (1u << 3), w4 = need & (1u << 4), w5 = need & (1u << 5);
-        const float2 *tab3 = a.tab, *tab4 = a.tab + n, *tab5 = a.tab + 2 * n;
+        const float2 *tab3 = J.tab, *tab4 = J.tab + n, *tab5 = J.tab + 2 * n;
         float re3 = 0.f, im3 = 0.f, re4 = 0.f, im4 = 0.f, re5 = 0.f, im5 = 0.f;
         const int lo = max(1, jlo - m2), hi = min(n - m2, jhi - m2);
         for (int q = lo + lane; q < hi; q += 32) {
@@ -329,7 +324,7 @@ __global__ void __launch_bounds__(32 * L)
 
     float r6v = 0.f, r7v = 0.f;
     if (kSel) {
-        SelScratch *scr = reinterpret_cast<SelScratch *>(sm + L * a.stride) + 2 * warp;
+        SelScratch *scr = reinterpret_cast<SelScratch *>(sm + L * stride) + 2 * warp;
         const float xmax = __int_as_float(warp_max(__float_as_int(lmax)));
         // T6: keys r1 * x[m2 + r1], r1 in [0, N - m2); T7: keys x[m1 ..]
         select_t67(x, jlo, jhi, m1, m2, need & (1u << 6), need & (1u << 7), xmax, Q, scr,
@@ -337,10 +332,10 @@ __global__ void __launch_bounds__(32 * L)
     }
 
     if (lane == 0) {
-        const size_t plane = (size_t)a.n_angles * n;
+        const size_t plane = J.plane;
         const size_t at = (size_t)angle * n + col;
-        for (int t = 0; t < a.n_t; t++) {
-            const int f = a.tf[t];
+        for (int t = 0; t < n_t; t++) {
+            const int f = (int)((tf_code >> (3 * t)) & 7ull);
             float v;
             int med;
             switch (f) {
@@ -353,10 +348,107 @@ __global__ void __launch_bounds__(32 * L)
             case 6: v = r6v; med = m2; break;
             default: v = r7v; med = m1; break;
             }
-            a.out[t * plane + at] = v;
-            if (a.medians)
-                a.medians[t * plane + at] = med;
+            J.out[t * plane + at] = v;
+            if (J.medians)
+                J.medians[t * plane + at] = med;
         }
+    }
+    } // col < n
+}
+
+template <int L, bool kSel>
+__global__ void __launch_bounds__(32 * L)
+    sino_kernel(const SinoArgs a) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ int s_range[2];
+    __shared__ int s_region[4];
+    // support region: static, or the non-zero box found on the device
+    if (threadIdx.x == 0) {
+        if (a.dyn_region) {
+            s_region[0] = a.dyn_region[0];
+            s_region[1] = a.dyn_region[1];
+            s_region[2] = a.dyn_region[2];
+            s_region[3] = a.dyn_region[3];
+        } else {
+            s_region[0] = a.row_off;
+            s_region[1] = a.col_off;
+            s_region[2] = a.src_rows;
+            s_region[3] = a.src_cols;
+        }
+    }
+    __syncthreads();
+    BlockJob J;
+    J.tex = a.tex;
+    J.tu = 1.f - (float)a.tex_row_off;
+    J.tv = 1.f - (float)a.tex_col_off;
+    J.n = a.n;
+    J.col0 = blockIdx.x * L;
+    J.angle = blockIdx.y;
+    const float2 cs = a.trig[blockIdx.y];
+    J.c = cs.x;
+    J.s = cs.y;
+    J.roff = s_region[0];
+    J.coff = s_region[1];
+    J.rr = s_region[2];
+    J.rc = s_region[3];
+    J.tab = a.tab;
+    J.out = a.out;
+    J.medians = a.medians;
+    J.plane = (size_t)a.n_angles * a.n;
+    unsigned long long code = 0;
+    for (int t = 0; t < a.n_t; t++)
+        code |= (unsigned long long)(a.tf[t] & 7) << (3 * t);
+    sino_block<L, kSel>(J, code, a.n_t, a.need, a.stride, reinterpret_cast<float *>(smraw),
+                        s_range);
+}
+
+// Persistent kernel over a batch of images of different sizes and angle
+// counts: each CTA claims work items (image, angle, line block) from a
+// counter until all are taken; items are numbered largest image first.
+template <int L, bool kSel>
+__global__ void __launch_bounds__(32 * L)
+    sino_batch_kernel(const BatchSinoArgs b) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ int s_range[2];
+    __shared__ int s_item;
+    for (;;) {
+        __syncthreads(); // the previous item is done with shared memory
+        if (threadIdx.x == 0)
+            s_item = (int)atomicAdd(b.counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= b.total_items)
+            break;
+        int lo = 0, hi = b.n_img - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&b.img[mid].items_begin) <= item)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const BatchImage &im = b.img[lo];
+        const int k = item - im.items_begin;
+        BlockJob J;
+        J.tex = im.tex;
+        J.tu = 1.f - (float)im.row_off;
+        J.tv = 1.f - (float)im.col_off;
+        J.n = im.n;
+        J.angle = k / im.blocks;
+        J.col0 = (k - J.angle * im.blocks) * L;
+        const float2 cs = b.trig[im.trig_off + J.angle];
+        J.c = cs.x;
+        J.s = cs.y;
+        J.roff = im.row_off;
+        J.coff = im.col_off;
+        J.rr = im.rows;
+        J.rc = im.cols;
+        J.tab = b.tab + im.tab_off;
+        J.out = b.sino + im.sino_off;
+        J.medians = nullptr;
+        J.plane = (size_t)im.n_angles * im.n;
+        sino_block<L, kSel>(J, b.tf_code, b.n_t, b.need, b.stride,
+                            reinterpret_cast<float *>(smraw), s_range);
     }
 }
 
@@ -487,6 +579,61 @@ cudaError_t launch_sinograms(const SinoArgs &a, int lines, cudaStream_t stream) 
     if (lines == 8)
         return sel ? launch_one<8, true>(a, smem, stream) : launch_one<8, false>(a, smem, stream);
     return sel ? launch_one<4, true>(a, smem, stream) : launch_one<4, false>(a, smem, stream);
+}
+
+namespace {
+template <int L, bool kSel> cudaError_t set_batch_attr(size_t smem) {
+    static size_t limit = 0;
+    if (limit == 0) {
+        limit = dynamic_smem_limit((const void *)sino_batch_kernel<L, kSel>);
+        cudaError_t e = cudaFuncSetAttribute(sino_batch_kernel<L, kSel>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)limit);
+        if (e != cudaSuccess)
+            return e;
+    }
+    return smem > limit ? cudaErrorInvalidValue : cudaSuccess;
+}
+
+template <int L, bool kSel> int batch_occ(size_t smem) {
+    int blocks = 0;
+    if (set_batch_attr<L, kSel>(smem) != cudaSuccess)
+        return 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sino_batch_kernel<L, kSel>, 32 * L,
+                                                  smem);
+    return blocks;
+}
+} // namespace
+
+cudaError_t prepare_sino_batch(int lines, bool sel, size_t smem) {
+    if (lines == 8)
+        return sel ? set_batch_attr<8, true>(smem) : set_batch_attr<8, false>(smem);
+    return sel ? set_batch_attr<4, true>(smem) : set_batch_attr<4, false>(smem);
+}
+
+int sino_batch_occupancy(int lines, bool sel, size_t smem) {
+    if (lines == 8)
+        return sel ? batch_occ<8, true>(smem) : batch_occ<8, false>(smem);
+    return sel ? batch_occ<4, true>(smem) : batch_occ<4, false>(smem);
+}
+
+cudaError_t launch_sino_batch(const BatchSinoArgs &a, int lines, int grid, size_t smem,
+                              cudaStream_t stream) {
+    if (grid <= 0 || a.total_items <= 0)
+        return cudaSuccess;
+    const bool sel = a.need & ((1u << 6) | (1u << 7));
+    if (lines == 8) {
+        if (sel)
+            sino_batch_kernel<8, true><<<grid, 256, smem, stream>>>(a);
+        else
+            sino_batch_kernel<8, false><<<grid, 256, smem, stream>>>(a);
+    } else {
+        if (sel)
+            sino_batch_kernel<4, true><<<grid, 128, smem, stream>>>(a);
+        else
+            sino_batch_kernel<4, false><<<grid, 128, smem, stream>>>(a);
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_rotate(cudaTextureObject_t tex, int rows, int cols, float c, float s,

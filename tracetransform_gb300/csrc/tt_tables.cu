@@ -71,4 +71,44 @@ void p3_tables(int n, float2 *chirp, float2 *filt, float2 *twid, float *lin,
         lin[p] = (float)(-1 + p * 2.0 / (n - 1));
 }
 
+// pad() of c++/src/auxiliary.cpp:257-275: side N of the zero frame that holds
+// every rotation of a rows x cols image, and the image's offset inside it
+// (the reference's float origin and hypot arithmetic).
+void pad_geometry(int rows, int cols, int *n, int *row_off, int *col_off) {
+    const float ox = (float)(std::floor((cols + 1) / 2.0) - 1);
+    const float oy = (float)(std::floor((rows + 1) / 2.0) - 1);
+    const float hx = (float)(cols - 1) - ox - 1;
+    const float hy = (float)(rows - 1) - oy - 1;
+    const int r_last = (int)std::ceil(std::hypot(hx, hy)) + 1;
+    const int nb = 2 * r_last + 1;
+    const float opad = (float)(std::floor((nb + 1) / 2.0) - 1);
+    *n = nb;
+    *col_off = (int)(opad - ox);
+    *row_off = (int)(opad - oy);
+}
+
+// (cos(-theta), sin(-theta)) of an angle in degrees, rounded as the reference
+// rounds them: deg2rad on a float in double arithmetic (c++/src/auxiliary.cpp:
+// 180), then std::cos / std::sin of the float (auxiliary.cpp:227-237).
+float2 rotation(float degrees) {
+    const float ang = (float)(degrees * M_PI / 180);
+    return make_float2(std::cos(-ang), std::sin(-ang));
+}
+
+// T3, T4, T5 kernels r^k exp(i m log r), r = 1 .. n-1, in double and rounded
+// once (c++/src/functionals.cpp:136-198); out holds 3 n entries, T3 first.
+void t345_tables(int n, float2 *out) {
+    for (int i = 0; i < 3 * n; i++)
+        out[i] = make_float2(0.f, 0.f);
+    for (int r = 1; r < n; r++) {
+        out[r] = make_float2((float)(r * std::cos(5.0 * std::log((double)r))),
+                             (float)(r * std::sin(5.0 * std::log((double)r))));
+        out[n + r] = make_float2((float)std::cos(3.0 * std::log((double)r)),
+                                 (float)std::sin(3.0 * std::log((double)r)));
+        out[2 * n + r] =
+            make_float2((float)(std::sqrt((double)r) * std::cos(4.0 * std::log((double)r))),
+                        (float)(std::sqrt((double)r) * std::sin(4.0 * std::log((double)r))));
+    }
+}
+
 } // namespace tt

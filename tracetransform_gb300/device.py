@@ -112,6 +112,30 @@ class Engine:
                                      _stream(circus)))
         return out
 
+    def transform_batch(self, flat: torch.Tensor, offsets, rows, cols, steps, tfuncs, pfuncs,
+                        circus: Optional[torch.Tensor] = None,
+                        signatures: Optional[torch.Tensor] = None):
+        """Batched engine on device: flat holds the column-major images at
+        element offsets; returns flat circus and signature tensors (image after
+        image, n_t x n_p x A_i each)."""
+        off = np.ascontiguousarray(np.asarray(offsets, np.int64))
+        r = np.ascontiguousarray(np.asarray(rows, np.int32))
+        c = np.ascontiguousarray(np.asarray(cols, np.int32))
+        s = np.ascontiguousarray(np.asarray(steps, np.int32))
+        ids = np.ascontiguousarray(np.asarray([int(t) for t in tfuncs], np.int32))
+        total = int(sum(len(ids) * len(pfuncs) * (360 // int(x)) for x in s))
+        if circus is None:
+            circus = torch.empty(max(total, 1), dtype=torch.float32, device=flat.device)
+        if signatures is None:
+            signatures = torch.empty(max(total, 1), dtype=torch.float32, device=flat.device)
+        I32 = ctypes.POINTER(ctypes.c_int32)
+        check(lib().tt_transform_batch_device(
+            self.plan.handle, _ptr(flat), off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            r.ctypes.data_as(I32), c.ctypes.data_as(I32), s.ctypes.data_as(I32), len(r),
+            ids.ctypes.data_as(I32), len(ids), _pf(pfuncs), len(pfuncs), _ptr(circus),
+            _ptr(signatures), _stream(flat)))
+        return circus, signatures
+
     def transform(self, image_cm: torch.Tensor, rows: int, cols: int, angles_deg, tfuncs,
                   pfuncs, out_sino=None):
         """Regular (non-orthonormal) transform on the device: returns
