@@ -59,7 +59,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch512"],
+                    default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-only", type=int, default=0, metavar="CALLS",
                     help="for profiler captures: run only the fused sinogram kernel CALLS "
@@ -348,6 +349,174 @@ def run_engine(args, world, rank, local_rank):
     print(json.dumps(line), flush=True)
 
 
+BATCH_T, BATCH_P = [0, 1, 2, 3, 4, 5], [1, 2, 3]
+
+
+def make_batch():
+    from tracetransform_gb300.synthetic import workload
+    items = workload("batch512")
+    return [im for im, _ in items], [int(s) for _, s in items]
+
+
+def batch_config(imgs, steps, world):
+    return {"workload": "batch512", "images": len(imgs),
+            "sides": "rows, cols independently uniform in 64..512",
+            "angles": "360 or 180 (step 1 or 2 degrees, p = 1/2)",
+            "t_functionals": BATCH_T, "p_functionals": BATCH_P,
+            "images_per_step_per_gpu": len(imgs),
+            "l2": "inputs 170 MB > L2 and L2 flushed between timed steps",
+            "parallelism": f"replicas{world}" if world > 1 else "single"}
+
+
+def run_batch(args, world, rank, local_rank):
+    """512 uneven images per step through the batched engine (one graph),
+    against the same 512 images through the plain per-image path."""
+    import torch
+    import tracetransform_gb300 as tt
+    from tracetransform_gb300.device import Engine
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    imgs, steps = make_batch()
+    rows = [im.shape[0] for im in imgs]
+    cols = [im.shape[1] for im in imgs]
+    bufs = [np.ascontiguousarray(im.ravel(order="F")) for im in imgs]
+    offsets = np.zeros(len(bufs), np.int64)
+    offsets[1:] = np.cumsum([b.size for b in bufs])[:-1]
+    flat_h = np.concatenate(bufs)
+    flat = torch.from_numpy(flat_h).to(dev)
+    eng = Engine(local_rank)
+    pf = [(p, -1, -1) for p in BATCH_P]
+    n_sino = len(imgs) * len(BATCH_T)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def batched():
+        return eng.transform_batch(flat, offsets, rows, cols, steps, BATCH_T, pf)
+
+    def timed(fn, k):
+        ms = []
+        for _ in range(k):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return ms
+
+    for _ in range(args.warmup):     # the first call builds, autotunes and captures
+        batched()
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    ms = statistics.mean(timed(batched, args.steps))
+
+    # plain per-image device path: three launches per image, no graph
+    views = [flat[int(o): int(o) + r * c].view(c, r) for o, r, c in zip(offsets, rows, cols)]
+    angle_lists = {s: tt.angles_from_step(s) for s in set(steps)}
+
+    def plain():
+        for v, r, c, s in zip(views, rows, cols, steps):
+            sino = eng.sinograms(v, r, c, angle_lists[s], BATCH_T)
+            eng.zscore(eng.circus(sino, pf))
+
+    plain()
+    torch.cuda.synchronize()
+    plain_ms = statistics.mean(timed(plain, max(1, min(3, args.steps))))
+
+    # end to end: host buffers through the C ABI, batched and per image
+    h_flat = torch.from_numpy(flat_h).pin_memory().numpy()
+    tt.api.transform_batch_flat(h_flat, offsets, rows, cols, steps, BATCH_T, BATCH_P,
+                                plan=eng.plan)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        tt.api.transform_batch_flat(h_flat, offsets, rows, cols, steps, BATCH_T, BATCH_P,
+                                    plan=eng.plan)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    t0 = time.perf_counter()
+    for im, s in zip(imgs, steps):
+        tt.Transformer(im, "plain", s, False, plan=eng.plan).getTransform(
+            [str(t) for t in BATCH_T], [str(p) for p in BATCH_P], write_data=False)
+    e2e_plain_s = time.perf_counter() - t0
+    clk = clocks.stop()
+    ms = max_over_ranks(ms, world)
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    alg = 0.0
+    out_floats = 0
+    for r, c, s in zip(rows, cols, steps):
+        n = tt.pad_geometry(r, c)[0]
+        a = 360 // s
+        alg += 4.0 * a * r * c + 4.0 * len(BATCH_T) * n * a
+        out_floats += len(BATCH_T) * len(BATCH_P) * a
+    achieved = alg / (ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": world * n_sino / (ms / 1e3), "unit": "sinograms/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded blob+noise, the reference ships no images)",
+        "config": batch_config(imgs, steps, world),
+        "e2e": {"value": world * n_sino / e2e_s, "unit": "sinograms/s",
+                "h2d_bytes_per_step": int(flat_h.nbytes),
+                "d2h_bytes_per_step": int(2 * 4 * out_floats)},
+        "plain_per_image": {"value": n_sino / (plain_ms / 1e3), "unit": "sinograms/s",
+                            "ms_per_step": plain_ms,
+                            "e2e_value": n_sino / e2e_plain_s,
+                            "note": "the same 512 images, one tt_sinograms_device + "
+                                    "tt_circus_device + tt_zscore_device per image; e2e: one "
+                                    "tt_transform (host buffers) per image"},
+        "batched_over_plain": plain_ms / ms,
+        "gpu_launches": 3 * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "batch graph (sino + circus + zscore)",
+                     "achieved": achieved, "peak": peak, "peak_source": peak_kind,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "algorithmic_bytes_per_launch": alg, "kernel_ms": ms},
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = batch_cpu_sample(imgs, steps, args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+
+
+def batch_cpu_sample(imgs, steps, target_s):
+    """The oracle on the first images of the batch until target_s, scaled to 512."""
+    from oracle import oracle as O
+    O.build()
+    t0 = time.perf_counter()
+    k = 0
+    while k < len(imgs) and time.perf_counter() - t0 < target_s:
+        O.transform(imgs[k], steps[k], BATCH_T, [(p, 0) for p in BATCH_P])
+        k += 1
+    dt = time.perf_counter() - t0
+    per_batch = dt * len(imgs) / k
+    return {"value": len(imgs) * len(BATCH_T) / per_batch, "unit": "sinograms/s",
+            "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"{k} of {len(imgs)} images transformed, {dt:.1f} s, scaled by "
+                      f"{len(imgs) / k:.1f}"}
+
+
+def run_reference_batch(args, world):
+    imgs, steps = make_batch()
+    target = max(1.0, args.cpu_seconds / max(1, args.steps))
+    samples = [batch_cpu_sample(imgs, steps, target) for _ in range(args.warmup + args.steps)]
+    cb = samples[-1]
+    value = statistics.median(s["value"] for s in samples[args.warmup:])
+    cb["value"] = value
+    line = {"metric": METRIC, "value": value, "unit": "sinograms/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * len(imgs) * len(BATCH_T) / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded blob+noise)", "impl": "reference",
+            "config": batch_config(imgs, steps, world), "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "sinograms/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -389,14 +558,20 @@ def main():
     if args.impl == "reference":
         if world > 1 and rank != 0:
             return
-        run_reference(args, world, rank)
+        if args.workload == "batch512":
+            run_reference_batch(args, world)
+        else:
+            run_reference(args, world, rank)
         return
     if world > 1:
         import torch
         import torch.distributed as dist
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
-    run_engine(args, world, rank, local_rank)
+    if args.workload == "batch512":
+        run_batch(args, world, rank, local_rank)
+    else:
+        run_engine(args, world, rank, local_rank)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

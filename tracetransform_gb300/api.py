@@ -273,6 +273,30 @@ def _ostream_float(v: float) -> str:
     return "%g" % v
 
 
+def transform_batch_flat(flat: np.ndarray, offsets, rows, cols, angle_stepsizes,
+                         tfunctionals: Sequence, pfunctionals: Sequence,
+                         plan: Optional[Plan] = None):
+    """tt_transform_batch on images already packed column-major into one float32
+    buffer at element offsets; returns flat (circus, signatures), image after
+    image, n_t x n_p x A_i each."""
+    tfs = _as_tfunctionals(tfunctionals)
+    pfs = _as_pfunctionals(pfunctionals)
+    flat = np.ascontiguousarray(flat, dtype=np.float32)
+    offsets = np.ascontiguousarray(np.asarray(offsets, np.int64))
+    r = np.ascontiguousarray(np.asarray(rows, np.int32))
+    c = np.ascontiguousarray(np.asarray(cols, np.int32))
+    steps = np.ascontiguousarray(np.asarray([int(s) for s in angle_stepsizes], np.int32))
+    ids = np.array([int(t.functional) for t in tfs], np.int32)
+    total = sum(len(ids) * len(pfs) * (360 // int(s)) for s in steps)
+    circus = np.zeros(max(total, 1), np.float32)
+    sig = np.zeros(max(total, 1), np.float32)
+    check(lib().tt_transform_batch(
+        _handle(plan), fptr(flat), offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+        iptr(r), iptr(c), iptr(steps), len(r), iptr(ids), len(ids), _pf_array(pfs),
+        len(pfs), fptr(circus), fptr(sig)))
+    return circus[:total], sig[:total]
+
+
 def transform_batch(images: Sequence, angle_stepsizes: Sequence[int], tfunctionals: Sequence,
                     pfunctionals: Sequence, plan: Optional[Plan] = None):
     """Transform many images of uneven sizes in one pass of the batched engine
@@ -289,18 +313,11 @@ def transform_batch(images: Sequence, angle_stepsizes: Sequence[int], tfunctiona
     if bufs:
         offsets[1:] = np.cumsum([b.size for b in bufs])[:-1]
     flat = np.concatenate(bufs) if bufs else np.zeros(1, np.float32)
-    rows = np.array([im.shape[0] for im in imgs], np.int32)
-    cols = np.array([im.shape[1] for im in imgs], np.int32)
-    steps = np.array([int(s) for s in angle_stepsizes], np.int32)
-    ids = np.array([int(t.functional) for t in tfs], np.int32)
-    na = [360 // int(s) for s in steps]
-    total = sum(len(ids) * len(pfs) * a for a in na)
-    circus = np.zeros(max(total, 1), np.float32)
-    sig = np.zeros(max(total, 1), np.float32)
-    check(lib().tt_transform_batch(
-        _handle(plan), fptr(flat), offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
-        iptr(rows), iptr(cols), iptr(steps), len(imgs), iptr(ids), len(ids), _pf_array(pfs),
-        len(pfs), fptr(circus), fptr(sig)))
+    circus, sig = transform_batch_flat(flat, offsets, [im.shape[0] for im in imgs],
+                                       [im.shape[1] for im in imgs], angle_stepsizes, tfs, pfs,
+                                       plan)
+    ids = [int(t.functional) for t in tfs]
+    na = [360 // int(s) for s in angle_stepsizes]
     out, at = [], 0
     for a in na:
         k = len(ids) * len(pfs) * a

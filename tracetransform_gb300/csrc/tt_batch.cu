@@ -157,7 +157,15 @@ void save_tune_cache(const std::map<std::string, Tune> &m) {
 class BatchEngine {
   public:
     explicit BatchEngine(int device) : device_(device) {}
-    ~BatchEngine() { release(); }
+    ~BatchEngine() {
+        release();
+        if (ev_in_)
+            cudaEventDestroy(ev_in_);
+        if (ev_out_)
+            cudaEventDestroy(ev_out_);
+        if (own_)
+            cudaStreamDestroy(own_);
+    }
 
     int run(const float *d_images, const long long *offsets, const int *rows, const int *cols,
             const int *steps, int n_img, const int32_t *tfuncs, int n_t,
@@ -193,6 +201,11 @@ class BatchEngine {
     Tune tune_;
     size_t sino_smem_ = 0;
     cudaGraphExec_t exec_ = nullptr;
+    // the graph is captured on and replayed from the engine's own stream
+    // (the legacy default stream cannot be captured), ordered after and
+    // before the caller's stream by events
+    cudaStream_t own_ = nullptr;
+    cudaEvent_t ev_in_ = nullptr, ev_out_ = nullptr;
 };
 
 void BatchEngine::release() {
@@ -539,21 +552,32 @@ int BatchEngine::run(const float *d_images, const long long *offsets, const int 
     for (int p = 0; p < n_p; p++)
         s.pk.push_back(pf[p].kind);
     s.src = d_images;
+    if (!own_) {
+        B_CUDA(cudaStreamCreateWithFlags(&own_, cudaStreamNonBlocking));
+        B_CUDA(cudaEventCreateWithFlags(&ev_in_, cudaEventDisableTiming));
+        B_CUDA(cudaEventCreateWithFlags(&ev_out_, cudaEventDisableTiming));
+    }
+    // the engine's stream starts after the caller's pending work (the images)
+    B_CUDA(cudaEventRecord(ev_in_, st));
+    B_CUDA(cudaStreamWaitEvent(own_, ev_in_, 0));
     if (!built_ || !(s == shape_)) {
         B_CUDA(cudaDeviceSynchronize()); // kernels of the old shape may still read its arrays
         release();
         shape_ = s;
-        B_CHECK(build(st));
-        B_CHECK(autotune(st));
-        B_CHECK(capture(st));
+        B_CHECK(build(own_));
+        B_CHECK(autotune(own_));
+        B_CHECK(capture(own_));
     }
-    B_CUDA(cudaGraphLaunch(exec_, st));
+    B_CUDA(cudaGraphLaunch(exec_, own_));
     if (d_circus)
         B_CUDA(cudaMemcpyAsync(d_circus, circ_.p, sizeof(float) * out_floats_,
-                               cudaMemcpyDeviceToDevice, st));
+                               cudaMemcpyDeviceToDevice, own_));
     if (d_sig)
         B_CUDA(cudaMemcpyAsync(d_sig, sig_.p, sizeof(float) * out_floats_,
-                               cudaMemcpyDeviceToDevice, st));
+                               cudaMemcpyDeviceToDevice, own_));
+    // and the caller's stream continues after the results
+    B_CUDA(cudaEventRecord(ev_out_, own_));
+    B_CUDA(cudaStreamWaitEvent(st, ev_out_, 0));
     return TT_OK;
 }
 
