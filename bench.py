@@ -59,7 +59,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch512"],
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch512", "grad64"],
                     default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-only", type=int, default=0, metavar="CALLS",
@@ -517,6 +517,141 @@ def run_reference_batch(args, world):
     print(json.dumps(line), flush=True)
 
 
+GRAD_T, GRAD_P, GRAD_IMAGES, GRAD_SIDE = [0, 1, 2], [1, 3], 64, 256
+
+
+def make_grad_batch(seed0):
+    from tracetransform_gb300.synthetic import blob_image
+    return np.stack([np.ascontiguousarray(blob_image(GRAD_SIDE, GRAD_SIDE, 8, (8, 40),
+                                                     (40, 200), seed0 + i))
+                     for i in range(GRAD_IMAGES)])
+
+
+def grad_config(world):
+    return {"workload": "grad64", "images": GRAD_IMAGES, "image": f"{GRAD_SIDE}x{GRAD_SIDE}",
+            "angles": 360, "t_functionals": GRAD_T, "p_functionals": GRAD_P,
+            "loss": "MSE against the circus functions of a second seed's images",
+            "step": "forward (sinograms + medians, circus) + loss + backward to the images",
+            "images_per_step_per_gpu": GRAD_IMAGES,
+            "l2": "flushed between timed steps (256 MiB write)",
+            "parallelism": f"replicas{world}" if world > 1 else "single"}
+
+
+def run_grad(args, world, rank, local_rank):
+    """64 images of 256 x 256, T0-T2 x P1/P3 over 360 angles: MSE loss
+    against a second seed's circus functions and the gradient to the images
+    through tracetransform_gb300.autograd (the hand-written adjoint kernels)."""
+    import torch
+    import tracetransform_gb300 as tt
+    from tracetransform_gb300 import autograd as tta
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    angles = tt.angles_from_step(1)
+    h_imgs = torch.from_numpy(make_grad_batch(10)).pin_memory()
+    imgs = h_imgs.to(dev)
+    with torch.no_grad():
+        target = tta.circus(torch.from_numpy(make_grad_batch(5000)).to(dev), angles, GRAD_T,
+                            GRAD_P)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    n = tt.pad_geometry(GRAD_SIDE, GRAD_SIDE)[0]
+    A = len(angles)
+
+    def train_step(x_dev, evs=None):
+        x = x_dev.requires_grad_(True)
+        loss = torch.nn.functional.mse_loss(tta.circus(x, angles, GRAD_T, GRAD_P), target)
+        if evs:
+            evs[1].record(stream)
+        loss.backward()
+        return loss, x.grad
+
+    for _ in range(args.warmup):
+        train_step(imgs.clone())
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    fwd, bwd, tot = [], [], []
+    for _ in range(args.steps):
+        x_dev = imgs.clone()
+        flush.zero_()
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        evs[0].record(stream)
+        train_step(x_dev, evs)
+        evs[2].record(stream)
+        torch.cuda.synchronize()
+        fwd.append(evs[0].elapsed_time(evs[1]))
+        bwd.append(evs[1].elapsed_time(evs[2]))
+        tot.append(evs[0].elapsed_time(evs[2]))
+    ms = max_over_ranks(statistics.mean(tot), world)
+
+    # the dominant backward kernels alone: line parameters + adjoint gather
+    eng = tta.engine_for(dev)
+    grad_sino = torch.randn((len(GRAD_T), A, n), dtype=torch.float32, device=dev)
+    _, med = eng.sinograms(imgs[0].t().contiguous(), GRAD_SIDE, GRAD_SIDE, angles, GRAD_T,
+                           medians=True)
+    adj = []
+    for _ in range(max(3, args.steps)):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.sinograms_backward(grad_sino, med, GRAD_SIDE, GRAD_SIDE, angles, GRAD_T)
+        b.record(stream)
+        torch.cuda.synchronize()
+        adj.append(a.elapsed_time(b))
+    adj_ms = statistics.mean(adj)
+
+    # end to end: pinned host images in, loss and image gradients out
+    h_grad = torch.empty_like(h_imgs).pin_memory()
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loss, g = train_step(h_imgs.to(dev, non_blocking=True))
+        h_grad.copy_(g, non_blocking=True)
+        lv = loss.item()
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    e2e_s = max_over_ranks(statistics.mean(e2e), world)
+    if rank != 0:
+        return
+    n_sino = GRAD_IMAGES * len(GRAD_T)
+    peak, peak_kind = measured_peak()
+    alg = 4.0 * 2 * len(GRAD_T) * n * A + 16.0 * 2 * n * A + 4.0 * GRAD_SIDE * GRAD_SIDE
+    achieved = alg / (adj_ms / 1e3) / 1e9
+    per_image_launches = 2 + 2 + 2  # sinograms + circus, circus_backward, line params + gather
+    line = {
+        "metric": METRIC, "value": world * n_sino / (ms / 1e3), "unit": "sinograms/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded blob+noise, the reference ships no images)",
+        "config": grad_config(world),
+        "forward_ms": statistics.mean(fwd), "backward_ms": statistics.mean(bwd),
+        "backward_over_forward": statistics.mean(bwd) / statistics.mean(fwd),
+        "e2e": {"value": world * n_sino / e2e_s, "unit": "sinograms/s",
+                "h2d_bytes_per_step": int(h_imgs.numel() * 4),
+                "d2h_bytes_per_step": int(h_grad.numel() * 4 + 4), "loss": lv},
+        "gpu_launches": per_image_launches * GRAD_IMAGES * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "line_params + adjoint_gather (one image)",
+                     "achieved": achieved, "peak": peak, "peak_source": peak_kind,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "algorithmic_bytes_per_launch": alg, "kernel_ms": adj_ms},
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        img = make_grad_batch(10)[0]
+        per, desc, cores = cpu_sample(img, angles, GRAD_T, GRAD_P, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": len(GRAD_T) / per, "unit": "sinograms/s",
+                                "cores": cores, "kind": "port",
+                                "sample": desc + "; forward only (the reference has no "
+                                                 "gradient)"}
+    print(json.dumps(line), flush=True)
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -560,6 +695,9 @@ def main():
             return
         if args.workload == "batch512":
             run_reference_batch(args, world)
+        elif args.workload == "grad64":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference computes no "
+                              "gradients; grad64 has no reference arm"}), flush=True)
         else:
             run_reference(args, world, rank)
         return
@@ -570,6 +708,8 @@ def main():
         dist.init_process_group("nccl")
     if args.workload == "batch512":
         run_batch(args, world, rank, local_rank)
+    elif args.workload == "grad64":
+        run_grad(args, world, rank, local_rank)
     else:
         run_engine(args, world, rank, local_rank)
     if world > 1:

@@ -171,6 +171,45 @@ tt_status tt_zscore_device(tt_plan *plan, const float *d_in, int n_vec, int len,
 /* Synchronise the plan's stream. */
 tt_status tt_plan_synchronize(tt_plan *plan);
 
+/* ---- backward pass -------------------------------------------------------- */
+/* The reference has no derivatives; these are the adjoints of the forward
+ * path for T0, T1, T2 (c++/src/functionals.cpp:95-129), P1 and P3
+ * (:287-360) and the bilinear rotation (c++/src/auxiliary.cpp:182-255).
+ * The weighted median of T1/T2 is held at the row the forward chose (pass
+ * the d_medians the forward wrote).  Other functionals are
+ * TT_ERR_UNSUPPORTED. */
+/* d_grad_circus: n_sino x n_p x cols -> d_grad_sino: n_sino x cols x rows. */
+tt_status tt_circus_backward_device(tt_plan *plan, const float *d_sino, int rows, int cols,
+                                    int n_sino, const tt_pfunctional *pfuncs, int n_p,
+                                    const float *d_grad_circus, float *d_grad_sino,
+                                    void *stream);
+/* d_grad_sino, d_medians: n_t x n x n_angles (as tt_sinograms_device wrote
+ * them) -> d_grad_image: src_rows x src_cols (the rotation adjoint, gathered
+ * per pixel; rotations are recomputed, not stored). */
+tt_status tt_sinograms_backward_device(tt_plan *plan, int src_rows, int src_cols, int n,
+                                       int row_off, int col_off, const float *angles_deg,
+                                       int n_angles, const int32_t *tfuncs, int n_t,
+                                       const float *d_grad_sino, const int32_t *d_medians,
+                                       float *d_grad_image, void *stream);
+/* Double-precision forward (T0-T2 on a rows x cols image in its pad() frame,
+ * with exact double coordinates; P1, P3) and backward, for finite-difference
+ * checks. */
+tt_status tt_sinograms_f64_device(tt_plan *plan, const double *d_img, int rows, int cols,
+                                  const float *angles_deg, int n_angles, const int32_t *tfuncs,
+                                  int n_t, double *d_out, int32_t *d_medians, void *stream);
+tt_status tt_circus_f64_device(tt_plan *plan, const double *d_sino, int rows, int cols,
+                               int n_sino, const tt_pfunctional *pfuncs, int n_p, double *d_out,
+                               void *stream);
+tt_status tt_circus_backward_f64_device(tt_plan *plan, const double *d_sino, int rows, int cols,
+                                        int n_sino, const tt_pfunctional *pfuncs, int n_p,
+                                        const double *d_grad_circus, double *d_grad_sino,
+                                        void *stream);
+tt_status tt_sinograms_backward_f64_device(tt_plan *plan, int src_rows, int src_cols, int n,
+                                           int row_off, int col_off, const float *angles_deg,
+                                           int n_angles, const int32_t *tfuncs, int n_t,
+                                           const double *d_grad_sino, const int32_t *d_medians,
+                                           double *d_grad_image, void *stream);
+
 /* ---- batched engine ------------------------------------------------------ */
 /* Many images of uneven sizes and angle counts in one pass: the reference
  * transforms its inputs one after another (the demo's loop over files and

@@ -23,6 +23,8 @@ EXPORTS = (
     "tt_pad_geometry", "tt_ortho_size", "tt_angles_from_step", "tt_sinograms", "tt_circus",
     "tt_zscore", "tt_rotate", "tt_transform", "tt_sinograms_device", "tt_circus_device", "tt_zscore_device",
     "tt_circus_zscore_noalloc", "tt_transform_batch", "tt_transform_batch_device",
+    "tt_circus_backward_device", "tt_sinograms_backward_device", "tt_sinograms_f64_device",
+    "tt_circus_f64_device", "tt_circus_backward_f64_device", "tt_sinograms_backward_f64_device",
 )
 
 
@@ -84,6 +86,17 @@ def lib():
                                ctypes.POINTER(PFunctionalC), _int, _F, _F],
         "tt_transform_batch_device": [_P, _P, _I64, _I32, _I32, _I32, _int, _I32, _int,
                                       ctypes.POINTER(PFunctionalC), _int, _P, _P, _P],
+        "tt_circus_backward_device": [_P, _P, _int, _int, _int, ctypes.POINTER(PFunctionalC),
+                                      _int, _P, _P, _P],
+        "tt_circus_backward_f64_device": [_P, _P, _int, _int, _int,
+                                          ctypes.POINTER(PFunctionalC), _int, _P, _P, _P],
+        "tt_sinograms_backward_device": [_P, _int, _int, _int, _int, _int, _F, _int, _I32, _int,
+                                         _P, _P, _P, _P],
+        "tt_sinograms_backward_f64_device": [_P, _int, _int, _int, _int, _int, _F, _int, _I32,
+                                             _int, _P, _P, _P, _P],
+        "tt_sinograms_f64_device": [_P, _P, _int, _int, _F, _int, _I32, _int, _P, _P, _P],
+        "tt_circus_f64_device": [_P, _P, _int, _int, _int, ctypes.POINTER(PFunctionalC), _int,
+                                 _P, _P],
     }
     for name, args in sig.items():
         fn = getattr(l, name)

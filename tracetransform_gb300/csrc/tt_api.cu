@@ -265,9 +265,80 @@ struct tt_plan {
     std::map<std::tuple<int, int, int>, float *> herm;  // (n, order, center)
     std::map<std::vector<float>, float2 *> trig;        // angle list -> (c, s)
     std::map<std::vector<long>, const float **> herm_ptrs;
-    DevBuf in, sino, circ, sig, region, nos, batch_in, batch_out;
+    DevBuf in, sino, circ, sig, region, nos, batch_in, batch_out, params;
     SourceTexture src;
     tt::BatchEngine *batch = nullptr;
+    // backward / double-precision tables
+    std::map<int, float *> dft32;                  // n -> cos, sin(2 pi j / n), 2 n
+    std::map<int, double *> dft64, lin64;
+    std::map<std::vector<float>, double *> trig64; // angle list -> (cos, sin) in double
+    std::map<std::vector<int>, int *> kinds;
+
+    template <typename T> tt_status get_dft(int n, const T **cosv, const T **sinv) {
+        std::map<int, T *> &cache = dft_cache((T *)nullptr);
+        auto it = cache.find(n);
+        if (it == cache.end()) {
+            std::vector<T> h(2 * (size_t)n);
+            for (int j = 0; j < n; j++) {
+                h[j] = (T)std::cos(2 * M_PI * j / n);
+                h[n + j] = (T)std::sin(2 * M_PI * j / n);
+            }
+            T *d;
+            TT_CHECK(upload(&d, h));
+            it = cache.emplace(n, d).first;
+        }
+        *cosv = it->second;
+        *sinv = it->second + n;
+        return TT_OK;
+    }
+    std::map<int, float *> &dft_cache(float *) { return dft32; }
+    std::map<int, double *> &dft_cache(double *) { return dft64; }
+
+    tt_status get_lin64(int n, const double **out) {
+        auto it = lin64.find(n);
+        if (it == lin64.end()) {
+            std::vector<double> h(n);
+            for (int p = 0; p < n; p++)
+                h[p] = -1 + p * 2.0 / (n - 1);
+            double *d;
+            TT_CHECK(upload(&d, h));
+            it = lin64.emplace(n, d).first;
+        }
+        *out = it->second;
+        return TT_OK;
+    }
+
+    tt_status get_trig64(const float *angles, int n_angles, const double **out) {
+        std::vector<float> key(angles, angles + n_angles);
+        auto it = trig64.find(key);
+        if (it == trig64.end()) {
+            std::vector<double> h(2 * (size_t)n_angles);
+            for (int a = 0; a < n_angles; a++) {
+                const double th = angles[a] * M_PI / 180;
+                h[2 * a] = std::cos(-th);
+                h[2 * a + 1] = std::sin(-th);
+            }
+            double *d;
+            TT_CHECK(upload(&d, h));
+            it = trig64.emplace(key, d).first;
+        }
+        *out = it->second;
+        return TT_OK;
+    }
+
+    tt_status get_kinds(const tt_pfunctional *pf, int n_p, const int **out) {
+        std::vector<int> key;
+        for (int p = 0; p < n_p; p++)
+            key.push_back(pf[p].kind);
+        auto it = kinds.find(key);
+        if (it == kinds.end()) {
+            int *d;
+            TT_CHECK(upload(&d, key.empty() ? std::vector<int>{0} : key));
+            it = kinds.emplace(key, d).first;
+        }
+        *out = it->second;
+        return TT_OK;
+    }
     std::vector<void *> owned;
 
     ~tt_plan() {
@@ -281,7 +352,7 @@ struct tt_plan {
         src.release();
         for (void *p : owned)
             cudaFree(p);
-        for (DevBuf *b : {&in, &sino, &circ, &sig, &region, &nos, &batch_in, &batch_out})
+        for (DevBuf *b : {&in, &sino, &circ, &sig, &region, &nos, &batch_in, &batch_out, &params})
             cudaFree(b->p);
         if (stream)
             cudaStreamDestroy(stream);
@@ -726,6 +797,163 @@ tt_status tt_transform_batch(tt_plan *plan, const float *images, const int64_t *
         TT_CUDA(cudaMemcpyAsync(signatures, d_sig, sizeof(float) * out_elems,
                                 cudaMemcpyDeviceToHost, st));
     TT_CUDA(cudaStreamSynchronize(st));
+    return TT_OK;
+}
+
+// ---- backward ------------------------------------------------------------
+
+static tt_status check_grad_funcs(const int32_t *tfuncs, int n_t, const tt_pfunctional *pf,
+                                  int n_p, unsigned long long *code) {
+    unsigned need;
+    if (tfuncs || n_t) {
+        TT_CHECK(check_tfuncs(tfuncs, n_t, &need));
+        *code = 0;
+        for (int t = 0; t < n_t; t++) {
+            if (tfuncs[t] > 2)
+                return fail(TT_ERR_UNSUPPORTED, "gradients exist for T0, T1 and T2, not T%d",
+                            tfuncs[t]);
+            *code |= (unsigned long long)tfuncs[t] << (3 * t);
+        }
+    }
+    if (pf || n_p) {
+        TT_CHECK(check_pfuncs(pf, n_p, false, &need));
+        for (int p = 0; p < n_p; p++)
+            if (pf[p].kind != TT_P1 && pf[p].kind != TT_P3)
+                return fail(TT_ERR_UNSUPPORTED, "gradients exist for P1 and P3 only");
+    }
+    return TT_OK;
+}
+
+extern "C++" {
+template <typename T>
+static tt_status circus_backward_impl(tt_plan *plan, const T *d_sino, int rows, int cols,
+                                      int n_sino, const tt_pfunctional *pf, int n_p,
+                                      const T *d_grad_circus, T *d_grad_sino, void *stream) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    unsigned long long code;
+    TT_CHECK(check_grad_funcs(nullptr, 0, pf, n_p, &code));
+    if (rows <= 0 || cols < 0 || n_sino < 0 || !d_sino || !d_grad_circus || !d_grad_sino)
+        return fail(TT_ERR_INVALID_ARG, "bad sinogram stack for the backward pass");
+    const T *cosv, *sinv, *lin;
+    const int *kinds;
+    TT_CHECK(p->get_dft<T>(rows, &cosv, &sinv));
+    TT_CHECK(p->get_kinds(pf, n_p, &kinds));
+    if (sizeof(T) == sizeof(float)) {
+        const FftTables *f;
+        TT_CHECK(p->get_fft(rows, &f)); // the forward's float linspace
+        lin = (const T *)f->lin;
+    } else {
+        const double *l;
+        TT_CHECK(p->get_lin64(rows, &l));
+        lin = (const T *)l;
+    }
+    TT_CUDA(tt::launch_circus_backward<T>(d_sino, rows, cols, n_sino, kinds, n_p, d_grad_circus,
+                                          cosv, sinv, lin, d_grad_sino, pick_stream(p, stream)));
+    return TT_OK;
+}
+
+template <typename T>
+static tt_status sino_backward_impl(tt_plan *plan, int src_rows, int src_cols, int n, int row_off,
+                                    int col_off, const float *angles_deg, int n_angles,
+                                    const int32_t *tfuncs, int n_t, const T *d_grad_sino,
+                                    const int32_t *d_medians, T *d_grad_image, void *stream) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    unsigned long long code;
+    TT_CHECK(check_grad_funcs(tfuncs, n_t, nullptr, 0, &code));
+    if (n <= 0 || src_rows <= 0 || src_cols <= 0 || row_off < 0 || col_off < 0 ||
+        row_off + src_rows > n || col_off + src_cols > n || n_angles < 0 || !angles_deg ||
+        !d_grad_sino || !d_medians || !d_grad_image)
+        return fail(TT_ERR_INVALID_ARG, "bad geometry or buffers for the backward pass");
+    const T *cs;
+    if (sizeof(T) == sizeof(float)) {
+        const float2 *t;
+        TT_CHECK(p->get_trig(angles_deg, n_angles, &t));
+        cs = (const T *)t;
+    } else {
+        const double *t;
+        TT_CHECK(p->get_trig64(angles_deg, n_angles, &t));
+        cs = (const T *)t;
+    }
+    TT_CHECK(p->ensure(p->params, sizeof(T) * 4 * (size_t)n * std::max(n_angles, 1)));
+    TT_CUDA(tt::launch_sino_backward<T>(d_grad_sino, d_medians, n, n_angles, code, n_t,
+                                        (T *)p->params.p, src_rows, src_cols, row_off, col_off,
+                                        cs, d_grad_image, pick_stream(p, stream)));
+    return TT_OK;
+}
+} // extern "C++"
+
+tt_status tt_circus_backward_device(tt_plan *plan, const float *d_sino, int rows, int cols,
+                                    int n_sino, const tt_pfunctional *pfuncs, int n_p,
+                                    const float *d_grad_circus, float *d_grad_sino,
+                                    void *stream) {
+    return circus_backward_impl<float>(plan, d_sino, rows, cols, n_sino, pfuncs, n_p,
+                                       d_grad_circus, d_grad_sino, stream);
+}
+
+tt_status tt_sinograms_backward_device(tt_plan *plan, int src_rows, int src_cols, int n,
+                                       int row_off, int col_off, const float *angles_deg,
+                                       int n_angles, const int32_t *tfuncs, int n_t,
+                                       const float *d_grad_sino, const int32_t *d_medians,
+                                       float *d_grad_image, void *stream) {
+    return sino_backward_impl<float>(plan, src_rows, src_cols, n, row_off, col_off, angles_deg,
+                                     n_angles, tfuncs, n_t, d_grad_sino, d_medians,
+                                     d_grad_image, stream);
+}
+
+tt_status tt_circus_backward_f64_device(tt_plan *plan, const double *d_sino, int rows, int cols,
+                                        int n_sino, const tt_pfunctional *pfuncs, int n_p,
+                                        const double *d_grad_circus, double *d_grad_sino,
+                                        void *stream) {
+    return circus_backward_impl<double>(plan, d_sino, rows, cols, n_sino, pfuncs, n_p,
+                                        d_grad_circus, d_grad_sino, stream);
+}
+
+tt_status tt_sinograms_backward_f64_device(tt_plan *plan, int src_rows, int src_cols, int n,
+                                           int row_off, int col_off, const float *angles_deg,
+                                           int n_angles, const int32_t *tfuncs, int n_t,
+                                           const double *d_grad_sino, const int32_t *d_medians,
+                                           double *d_grad_image, void *stream) {
+    return sino_backward_impl<double>(plan, src_rows, src_cols, n, row_off, col_off, angles_deg,
+                                      n_angles, tfuncs, n_t, d_grad_sino, d_medians,
+                                      d_grad_image, stream);
+}
+
+tt_status tt_sinograms_f64_device(tt_plan *plan, const double *d_img, int rows, int cols,
+                                  const float *angles_deg, int n_angles, const int32_t *tfuncs,
+                                  int n_t, double *d_out, int32_t *d_medians, void *stream) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    unsigned long long code;
+    TT_CHECK(check_grad_funcs(tfuncs, n_t, nullptr, 0, &code));
+    if (rows <= 0 || cols <= 0 || n_angles < 0 || !d_img || !d_out || !d_medians || !angles_deg)
+        return fail(TT_ERR_INVALID_ARG, "bad double-precision sinogram arguments");
+    int n, ro, co;
+    pad_geometry(rows, cols, &n, &ro, &co);
+    const double *cs;
+    TT_CHECK(p->get_trig64(angles_deg, n_angles, &cs));
+    TT_CUDA(tt::launch_sino_f64(d_img, rows, cols, ro, co, n, cs, code, n_t, n_angles, d_out,
+                                d_medians, pick_stream(p, stream)));
+    return TT_OK;
+}
+
+tt_status tt_circus_f64_device(tt_plan *plan, const double *d_sino, int rows, int cols,
+                               int n_sino, const tt_pfunctional *pfuncs, int n_p, double *d_out,
+                               void *stream) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    unsigned long long code;
+    TT_CHECK(check_grad_funcs(nullptr, 0, pfuncs, n_p, &code));
+    if (rows <= 0 || cols < 0 || n_sino < 0 || !d_sino || !d_out)
+        return fail(TT_ERR_INVALID_ARG, "bad double-precision sinogram stack");
+    const double *cosv, *sinv, *lin;
+    const int *kinds;
+    TT_CHECK(p->get_dft<double>(rows, &cosv, &sinv));
+    TT_CHECK(p->get_lin64(rows, &lin));
+    TT_CHECK(p->get_kinds(pfuncs, n_p, &kinds));
+    TT_CUDA(tt::launch_circus_f64(d_sino, rows, cols, n_sino, kinds, n_p, cosv, sinv, lin, d_out,
+                                  pick_stream(p, stream)));
     return TT_OK;
 }
 

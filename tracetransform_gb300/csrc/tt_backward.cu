@@ -1,0 +1,446 @@
+// tt_backward.cu -- gradients of circus functions with respect to the image.
+//
+// The reference has no derivative; this is the hand-written adjoint of the
+// forward path for the functionals config 4 differentiates: T0, T1, T2
+// (c++/src/functionals.cpp:95-129) and P1, P3 (:287-360), through the
+// bilinear rotation (c++/src/auxiliary.cpp:182-255).
+//
+//   circus_backward   P-stage adjoint per sinogram column:
+//                       P1:  d/dx_n sum|x_p - x_{p-1}| = sgn(x_n - x_{n-1}) - sgn(x_{n+1} - x_n)
+//                       P3:  y_p = |F_m(p)|^4 / N^4 with the reference's mirror m(p),
+//                            P3 = trapz(lin, y), so with w_p the trapz weights and
+//                            d_k = 2 |F_k|^2 / N^4 sum_{m(p) = k} w_p,
+//                            dP3/dx_n = sum_{k <= N/2} 2 d_k Re(conj(F_k) e^{-2 pi i k n / N})
+//                     (direct DFTs with an exact twiddle index; the P-stage is small)
+//   line_params       per line (angle, column): (G0, G1, G2, m) with G_t the
+//                     gradient of sinogram t at that entry and m the weighted
+//                     median the forward used -- dT1/dx_j = (j - m)+,
+//                     dT2/dx_j = (j - m)+^2, dT0/dx_j = 1
+//   adjoint_gather    rotation adjoint in gather form: one thread per image
+//                     pixel enumerates, per angle, the 3 x 3 rotated-grid
+//                     points around its inverse-rotated position, recomputes
+//                     their coordinates exactly as the forward did, and adds
+//                     bilinear weight x line gradient for the points whose
+//                     stencil holds the pixel (no atomics, deterministic;
+//                     rotations are recomputed, never stored)
+//
+// Everything is templated on float / double.  The double instantiation, with
+// the plain double forward below (sino_f64_kernel, circus_f64_kernel), is what
+// the finite-difference check runs in.
+#include <climits>
+
+#include "tt_common.cuh"
+#include "tt_internal.h"
+
+namespace tt {
+namespace {
+
+template <typename T> struct Coord;
+// The forward's float coordinate arithmetic, bit for bit.
+template <> struct Coord<float> {
+    static __device__ __forceinline__ void q(float X, float Y, float c, float s, float o,
+                                             float &qx, float &qy) {
+        qx = __fadd_rn(__fadd_rn(__fmul_rn(X, c), __fmul_rn(Y, s)), o);
+        qy = __fadd_rn(__fadd_rn(__fmul_rn(X, -s), __fmul_rn(Y, c)), o);
+    }
+};
+template <> struct Coord<double> {
+    static __device__ __forceinline__ void q(double X, double Y, double c, double s, double o,
+                                             double &qx, double &qy) {
+        qx = X * c + Y * s + o;
+        qy = X * (-s) + Y * c + o;
+    }
+};
+
+template <typename T> __device__ __forceinline__ T sgn(T v) {
+    return (T)((v > (T)0) - (v < (T)0));
+}
+
+template <typename T> __device__ __forceinline__ T block_sum_t(T v, T *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1)
+        v += __shfl_xor_sync(TT_FULL_MASK, v, d);
+    __syncthreads();
+    if (lane == 0)
+        red[warp] = v;
+    __syncthreads();
+    T t = 0;
+    for (int w = 0; w < nw; w++)
+        t += red[w];
+    return t;
+}
+
+// P-stage adjoint.  Block per column (sinogram s, column a); dynamic shared
+// memory: x (rows), F (2 * (rows / 2 + 1)), d (rows / 2 + 1), all of T.
+// grad_circus: n_sino x n_p x cols; out: n_sino x cols x rows.
+template <typename T>
+__global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int cols,
+                                       int n_sino, const int *__restrict__ kinds, int n_p,
+                                       const T *__restrict__ grad_circus,
+                                       const T *__restrict__ cosv, const T *__restrict__ sinv,
+                                       const T *__restrict__ lin, T *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *x = reinterpret_cast<T *>(smraw);
+    const int nb = rows / 2 + 1;
+    T *Fr = x + rows, *Fi = Fr + nb, *d = Fi + nb;
+    const int a = blockIdx.x, s = blockIdx.y, tid = threadIdx.x, bd = blockDim.x;
+    const T *col = sino + ((size_t)s * cols + a) * rows;
+    for (int i = tid; i < rows; i += bd)
+        x[i] = col[i];
+    T g1 = 0, g3 = 0;
+    for (int p = 0; p < n_p; p++) {
+        const T g = grad_circus[((size_t)s * n_p + p) * cols + a];
+        if (kinds[p] == 1)
+            g1 += g;
+        else if (kinds[p] == 3)
+            g3 += g;
+    }
+    __syncthreads();
+    if (g3 != (T)0) {
+        // F_k, k <= N/2 (twiddle index k n mod N)
+        for (int k = tid; k < nb; k += bd) {
+            T re = 0, im = 0;
+            long idx = 0;
+            for (int n = 0; n < rows; n++) {
+                re += x[n] * cosv[idx];
+                im -= x[n] * sinv[idx];
+                idx += k;
+                if (idx >= rows)
+                    idx -= rows;
+            }
+            Fr[k] = re;
+            Fi[k] = im;
+        }
+        __syncthreads();
+        // d_k = 2 |F_k|^2 / N^4 * sum of trapz weights of the p that read bin k
+        const T n4 = (T)rows * rows * rows * rows;
+        for (int k = tid; k < nb; k += bd) {
+            T wsum = 0;
+            const int ps[2] = {k, rows - k};
+            for (int u = 0; u < 2; u++) {
+                const int p = ps[u];
+                if (p < 0 || p >= rows || (u == 1 && (p <= rows / 2 || p == k)))
+                    continue;
+                T w = 0;
+                if (p + 1 <= rows - 1)
+                    w += (T)0.5 * (lin[p + 1] - lin[p]);
+                if (p >= 1)
+                    w += (T)0.5 * (lin[p] - lin[p - 1]);
+                wsum += w;
+            }
+            d[k] = (T)2 * (Fr[k] * Fr[k] + Fi[k] * Fi[k]) / n4 * wsum;
+        }
+        __syncthreads();
+    }
+    for (int n = tid; n < rows; n += bd) {
+        T g = 0;
+        if (g1 != (T)0) {
+            T v = 0;
+            if (n >= 1)
+                v += sgn(x[n] - x[n - 1]);
+            if (n + 1 < rows)
+                v -= sgn(x[n + 1] - x[n]);
+            g += g1 * v;
+        }
+        if (g3 != (T)0) {
+            // sum_k 2 d_k Re(conj(F_k) e^{-2 pi i k n / N})
+            //     = sum_k 2 d_k (Fr cos(2 pi k n / N) - Fi sin(2 pi k n / N))
+            T acc = 0;
+            long idx = 0;
+            for (int k = 0; k < nb; k++) {
+                acc += (T)2 * d[k] * (Fr[k] * cosv[idx] - Fi[k] * sinv[idx]);
+                idx += n;
+                if (idx >= rows)
+                    idx -= rows;
+            }
+            g += g3 * acc;
+        }
+        out[((size_t)s * cols + a) * rows + n] = g;
+    }
+}
+
+// (G0, G1, G2, m) per line (angle a, column col): grad_sino is n_t x A x n,
+// medians the same shape (the forward's weighted-median rows).
+template <typename T>
+__global__ void line_params_kernel(const T *__restrict__ grad_sino,
+                                   const int *__restrict__ medians, int n, int n_angles,
+                                   unsigned long long tf_code, int n_t, T *__restrict__ params) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long plane = (long long)n * n_angles;
+    if (i >= plane)
+        return;
+    T g[3] = {0, 0, 0};
+    int m = 0;
+    for (int t = 0; t < n_t; t++) {
+        const int f = (int)((tf_code >> (3 * t)) & 7ull);
+        g[f] += grad_sino[t * plane + i];
+        if (f == 1 || f == 2)
+            m = medians[t * plane + i];
+    }
+    params[4 * i + 0] = g[0];
+    params[4 * i + 1] = g[1];
+    params[4 * i + 2] = g[2];
+    params[4 * i + 3] = (T)m;
+}
+
+// Rotation adjoint by gathering: pixel (r, c) of the rows x cols image sits at
+// frame point (x, y) = (c + col_off, r + row_off).  For each angle the rotated
+// grid points (col, j) whose bilinear stencil can hold it lie within 1.5 of
+// its inverse-rotated position; each is recomputed as the forward computed it.
+template <typename T>
+__global__ void adjoint_gather_kernel(int rows, int cols, int row_off, int col_off, int n,
+                                      int n_angles, const T *__restrict__ cs,
+                                      const T *__restrict__ params, T *__restrict__ grad_img) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)rows * cols)
+        return;
+    const int r = (int)(i % rows), c = (int)(i / rows);
+    const int px = c + col_off, py = r + row_off;
+    const T o = (T)(n - 1) * (T)0.5, nm1 = (T)(n - 1);
+    const T dx = (T)px - o, dy = (T)py - o;
+    T acc = 0;
+    for (int a = 0; a < n_angles; a++) {
+        const T ca = cs[2 * a], sa = cs[2 * a + 1];
+        // inverse of (X, Y) -> (X c + Y s, -X s + Y c)
+        const T Xs = ca * dx - sa * dy, Ys = sa * dx + ca * dy;
+        const int c0 = (int)floor((double)(Xs + o) + 0.5), j0 = (int)floor((double)(Ys + o) + 0.5);
+        const T *pa = params + (size_t)4 * a * n;
+        for (int cc = c0 - 1; cc <= c0 + 1; cc++) {
+            if (cc < 0 || cc >= n)
+                continue;
+            const T *pl = pa + 4 * cc;
+            const T g0 = pl[0], g1 = pl[1], g2 = pl[2];
+            const int m = (int)pl[3];
+            if (g0 == (T)0 && g1 == (T)0 && g2 == (T)0)
+                continue;
+            for (int j = j0 - 1; j <= j0 + 1; j++) {
+                if (j < 0 || j >= n)
+                    continue;
+                T qx, qy;
+                Coord<T>::q((T)cc - o, (T)j - o, ca, sa, o, qx, qy);
+                if (!(qx >= (T)0 && qx < nm1 && qy >= (T)0 && qy < nm1))
+                    continue;
+                const T xi = trunc(qx), yi = trunc(qy);
+                const T xf = qx - xi, yf = qy - yi;
+                T wx, wy;
+                if ((int)xi == px)
+                    wx = (T)1 - xf;
+                else if ((int)xi + 1 == px)
+                    wx = xf;
+                else
+                    continue;
+                if ((int)yi == py)
+                    wy = (T)1 - yf;
+                else if ((int)yi + 1 == py)
+                    wy = yf;
+                else
+                    continue;
+                T g = g0;
+                if (j >= m) {
+                    const T rr = (T)(j - m);
+                    g += g1 * rr + g2 * rr * rr;
+                }
+                acc += wx * wy * g;
+            }
+        }
+    }
+    grad_img[i] = acc;
+}
+
+// ---- plain double-precision forward (for the finite-difference check) ----
+
+// Sinograms T0, T1, T2 of a rows x cols double image in its pad() frame,
+// computed in double: block per line (angle, column), samples in shared
+// memory (n doubles), one thread sums.  out / medians: n_t x A x n.
+__global__ void sino_f64_kernel(const double *__restrict__ img, int rows, int cols,
+                                int row_off, int col_off, int n, const double *__restrict__ cs,
+                                unsigned long long tf_code, int n_t, int n_angles,
+                                double *__restrict__ out, int *__restrict__ medians) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    double *x = reinterpret_cast<double *>(smraw);
+    const int col = blockIdx.x, a = blockIdx.y;
+    const double o = (n - 1) * 0.5, nm1 = n - 1;
+    const double ca = cs[2 * a], sa = cs[2 * a + 1];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        double qx, qy;
+        Coord<double>::q(col - o, j - o, ca, sa, o, qx, qy);
+        double v = 0;
+        if (qx >= 0 && qx < nm1 && qy >= 0 && qy < nm1) {
+            const double xi = trunc(qx), yi = trunc(qy), xf = qx - xi, yf = qy - yi;
+            const int x0 = (int)xi - col_off, y0 = (int)yi - row_off;
+            double tap[4] = {0, 0, 0, 0};
+            for (int u = 0; u < 4; u++) {
+                const int xx = x0 + (u & 1), yy = y0 + (u >> 1);
+                if (xx >= 0 && xx < cols && yy >= 0 && yy < rows)
+                    tap[u] = img[yy + (size_t)xx * rows];
+            }
+            v = tap[0] * (1 - xf) * (1 - yf) + tap[1] * xf * (1 - yf) + tap[2] * (1 - xf) * yf +
+                tap[3] * xf * yf;
+        }
+        x[j] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double S = 0;
+        for (int j = 0; j < n; j++)
+            S += x[j];
+        int m = n - 1;
+        double run = 0;
+        for (int j = 0; j < n; j++) {
+            run += x[j];
+            if (2 * run >= S) {
+                m = j;
+                break;
+            }
+        }
+        double t1 = 0, t2 = 0;
+        for (int j = m; j < n; j++) {
+            t1 += x[j] * (j - m);
+            t2 += x[j] * (double)(j - m) * (j - m);
+        }
+        const size_t plane = (size_t)n_angles * n, at = (size_t)a * n + col;
+        for (int t = 0; t < n_t; t++) {
+            const int f = (int)((tf_code >> (3 * t)) & 7ull);
+            out[t * plane + at] = f == 0 ? S : f == 1 ? t1 : t2;
+            medians[t * plane + at] = f == 0 ? -1 : m;
+        }
+    }
+}
+
+// P1 and P3 of double sinogram columns (direct DFT), block per column.
+__global__ void circus_f64_kernel(const double *__restrict__ sino, int rows, int cols,
+                                  const int *__restrict__ kinds, int n_p,
+                                  const double *__restrict__ cosv, const double *__restrict__ sinv,
+                                  const double *__restrict__ lin, double *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[8];
+    double *x = reinterpret_cast<double *>(smraw);
+    double *y = x + rows;
+    const int a = blockIdx.x, s = blockIdx.y, tid = threadIdx.x, bd = blockDim.x;
+    const double *colp = sino + ((size_t)s * cols + a) * rows;
+    for (int i = tid; i < rows; i += bd)
+        x[i] = colp[i];
+    __syncthreads();
+    const int nb = rows / 2 + 1;
+    for (int k = tid; k < nb; k += bd) {
+        double re = 0, im = 0;
+        long idx = 0;
+        for (int j = 0; j < rows; j++) {
+            re += x[j] * cosv[idx];
+            im -= x[j] * sinv[idx];
+            idx += k;
+            if (idx >= rows)
+                idx -= rows;
+        }
+        const double h2 = (re * re + im * im) / ((double)rows * rows);
+        y[k] = h2 * h2;
+    }
+    __syncthreads();
+    double p1 = 0, p3 = 0;
+    for (int i = tid; i < rows; i += bd) {
+        if (i >= 1)
+            p1 += fabs(x[i] - x[i - 1]);
+        if (i + 1 < rows) {
+            const int m0 = i <= rows / 2 ? i : rows - i;
+            const int m1 = i + 1 <= rows / 2 ? i + 1 : rows - (i + 1);
+            p3 += 0.5 * (lin[i + 1] - lin[i]) * (y[m1] + y[m0]);
+        }
+    }
+    p1 = block_sum_t(p1, red);
+    p3 = block_sum_t(p3, red);
+    if (tid == 0)
+        for (int p = 0; p < n_p; p++)
+            out[((size_t)s * n_p + p) * cols + a] = kinds[p] == 1 ? p1 : kinds[p] == 3 ? p3 : 0;
+}
+
+} // namespace
+
+template <typename T>
+cudaError_t launch_circus_backward(const T *sino, int rows, int cols, int n_sino,
+                                   const int *d_kinds, int n_p, const T *grad_circus,
+                                   const T *cosv, const T *sinv, const T *lin, T *out,
+                                   cudaStream_t st) {
+    if (rows <= 0 || cols <= 0 || n_sino <= 0)
+        return cudaSuccess;
+    const size_t smem = sizeof(T) * ((size_t)rows + 3 * (size_t)(rows / 2 + 1));
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(circus_backward_kernel<T>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    circus_backward_kernel<T><<<dim3(cols, n_sino), 256, smem, st>>>(
+        sino, rows, cols, n_sino, d_kinds, n_p, grad_circus, cosv, sinv, lin, out);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_sino_backward(const T *grad_sino, const int *medians, int n, int n_angles,
+                                 unsigned long long tf_code, int n_t, T *params, int rows,
+                                 int cols, int row_off, int col_off, const T *cs, T *grad_img,
+                                 cudaStream_t st) {
+    const long long lines = (long long)n * n_angles, pix = (long long)rows * cols;
+    if (lines > 0)
+        line_params_kernel<T><<<(unsigned)((lines + 255) / 256), 256, 0, st>>>(
+            grad_sino, medians, n, n_angles, tf_code, n_t, params);
+    if (pix > 0)
+        adjoint_gather_kernel<T><<<(unsigned)((pix + 127) / 128), 128, 0, st>>>(
+            rows, cols, row_off, col_off, n, n_angles, cs, params, grad_img);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sino_f64(const double *img, int rows, int cols, int row_off, int col_off,
+                            int n, const double *cs, unsigned long long tf_code, int n_t,
+                            int n_angles, double *out, int *medians, cudaStream_t st) {
+    if (n <= 0 || n_angles <= 0)
+        return cudaSuccess;
+    const size_t smem = sizeof(double) * (size_t)n;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(sino_f64_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    sino_f64_kernel<<<dim3(n, n_angles), 128, smem, st>>>(img, rows, cols, row_off, col_off, n,
+                                                           cs, tf_code, n_t, n_angles, out,
+                                                           medians);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_circus_f64(const double *sino, int rows, int cols, int n_sino,
+                              const int *d_kinds, int n_p, const double *cosv,
+                              const double *sinv, const double *lin, double *out,
+                              cudaStream_t st) {
+    if (rows <= 0 || cols <= 0 || n_sino <= 0)
+        return cudaSuccess;
+    const size_t smem = sizeof(double) * ((size_t)rows + rows / 2 + 1);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(circus_f64_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    circus_f64_kernel<<<dim3(cols, n_sino), 256, smem, st>>>(sino, rows, cols, d_kinds, n_p, cosv,
+                                                             sinv, lin, out);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_circus_backward<float>(const float *, int, int, int, const int *, int,
+                                                   const float *, const float *, const float *,
+                                                   const float *, float *, cudaStream_t);
+template cudaError_t launch_circus_backward<double>(const double *, int, int, int, const int *,
+                                                    int, const double *, const double *,
+                                                    const double *, const double *, double *,
+                                                    cudaStream_t);
+template cudaError_t launch_sino_backward<float>(const float *, const int *, int, int,
+                                                 unsigned long long, int, float *, int, int, int,
+                                                 int, const float *, float *, cudaStream_t);
+template cudaError_t launch_sino_backward<double>(const double *, const int *, int, int,
+                                                  unsigned long long, int, double *, int, int, int,
+                                                  int, const double *, double *, cudaStream_t);
+
+} // namespace tt

@@ -74,6 +74,27 @@ int batch_run(BatchEngine *b, const float *d_images, const long long *offsets, c
               const tt_pfunctional *pf, int n_p, float *d_circus, float *d_sig,
               cudaStream_t st);
 
+// Backward pass (tt_backward.cu), T = float or double.  cs: (cos, sin) per
+// angle as the forward used them; cosv / sinv: cos, sin(2 pi j / rows);
+// params: scratch of 4 T per line (n x n_angles).
+template <typename T>
+cudaError_t launch_circus_backward(const T *sino, int rows, int cols, int n_sino,
+                                   const int *d_kinds, int n_p, const T *grad_circus,
+                                   const T *cosv, const T *sinv, const T *lin, T *out,
+                                   cudaStream_t st);
+template <typename T>
+cudaError_t launch_sino_backward(const T *grad_sino, const int *medians, int n, int n_angles,
+                                 unsigned long long tf_code, int n_t, T *params, int rows,
+                                 int cols, int row_off, int col_off, const T *cs, T *grad_img,
+                                 cudaStream_t st);
+cudaError_t launch_sino_f64(const double *img, int rows, int cols, int row_off, int col_off,
+                            int n, const double *cs, unsigned long long tf_code, int n_t,
+                            int n_angles, double *out, int *medians, cudaStream_t st);
+cudaError_t launch_circus_f64(const double *sino, int rows, int cols, int n_sino,
+                              const int *d_kinds, int n_p, const double *cosv,
+                              const double *sinv, const double *lin, double *out,
+                              cudaStream_t st);
+
 // Record a failure for tt_last_error() on this thread; returns status.
 int record_error(int status, const char *message);
 

@@ -112,6 +112,54 @@ class Engine:
                                      _stream(circus)))
         return out
 
+    # ---- backward and double precision -----------------------------------
+    def circus_backward(self, sino: torch.Tensor, pfuncs, grad_circus: torch.Tensor):
+        """Adjoint of circus(): (nS, nP, A) gradient -> (nS, A, N) gradient."""
+        ns, a, n = sino.shape
+        out = torch.empty_like(sino)
+        fn = (lib().tt_circus_backward_f64_device if sino.dtype == torch.float64
+              else lib().tt_circus_backward_device)
+        check(fn(self.plan.handle, _ptr(sino), n, a, ns, _pf(pfuncs), len(pfuncs),
+                 _ptr(grad_circus.contiguous()), _ptr(out), _stream(sino)))
+        return out
+
+    def sinograms_backward(self, grad_sino: torch.Tensor, medians: torch.Tensor, rows: int,
+                           cols: int, angles_deg, tfuncs) -> torch.Tensor:
+        """Adjoint of sinograms() for T0-T2: returns the (cols, rows) column-major
+        image gradient."""
+        n, ro, co = pad_geometry(rows, cols)
+        ang = np.ascontiguousarray(np.asarray(angles_deg, np.float32))
+        ids = np.ascontiguousarray(np.asarray([int(t) for t in tfuncs], np.int32))
+        out = torch.empty((cols, rows), dtype=grad_sino.dtype, device=grad_sino.device)
+        fn = (lib().tt_sinograms_backward_f64_device if grad_sino.dtype == torch.float64
+              else lib().tt_sinograms_backward_device)
+        check(fn(self.plan.handle, rows, cols, n, ro, co,
+                 ang.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(ang),
+                 ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), len(ids),
+                 _ptr(grad_sino.contiguous()), _ptr(medians), _ptr(out), _stream(grad_sino)))
+        return out
+
+    def sinograms_f64(self, image_cm: torch.Tensor, rows: int, cols: int, angles_deg, tfuncs):
+        """T0-T2 sinograms of a double image in double: (nT, A, N) and medians."""
+        n = pad_geometry(rows, cols)[0]
+        ang = np.ascontiguousarray(np.asarray(angles_deg, np.float32))
+        ids = np.ascontiguousarray(np.asarray([int(t) for t in tfuncs], np.int32))
+        out = torch.empty((len(ids), len(ang), n), dtype=torch.float64, device=image_cm.device)
+        med = torch.empty(out.shape, dtype=torch.int32, device=image_cm.device)
+        check(lib().tt_sinograms_f64_device(
+            self.plan.handle, _ptr(image_cm), rows, cols,
+            ang.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(ang),
+            ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), len(ids), _ptr(out), _ptr(med),
+            _stream(image_cm)))
+        return out, med
+
+    def circus_f64(self, sino: torch.Tensor, pfuncs) -> torch.Tensor:
+        ns, a, n = sino.shape
+        out = torch.empty((ns, len(pfuncs), a), dtype=torch.float64, device=sino.device)
+        check(lib().tt_circus_f64_device(self.plan.handle, _ptr(sino), n, a, ns, _pf(pfuncs),
+                                         len(pfuncs), _ptr(out), _stream(sino)))
+        return out
+
     def transform_batch(self, flat: torch.Tensor, offsets, rows, cols, steps, tfuncs, pfuncs,
                         circus: Optional[torch.Tensor] = None,
                         signatures: Optional[torch.Tensor] = None):
