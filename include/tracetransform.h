@@ -183,10 +183,14 @@ tt_status tt_circus_backward_device(tt_plan *plan, const float *d_sino, int rows
                                     int n_sino, const tt_pfunctional *pfuncs, int n_p,
                                     const float *d_grad_circus, float *d_grad_sino,
                                     void *stream);
-/* d_grad_sino, d_medians: n_t x n x n_angles (as tt_sinograms_device wrote
- * them) -> d_grad_image: src_rows x src_cols (the rotation adjoint, gathered
- * per pixel; rotations are recomputed, not stored). */
-tt_status tt_sinograms_backward_device(tt_plan *plan, int src_rows, int src_cols, int n,
+/* n_images images of one size at a time: d_grad_sino, d_medians: n_images
+ * stacks of n_t x n x n_angles (as tt_sinograms_device wrote them) ->
+ * d_grad_image: n_images column-major src_rows x src_cols images (the
+ * rotation adjoint, gathered per pixel; rotations are recomputed, not
+ * stored).  Scratch of 16 n n_angles n_images bytes (32 for f64) is held by
+ * the plan. */
+tt_status tt_sinograms_backward_device(tt_plan *plan, int n_images, int src_rows, int src_cols,
+                                       int n,
                                        int row_off, int col_off, const float *angles_deg,
                                        int n_angles, const int32_t *tfuncs, int n_t,
                                        const float *d_grad_sino, const int32_t *d_medians,
@@ -204,7 +208,8 @@ tt_status tt_circus_backward_f64_device(tt_plan *plan, const double *d_sino, int
                                         int n_sino, const tt_pfunctional *pfuncs, int n_p,
                                         const double *d_grad_circus, double *d_grad_sino,
                                         void *stream);
-tt_status tt_sinograms_backward_f64_device(tt_plan *plan, int src_rows, int src_cols, int n,
+tt_status tt_sinograms_backward_f64_device(tt_plan *plan, int n_images, int src_rows,
+                                           int src_cols, int n,
                                            int row_off, int col_off, const float *angles_deg,
                                            int n_angles, const int32_t *tfuncs, int n_t,
                                            const double *d_grad_sino, const int32_t *d_medians,

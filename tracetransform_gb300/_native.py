@@ -90,10 +90,10 @@ def lib():
                                       _int, _P, _P, _P],
         "tt_circus_backward_f64_device": [_P, _P, _int, _int, _int,
                                           ctypes.POINTER(PFunctionalC), _int, _P, _P, _P],
-        "tt_sinograms_backward_device": [_P, _int, _int, _int, _int, _int, _F, _int, _I32, _int,
-                                         _P, _P, _P, _P],
-        "tt_sinograms_backward_f64_device": [_P, _int, _int, _int, _int, _int, _F, _int, _I32,
-                                             _int, _P, _P, _P, _P],
+        "tt_sinograms_backward_device": [_P, _int, _int, _int, _int, _int, _int, _F, _int, _I32,
+                                         _int, _P, _P, _P, _P],
+        "tt_sinograms_backward_f64_device": [_P, _int, _int, _int, _int, _int, _int, _F, _int,
+                                             _I32, _int, _P, _P, _P, _P],
         "tt_sinograms_f64_device": [_P, _P, _int, _int, _F, _int, _I32, _int, _P, _P, _P],
         "tt_circus_f64_device": [_P, _P, _int, _int, _int, ctypes.POINTER(PFunctionalC), _int,
                                  _P, _P],

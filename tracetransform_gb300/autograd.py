@@ -18,7 +18,8 @@ from typing import Dict, Sequence
 
 import torch
 
-from .device import Engine, to_colmajor
+from .api import pad_geometry
+from .device import Engine
 
 _engines: Dict[int, Engine] = {}
 
@@ -31,32 +32,45 @@ def engine_for(device: torch.device) -> Engine:
 
 
 class CircusFunction(torch.autograd.Function):
-    """circus = P(T(rotate(pad(image)))) of one (rows, cols) image."""
+    """circus = P(T(rotate(pad(images)))) of a (B, rows, cols) batch of
+    same-size images: one sinogram launch per image, then one P-stage launch,
+    one P-stage adjoint launch and one rotation-adjoint launch for the whole
+    batch."""
 
     @staticmethod
-    def forward(ctx, image, angles, tfuncs, pfuncs):
-        eng = engine_for(image.device)
-        rows, cols = image.shape
-        cm = to_colmajor(image)
+    def forward(ctx, images, angles, tfuncs, pfuncs):
+        eng = engine_for(images.device)
+        b, rows, cols = images.shape
+        n = pad_geometry(rows, cols)[0]
+        cm = images.transpose(1, 2).contiguous()  # (B, cols, rows): column-major images
         pf = [(int(p), -1, -1) for p in pfuncs]
-        if image.dtype == torch.float64:
-            sino, med = eng.sinograms_f64(cm, rows, cols, angles, tfuncs)
-            circ = eng.circus_f64(sino, pf)
-        else:
-            sino, med = eng.sinograms(cm, rows, cols, angles, tfuncs, medians=True)
-            circ = eng.circus(sino, pf)
+        shape = (b, len(tfuncs), len(angles), n)
+        sino = torch.empty(shape, dtype=images.dtype, device=images.device)
+        med = torch.empty(shape, dtype=torch.int32, device=images.device)
+        for i in range(b):
+            if images.dtype == torch.float64:
+                eng.sinograms_f64(cm[i], rows, cols, angles, tfuncs, out=sino[i],
+                                  med_out=med[i])
+            else:
+                eng.sinograms(cm[i], rows, cols, angles, tfuncs, medians=True, out=sino[i],
+                              med_out=med[i])
+        flat = sino.view(b * len(tfuncs), len(angles), n)
+        circ = eng.circus_f64(flat, pf) if images.dtype == torch.float64 else eng.circus(flat, pf)
         ctx.save_for_backward(sino, med)
         ctx.meta = (rows, cols, tuple(angles), tuple(tfuncs), pf)
-        return circ
+        return circ.view(b, len(tfuncs), len(pf), len(angles))
 
     @staticmethod
     def backward(ctx, grad_circ):
         sino, med = ctx.saved_tensors
         rows, cols, angles, tfuncs, pf = ctx.meta
         eng = engine_for(sino.device)
-        grad_sino = eng.circus_backward(sino, pf, grad_circ.to(sino.dtype).contiguous())
-        grad_cm = eng.sinograms_backward(grad_sino, med, rows, cols, angles, tfuncs)
-        return grad_cm.t(), None, None, None
+        b, nt, a, n = sino.shape
+        g = grad_circ.to(sino.dtype).contiguous().view(b * nt, len(pf), a)
+        grad_sino = eng.circus_backward(sino.view(b * nt, a, n), pf, g)
+        grad_cm = eng.sinograms_backward(grad_sino.view(b, nt, a, n), med, rows, cols, angles,
+                                         tfuncs)
+        return grad_cm.transpose(1, 2), None, None, None
 
 
 def circus(images: torch.Tensor, angles: Sequence[float], tfuncs: Sequence[int],
@@ -67,5 +81,5 @@ def circus(images: torch.Tensor, angles: Sequence[float], tfuncs: Sequence[int],
     tfuncs = [int(t) for t in tfuncs]
     pfuncs = [int(p) for p in pfuncs]
     if images.dim() == 2:
-        return CircusFunction.apply(images, angles, tfuncs, pfuncs)
-    return torch.stack([CircusFunction.apply(im, angles, tfuncs, pfuncs) for im in images])
+        return CircusFunction.apply(images.unsqueeze(0), angles, tfuncs, pfuncs)[0]
+    return CircusFunction.apply(images, angles, tfuncs, pfuncs)

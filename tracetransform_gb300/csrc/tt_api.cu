@@ -854,7 +854,8 @@ static tt_status circus_backward_impl(tt_plan *plan, const T *d_sino, int rows, 
 }
 
 template <typename T>
-static tt_status sino_backward_impl(tt_plan *plan, int src_rows, int src_cols, int n, int row_off,
+static tt_status sino_backward_impl(tt_plan *plan, int n_images, int src_rows, int src_cols,
+                                    int n, int row_off,
                                     int col_off, const float *angles_deg, int n_angles,
                                     const int32_t *tfuncs, int n_t, const T *d_grad_sino,
                                     const int32_t *d_medians, T *d_grad_image, void *stream) {
@@ -862,7 +863,7 @@ static tt_status sino_backward_impl(tt_plan *plan, int src_rows, int src_cols, i
     TT_CHECK(resolve_plan(plan, &p));
     unsigned long long code;
     TT_CHECK(check_grad_funcs(tfuncs, n_t, nullptr, 0, &code));
-    if (n <= 0 || src_rows <= 0 || src_cols <= 0 || row_off < 0 || col_off < 0 ||
+    if (n_images < 0 || n <= 0 || src_rows <= 0 || src_cols <= 0 || row_off < 0 || col_off < 0 ||
         row_off + src_rows > n || col_off + src_cols > n || n_angles < 0 || !angles_deg ||
         !d_grad_sino || !d_medians || !d_grad_image)
         return fail(TT_ERR_INVALID_ARG, "bad geometry or buffers for the backward pass");
@@ -876,8 +877,11 @@ static tt_status sino_backward_impl(tt_plan *plan, int src_rows, int src_cols, i
         TT_CHECK(p->get_trig64(angles_deg, n_angles, &t));
         cs = (const T *)t;
     }
-    TT_CHECK(p->ensure(p->params, sizeof(T) * 4 * (size_t)n * std::max(n_angles, 1)));
-    TT_CUDA(tt::launch_sino_backward<T>(d_grad_sino, d_medians, n, n_angles, code, n_t,
+    if (n_images == 0)
+        return TT_OK;
+    TT_CHECK(p->ensure(p->params,
+                       sizeof(T) * 4 * (size_t)n * std::max(n_angles, 1) * (size_t)n_images));
+    TT_CUDA(tt::launch_sino_backward<T>(d_grad_sino, d_medians, n_images, n, n_angles, code, n_t,
                                         (T *)p->params.p, src_rows, src_cols, row_off, col_off,
                                         cs, d_grad_image, pick_stream(p, stream)));
     return TT_OK;
@@ -892,12 +896,12 @@ tt_status tt_circus_backward_device(tt_plan *plan, const float *d_sino, int rows
                                        d_grad_circus, d_grad_sino, stream);
 }
 
-tt_status tt_sinograms_backward_device(tt_plan *plan, int src_rows, int src_cols, int n,
-                                       int row_off, int col_off, const float *angles_deg,
+tt_status tt_sinograms_backward_device(tt_plan *plan, int n_images, int src_rows, int src_cols,
+                                       int n, int row_off, int col_off, const float *angles_deg,
                                        int n_angles, const int32_t *tfuncs, int n_t,
                                        const float *d_grad_sino, const int32_t *d_medians,
                                        float *d_grad_image, void *stream) {
-    return sino_backward_impl<float>(plan, src_rows, src_cols, n, row_off, col_off, angles_deg,
+    return sino_backward_impl<float>(plan, n_images, src_rows, src_cols, n, row_off, col_off, angles_deg,
                                      n_angles, tfuncs, n_t, d_grad_sino, d_medians,
                                      d_grad_image, stream);
 }
@@ -910,12 +914,12 @@ tt_status tt_circus_backward_f64_device(tt_plan *plan, const double *d_sino, int
                                         d_grad_circus, d_grad_sino, stream);
 }
 
-tt_status tt_sinograms_backward_f64_device(tt_plan *plan, int src_rows, int src_cols, int n,
-                                           int row_off, int col_off, const float *angles_deg,
+tt_status tt_sinograms_backward_f64_device(tt_plan *plan, int n_images, int src_rows,
+                                           int src_cols, int n, int row_off, int col_off, const float *angles_deg,
                                            int n_angles, const int32_t *tfuncs, int n_t,
                                            const double *d_grad_sino, const int32_t *d_medians,
                                            double *d_grad_image, void *stream) {
-    return sino_backward_impl<double>(plan, src_rows, src_cols, n, row_off, col_off, angles_deg,
+    return sino_backward_impl<double>(plan, n_images, src_rows, src_cols, n, row_off, col_off, angles_deg,
                                       n_angles, tfuncs, n_t, d_grad_sino, d_medians,
                                       d_grad_image, stream);
 }

@@ -36,19 +36,25 @@ namespace tt {
 namespace {
 
 template <typename T> struct Coord;
-// The forward's float coordinate arithmetic, bit for bit.
+// The forward's coordinate arithmetic, bit for bit: q = (X c + Y s) + o,
+// products and sums rounded one at a time (no contraction into FMAs), so the
+// adjoint can hoist X c / Y s and still reproduce every coordinate.
 template <> struct Coord<float> {
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
     static __device__ __forceinline__ void q(float X, float Y, float c, float s, float o,
                                              float &qx, float &qy) {
-        qx = __fadd_rn(__fadd_rn(__fmul_rn(X, c), __fmul_rn(Y, s)), o);
-        qy = __fadd_rn(__fadd_rn(__fmul_rn(X, -s), __fmul_rn(Y, c)), o);
+        qx = add(add(mul(X, c), mul(Y, s)), o);
+        qy = add(add(mul(X, -s), mul(Y, c)), o);
     }
 };
 template <> struct Coord<double> {
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
     static __device__ __forceinline__ void q(double X, double Y, double c, double s, double o,
                                              double &qx, double &qy) {
-        qx = X * c + Y * s + o;
-        qy = X * (-s) + Y * c + o;
+        qx = add(add(mul(X, c), mul(Y, s)), o);
+        qy = add(add(mul(X, -s), mul(Y, c)), o);
     }
 };
 
@@ -79,7 +85,8 @@ __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int
                                        int n_sino, const int *__restrict__ kinds, int n_p,
                                        const T *__restrict__ grad_circus,
                                        const T *__restrict__ cosv, const T *__restrict__ sinv,
-                                       const T *__restrict__ lin, T *__restrict__ out) {
+                                       const T *__restrict__ lin, bool tab_in_smem,
+                                       T *__restrict__ out) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T *x = reinterpret_cast<T *>(smraw);
     const int nb = rows / 2 + 1;
@@ -88,6 +95,17 @@ __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int
     const T *col = sino + ((size_t)s * cols + a) * rows;
     for (int i = tid; i < rows; i += bd)
         x[i] = col[i];
+    // twiddles cos / sin(2 pi i / rows), staged in shared memory when they fit
+    const T *ct = cosv, *stw = sinv;
+    if (tab_in_smem) {
+        T *c_s = d + nb, *s_s = c_s + rows;
+        for (int i = tid; i < rows; i += bd) {
+            c_s[i] = cosv[i];
+            s_s[i] = sinv[i];
+        }
+        ct = c_s;
+        stw = s_s;
+    }
     T g1 = 0, g3 = 0;
     for (int p = 0; p < n_p; p++) {
         const T g = grad_circus[((size_t)s * n_p + p) * cols + a];
@@ -103,8 +121,8 @@ __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int
             T re = 0, im = 0;
             long idx = 0;
             for (int n = 0; n < rows; n++) {
-                re += x[n] * cosv[idx];
-                im -= x[n] * sinv[idx];
+                re += x[n] * ct[idx];
+                im -= x[n] * stw[idx];
                 idx += k;
                 if (idx >= rows)
                     idx -= rows;
@@ -149,7 +167,7 @@ __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int
             T acc = 0;
             long idx = 0;
             for (int k = 0; k < nb; k++) {
-                acc += (T)2 * d[k] * (Fr[k] * cosv[idx] - Fi[k] * sinv[idx]);
+                acc += (T)2 * d[k] * (Fr[k] * ct[idx] - Fi[k] * stw[idx]);
                 idx += n;
                 if (idx >= rows)
                     idx -= rows;
@@ -160,23 +178,27 @@ __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int
     }
 }
 
-// (G0, G1, G2, m) per line (angle a, column col): grad_sino is n_t x A x n,
-// medians the same shape (the forward's weighted-median rows).
+// (G0, G1, G2, m) per line (image, angle a, column col): grad_sino holds
+// n_images stacks of n_t x A x n, medians the same (the forward's
+// weighted-median rows); params: n_images x A x n x 4.
 template <typename T>
 __global__ void line_params_kernel(const T *__restrict__ grad_sino,
-                                   const int *__restrict__ medians, int n, int n_angles,
-                                   unsigned long long tf_code, int n_t, T *__restrict__ params) {
+                                   const int *__restrict__ medians, int n_images, int n,
+                                   int n_angles, unsigned long long tf_code, int n_t,
+                                   T *__restrict__ params) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long plane = (long long)n * n_angles;
-    if (i >= plane)
+    if (i >= plane * n_images)
         return;
+    const long long img = i / plane, at = i - img * plane;
+    const long long base = img * n_t * plane + at;
     T g[3] = {0, 0, 0};
     int m = 0;
     for (int t = 0; t < n_t; t++) {
         const int f = (int)((tf_code >> (3 * t)) & 7ull);
-        g[f] += grad_sino[t * plane + i];
+        g[f] += grad_sino[base + t * plane];
         if (f == 1 || f == 2)
-            m = medians[t * plane + i];
+            m = medians[base + t * plane];
     }
     params[4 * i + 0] = g[0];
     params[4 * i + 1] = g[1];
@@ -184,68 +206,101 @@ __global__ void line_params_kernel(const T *__restrict__ grad_sino,
     params[4 * i + 3] = (T)m;
 }
 
-// Rotation adjoint by gathering: pixel (r, c) of the rows x cols image sits at
-// frame point (x, y) = (c + col_off, r + row_off).  For each angle the rotated
-// grid points (col, j) whose bilinear stencil can hold it lie within 1.5 of
-// its inverse-rotated position; each is recomputed as the forward computed it.
+template <typename T> struct Quad;
+template <> struct Quad<float> {
+    static __device__ __forceinline__ void load(const float *p, float &a, float &b, float &c,
+                                                float &d) {
+        const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+        a = v.x; b = v.y; c = v.z; d = v.w;
+    }
+};
+template <> struct Quad<double> {
+    static __device__ __forceinline__ void load(const double *p, double &a, double &b,
+                                                double &c, double &d) {
+        const double2 u = __ldg(reinterpret_cast<const double2 *>(p));
+        const double2 v = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+        a = u.x; b = u.y; c = v.x; d = v.y;
+    }
+};
+
+constexpr int kAdjWarps = 8; // angle groups per pixel group
+
+// Rotation adjoint by gathering.  Pixel (r, c) of a rows x cols image sits at
+// frame point (px, py) = (c + col_off, r + row_off).  A rotated-grid point
+// (column cc, sample j) with frame coordinates q = (qx, qy) feeds it the
+// bilinear weight (1 - |qx - px|)+ (1 - |qy - py|)+ -- the forward's
+// (1 - xf) or xf factor exactly, since qx - px and 1 - |qx - px| are exact in
+// floating point for |qx - px| < 1 -- provided the forward sampled q at all
+// (0 <= qx, qy < n - 1).  Such points lie within sqrt(2) of the pixel's
+// inverse-rotated position, i.e. in the 3 x 3 lattice block around its
+// nearest lattice point; each is recomputed with the forward's arithmetic.
+//
+// CTA: 32 consecutive pixels (lanes) x kAdjWarps warps; warp w sums the angles
+// a = w (mod kAdjWarps) in increasing order and the warps' partial sums are
+// added in warp order, so the result is deterministic.  blockIdx.y = image.
 template <typename T>
-__global__ void adjoint_gather_kernel(int rows, int cols, int row_off, int col_off, int n,
-                                      int n_angles, const T *__restrict__ cs,
-                                      const T *__restrict__ params, T *__restrict__ grad_img) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= (long long)rows * cols)
-        return;
-    const int r = (int)(i % rows), c = (int)(i / rows);
-    const int px = c + col_off, py = r + row_off;
-    const T o = (T)(n - 1) * (T)0.5, nm1 = (T)(n - 1);
-    const T dx = (T)px - o, dy = (T)py - o;
+__global__ void __launch_bounds__(32 * kAdjWarps)
+adjoint_gather_kernel(int rows, int cols, int row_off, int col_off, int n, int n_angles,
+                      const T *__restrict__ cs, const T *__restrict__ params,
+                      T *__restrict__ grad_img) {
+    using C = Coord<T>;
+    __shared__ T part[kAdjWarps][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long pix = (long long)rows * cols;
+    const long long i = (long long)blockIdx.x * 32 + lane;
+    params += (size_t)blockIdx.y * 4 * (size_t)n * n_angles;
     T acc = 0;
-    for (int a = 0; a < n_angles; a++) {
-        const T ca = cs[2 * a], sa = cs[2 * a + 1];
-        // inverse of (X, Y) -> (X c + Y s, -X s + Y c)
-        const T Xs = ca * dx - sa * dy, Ys = sa * dx + ca * dy;
-        const int c0 = (int)floor((double)(Xs + o) + 0.5), j0 = (int)floor((double)(Ys + o) + 0.5);
-        const T *pa = params + (size_t)4 * a * n;
-        for (int cc = c0 - 1; cc <= c0 + 1; cc++) {
-            if (cc < 0 || cc >= n)
-                continue;
-            const T *pl = pa + 4 * cc;
-            const T g0 = pl[0], g1 = pl[1], g2 = pl[2];
-            const int m = (int)pl[3];
-            if (g0 == (T)0 && g1 == (T)0 && g2 == (T)0)
-                continue;
-            for (int j = j0 - 1; j <= j0 + 1; j++) {
-                if (j < 0 || j >= n)
+    if (i < pix) {
+        const int r = (int)(i % rows), c = (int)(i / rows);
+        const T fpx = (T)(c + col_off), fpy = (T)(r + row_off);
+        const T o = (T)(n - 1) * (T)0.5, nm1 = (T)(n - 1);
+        const T dx = fpx - o, dy = fpy - o;
+        for (int a = warp; a < n_angles; a += kAdjWarps) {
+            const T ca = __ldg(cs + 2 * a), sa = __ldg(cs + 2 * a + 1);
+            // inverse of (X, Y) -> (X c + Y s, -X s + Y c), nearest lattice point
+            const int c0 = (int)rint(ca * dx - sa * dy + o);
+            const int j0 = (int)rint(sa * dx + ca * dy + o);
+            T ys[3], yc[3];
+#pragma unroll
+            for (int u = 0; u < 3; u++) {
+                const T Y = (T)(j0 - 1 + u) - o;
+                ys[u] = C::mul(Y, sa);
+                yc[u] = C::mul(Y, ca);
+            }
+            const T *pa = params + (size_t)4 * a * n;
+#pragma unroll
+            for (int v = 0; v < 3; v++) {
+                const int cc = c0 - 1 + v;
+                if (cc < 0 || cc >= n)
                     continue;
-                T qx, qy;
-                Coord<T>::q((T)cc - o, (T)j - o, ca, sa, o, qx, qy);
-                if (!(qx >= (T)0 && qx < nm1 && qy >= (T)0 && qy < nm1))
-                    continue;
-                const T xi = trunc(qx), yi = trunc(qy);
-                const T xf = qx - xi, yf = qy - yi;
-                T wx, wy;
-                if ((int)xi == px)
-                    wx = (T)1 - xf;
-                else if ((int)xi + 1 == px)
-                    wx = xf;
-                else
-                    continue;
-                if ((int)yi == py)
-                    wy = (T)1 - yf;
-                else if ((int)yi + 1 == py)
-                    wy = yf;
-                else
-                    continue;
-                T g = g0;
-                if (j >= m) {
-                    const T rr = (T)(j - m);
-                    g += g1 * rr + g2 * rr * rr;
+                T g0, g1, g2, mf;
+                Quad<T>::load(pa + 4 * cc, g0, g1, g2, mf);
+                const T X = (T)cc - o;
+                const T xc = C::mul(X, ca), xs = C::mul(X, -sa);
+#pragma unroll
+                for (int u = 0; u < 3; u++) {
+                    const int j = j0 - 1 + u;
+                    const T qx = C::add(C::add(xc, ys[u]), o);
+                    const T qy = C::add(C::add(xs, yc[u]), o);
+                    const T wx = (T)1 - fabs(qx - fpx), wy = (T)1 - fabs(qy - fpy);
+                    const bool in = j >= 0 && j < n && qx >= (T)0 && qx < nm1 &&
+                                    qy >= (T)0 && qy < nm1 && wx > (T)0 && wy > (T)0;
+                    const T rr = (T)j - mf;
+                    const T g = rr >= (T)0 ? g0 + rr * (g1 + rr * g2) : g0;
+                    acc += in ? wx * wy * g : (T)0;
                 }
-                acc += wx * wy * g;
             }
         }
     }
-    grad_img[i] = acc;
+    part[warp][lane] = acc;
+    __syncthreads();
+    if (warp == 0 && i < pix) {
+        T t = part[0][lane];
+#pragma unroll
+        for (int w = 1; w < kAdjWarps; w++)
+            t += part[w][lane];
+        grad_img[(size_t)blockIdx.y * pix + i] = t;
+    }
 }
 
 // ---- plain double-precision forward (for the finite-difference check) ----
@@ -363,31 +418,41 @@ cudaError_t launch_circus_backward(const T *sino, int rows, int cols, int n_sino
                                    cudaStream_t st) {
     if (rows <= 0 || cols <= 0 || n_sino <= 0)
         return cudaSuccess;
-    const size_t smem = sizeof(T) * ((size_t)rows + 3 * (size_t)(rows / 2 + 1));
-    if (smem > 48 * 1024) {
+    const size_t base = sizeof(T) * ((size_t)rows + 3 * (size_t)(rows / 2 + 1));
+    const size_t with_tab = base + sizeof(T) * 2 * (size_t)rows;
+    static size_t limit = 0;
+    if (limit == 0) {
+        limit = dynamic_smem_limit((const void *)circus_backward_kernel<T>);
         cudaError_t e = cudaFuncSetAttribute(circus_backward_kernel<T>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+                                             (int)limit);
         if (e != cudaSuccess)
             return e;
     }
+    const bool tab = with_tab <= limit;
+    const size_t smem = tab ? with_tab : base;
+    if (smem > limit)
+        return cudaErrorInvalidValue;
     circus_backward_kernel<T><<<dim3(cols, n_sino), 256, smem, st>>>(
-        sino, rows, cols, n_sino, d_kinds, n_p, grad_circus, cosv, sinv, lin, out);
+        sino, rows, cols, n_sino, d_kinds, n_p, grad_circus, cosv, sinv, lin, tab, out);
     return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_sino_backward(const T *grad_sino, const int *medians, int n, int n_angles,
-                                 unsigned long long tf_code, int n_t, T *params, int rows,
-                                 int cols, int row_off, int col_off, const T *cs, T *grad_img,
-                                 cudaStream_t st) {
-    const long long lines = (long long)n * n_angles, pix = (long long)rows * cols;
+cudaError_t launch_sino_backward(const T *grad_sino, const int *medians, int n_images, int n,
+                                 int n_angles, unsigned long long tf_code, int n_t, T *params,
+                                 int rows, int cols, int row_off, int col_off, const T *cs,
+                                 T *grad_img, cudaStream_t st) {
+    if (n_images <= 0)
+        return cudaSuccess;
+    const long long lines = (long long)n * n_angles * n_images, pix = (long long)rows * cols;
     if (lines > 0)
         line_params_kernel<T><<<(unsigned)((lines + 255) / 256), 256, 0, st>>>(
-            grad_sino, medians, n, n_angles, tf_code, n_t, params);
+            grad_sino, medians, n_images, n, n_angles, tf_code, n_t, params);
     if (pix > 0)
-        adjoint_gather_kernel<T><<<(unsigned)((pix + 127) / 128), 128, 0, st>>>(
-            rows, cols, row_off, col_off, n, n_angles, cs, params, grad_img);
+        adjoint_gather_kernel<T><<<dim3((unsigned)((pix + 31) / 32), n_images), 32 * kAdjWarps,
+                                   0, st>>>(rows, cols, row_off, col_off, n, n_angles, cs,
+                                            params, grad_img);
     return cudaGetLastError();
 }
 
@@ -436,10 +501,10 @@ template cudaError_t launch_circus_backward<double>(const double *, int, int, in
                                                     int, const double *, const double *,
                                                     const double *, const double *, double *,
                                                     cudaStream_t);
-template cudaError_t launch_sino_backward<float>(const float *, const int *, int, int,
+template cudaError_t launch_sino_backward<float>(const float *, const int *, int, int, int,
                                                  unsigned long long, int, float *, int, int, int,
                                                  int, const float *, float *, cudaStream_t);
-template cudaError_t launch_sino_backward<double>(const double *, const int *, int, int,
+template cudaError_t launch_sino_backward<double>(const double *, const int *, int, int, int,
                                                   unsigned long long, int, double *, int, int, int,
                                                   int, const double *, double *, cudaStream_t);
 

@@ -83,10 +83,10 @@ cudaError_t launch_circus_backward(const T *sino, int rows, int cols, int n_sino
                                    const T *cosv, const T *sinv, const T *lin, T *out,
                                    cudaStream_t st);
 template <typename T>
-cudaError_t launch_sino_backward(const T *grad_sino, const int *medians, int n, int n_angles,
-                                 unsigned long long tf_code, int n_t, T *params, int rows,
-                                 int cols, int row_off, int col_off, const T *cs, T *grad_img,
-                                 cudaStream_t st);
+cudaError_t launch_sino_backward(const T *grad_sino, const int *medians, int n_images, int n,
+                                 int n_angles, unsigned long long tf_code, int n_t, T *params,
+                                 int rows, int cols, int row_off, int col_off, const T *cs,
+                                 T *grad_img, cudaStream_t st);
 cudaError_t launch_sino_f64(const double *img, int rows, int cols, int row_off, int col_off,
                             int n, const double *cs, unsigned long long tf_code, int n_t,
                             int n_angles, double *out, int *medians, cudaStream_t st);

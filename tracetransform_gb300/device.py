@@ -64,7 +64,7 @@ class Engine:
 
     def sinograms(self, image_cm: torch.Tensor, rows: int, cols: int, angles_deg, tfuncs,
                   padded: bool = False, medians: bool = False,
-                  out: Optional[torch.Tensor] = None):
+                  out: Optional[torch.Tensor] = None, med_out: Optional[torch.Tensor] = None):
         """Sinograms of a column-major image (see module doc).
 
         padded=False: image_cm is the unpadded R x C image, placed in its pad()
@@ -79,7 +79,9 @@ class Engine:
         ids = np.ascontiguousarray(np.asarray([int(t) for t in tfuncs], np.int32))
         if out is None:
             out = torch.empty((len(ids), len(ang), n), dtype=torch.float32, device=image_cm.device)
-        med = torch.empty_like(out, dtype=torch.int32) if medians else None
+        med = None
+        if medians:
+            med = med_out if med_out is not None else torch.empty_like(out, dtype=torch.int32)
         check(lib().tt_sinograms_device(
             self.plan.handle, _ptr(image_cm), rows, cols, rows, n, ro, co,
             ang.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(ang),
@@ -125,27 +127,35 @@ class Engine:
 
     def sinograms_backward(self, grad_sino: torch.Tensor, medians: torch.Tensor, rows: int,
                            cols: int, angles_deg, tfuncs) -> torch.Tensor:
-        """Adjoint of sinograms() for T0-T2: returns the (cols, rows) column-major
-        image gradient."""
+        """Adjoint of sinograms() for T0-T2.  grad_sino / medians: (nT, A, N)
+        or a batch (B, nT, A, N) of same-size images; returns the column-major
+        image gradient(s), (cols, rows) or (B, cols, rows)."""
         n, ro, co = pad_geometry(rows, cols)
+        batch = grad_sino.dim() == 4
+        b = grad_sino.shape[0] if batch else 1
         ang = np.ascontiguousarray(np.asarray(angles_deg, np.float32))
         ids = np.ascontiguousarray(np.asarray([int(t) for t in tfuncs], np.int32))
-        out = torch.empty((cols, rows), dtype=grad_sino.dtype, device=grad_sino.device)
+        out = torch.empty((b, cols, rows), dtype=grad_sino.dtype, device=grad_sino.device)
         fn = (lib().tt_sinograms_backward_f64_device if grad_sino.dtype == torch.float64
               else lib().tt_sinograms_backward_device)
-        check(fn(self.plan.handle, rows, cols, n, ro, co,
+        check(fn(self.plan.handle, b, rows, cols, n, ro, co,
                  ang.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(ang),
                  ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), len(ids),
-                 _ptr(grad_sino.contiguous()), _ptr(medians), _ptr(out), _stream(grad_sino)))
-        return out
+                 _ptr(grad_sino.contiguous()), _ptr(medians.contiguous()), _ptr(out),
+                 _stream(grad_sino)))
+        return out if batch else out[0]
 
-    def sinograms_f64(self, image_cm: torch.Tensor, rows: int, cols: int, angles_deg, tfuncs):
+    def sinograms_f64(self, image_cm: torch.Tensor, rows: int, cols: int, angles_deg, tfuncs,
+                      out: Optional[torch.Tensor] = None, med_out: Optional[torch.Tensor] = None):
         """T0-T2 sinograms of a double image in double: (nT, A, N) and medians."""
         n = pad_geometry(rows, cols)[0]
         ang = np.ascontiguousarray(np.asarray(angles_deg, np.float32))
         ids = np.ascontiguousarray(np.asarray([int(t) for t in tfuncs], np.int32))
-        out = torch.empty((len(ids), len(ang), n), dtype=torch.float64, device=image_cm.device)
-        med = torch.empty(out.shape, dtype=torch.int32, device=image_cm.device)
+        if out is None:
+            out = torch.empty((len(ids), len(ang), n), dtype=torch.float64,
+                              device=image_cm.device)
+        med = med_out if med_out is not None else torch.empty(out.shape, dtype=torch.int32,
+                                                                device=image_cm.device)
         check(lib().tt_sinograms_f64_device(
             self.plan.handle, _ptr(image_cm), rows, cols,
             ang.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(ang),
