@@ -164,6 +164,29 @@ tt_status tt_circus_device(tt_plan *plan, const float *d_sino, int rows, int col
                            int n_sino, const tt_pfunctional *pfuncs, int n_p,
                            const int32_t *centers, float *d_out, void *stream);
 
+/* Orthonormal (Hermite) circus functions of n_sino stacked rows x cols
+ * sinograms (as tt_sinograms_device wrote them): each sinogram's nearest
+ * orthonormal sinogram (c++/src/circus.cpp:68-102; here a parallel one-sided
+ * Jacobi SVD in double on the device), then the Hermite P-functionals with
+ * the center it yields (c++/src/transform.cpp:75-85).  pfuncs must all be
+ * TT_P_HERMITE (their centers are ignored).  d_out: n_sino x n_p x cols;
+ * centers (host, may be NULL): the n_sino centers used.  The reference runs
+ * this only on images stretched to tt_ortho_size; here it takes sinograms of
+ * any size, so a Hermite circus can sit beside P1-P3 of the regular
+ * sinograms.  Synchronises the stream once (the aligned matrices' sizes
+ * depend on the weighted medians) and then once per Jacobi sweep. */
+tt_status tt_circus_orthonormal_device(tt_plan *plan, const float *d_sino, int rows, int cols,
+                                       int n_sino, const tt_pfunctional *pfuncs, int n_p,
+                                       float *d_out, int32_t *centers, void *stream);
+
+/* Replaces nearest_orthonormal_sinogram(const Eigen::MatrixXf&, unsigned
+ * int& new_center) (c++/src/circus.cpp:68-102) for one rows x cols host
+ * sinogram.  out must hold 2 rows x cols floats; *out_rows receives the
+ * aligned row count m (out is m x cols), *new_center the center.
+ * TT_ERR_UNSUPPORTED when m < cols (the reference's U.block needs m >= cols). */
+tt_status tt_nos(tt_plan *plan, const float *sinogram, int rows, int cols, float *out,
+                 int32_t *out_rows, int32_t *new_center);
+
 /* z-score of n_vec consecutive vectors of length len (device). */
 tt_status tt_zscore_device(tt_plan *plan, const float *d_in, int n_vec, int len,
                            float *d_out, void *stream);

@@ -1,0 +1,64 @@
+"""Nearest orthonormal sinogram on the device (c++/src/circus.cpp:68-102)
+against the oracle's, and the orthonormal Hermite circus built on it."""
+import numpy as np
+import pytest
+
+import tracetransform_gb300 as tt
+from tracetransform_gb300._native import TTError
+from tracetransform_gb300.synthetic import blob_image
+
+pytestmark = pytest.mark.gpu
+
+
+def _sino(O, rows, cols, step, t=0, seed=3):
+    img = blob_image(rows, cols, 6, (3, 12), (40, 200), seed)
+    return O.sinograms(O.pad(img), O.angles_for_step(step), [t])[0]
+
+
+@pytest.mark.parametrize("rows,cols,step,t", [(20, 13, 15, 0), (48, 48, 8, 1), (40, 40, 6, 2),
+                                               (64, 48, 5, 0)])
+def test_nos_vs_oracle(oracle_lib, rows, cols, step, t):
+    sino = _sino(oracle_lib, rows, cols, step, t)
+    want, want_c = oracle_lib.nos(sino)
+    got, got_c = tt.nearest_orthonormal_sinogram(sino)
+    assert got.shape == want.shape and got_c == want_c
+    np.testing.assert_allclose(got, want, rtol=0, atol=2e-5)
+
+
+def test_nos_orthonormal_columns_full_size(oracle_lib):
+    """256 x 256 image, 360 angles (N = 363): columns of the result are
+    orthonormal and agree with the oracle's double Jacobi."""
+    sino = _sino(oracle_lib, 256, 256, 1, 0, seed=1)
+    got, c = tt.nearest_orthonormal_sinogram(sino)
+    g = got.astype(np.float64)
+    gram = g.T @ g
+    assert np.abs(gram - np.eye(gram.shape[0])).max() < 1e-4
+    want, wc = oracle_lib.nos(sino)
+    assert c == wc
+    assert np.abs(got - want).max() < 1e-4
+
+
+def test_nos_needs_rows(oracle_lib):
+    sino = _sino(oracle_lib, 12, 12, 1)  # 360 angles, N = 17: m < cols
+    with pytest.raises(TTError):
+        tt.nearest_orthonormal_sinogram(sino)
+
+
+def test_orthonormal_circus_device(oracle_lib):
+    import torch
+    from tracetransform_gb300.device import Engine
+    O = oracle_lib
+    img = blob_image(48, 40, 5, (3, 10), (40, 200), 9)
+    ang = O.angles_for_step(8)
+    tfs = [0, 1, 3]
+    ref = O.sinograms(O.pad(img), ang, tfs)  # (nT, N, A)
+    eng = Engine(0)
+    sino = torch.from_numpy(np.ascontiguousarray(ref.transpose(0, 2, 1))).cuda()
+    got, centers = eng.circus_orthonormal(sino, [1, 2, 3, 4, 5])
+    got = got.cpu().numpy()
+    for t in range(len(tfs)):
+        nos, c = O.nos(ref[t])
+        assert centers[t] == c
+        want = O.circus(nos, [(0, o, c) for o in (1, 2, 3, 4, 5)])
+        scale = np.abs(want).max(axis=1, keepdims=True)
+        assert np.abs(got[t] - want).max() <= 1e-3 * scale.max()

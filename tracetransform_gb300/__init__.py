@@ -8,12 +8,13 @@ host side.  Build the library with ``python -m tracetransform_gb300.build``.
 from . import api
 from .api import (PFunctional, PFunctionalWrapper, Plan, TFunctional, TFunctionalWrapper,
                   Transformer, ValidationError, angles_from_step, getCircusFunctions,
-                  getSinograms, ortho_size, pad, pad_geometry, rotate, transform_batch,
-                  writecsv, zscore)
+                  getSinograms, nearest_orthonormal_sinogram, ortho_size, pad, pad_geometry,
+                  rotate, transform_batch, writecsv, zscore)
 
 __all__ = [
     "PFunctional", "PFunctionalWrapper", "Plan", "TFunctional", "TFunctionalWrapper",
     "Transformer", "ValidationError", "angles_from_step", "getCircusFunctions", "getSinograms",
-    "ortho_size", "pad", "pad_geometry", "rotate", "transform_batch", "writecsv", "zscore",
+    "nearest_orthonormal_sinogram", "ortho_size", "pad", "pad_geometry", "rotate",
+    "transform_batch", "writecsv", "zscore",
 ]
 __version__ = "0.1.0"

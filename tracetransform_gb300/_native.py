@@ -25,6 +25,7 @@ EXPORTS = (
     "tt_circus_zscore_noalloc", "tt_transform_batch", "tt_transform_batch_device",
     "tt_circus_backward_device", "tt_sinograms_backward_device", "tt_sinograms_f64_device",
     "tt_circus_f64_device", "tt_circus_backward_f64_device", "tt_sinograms_backward_f64_device",
+    "tt_circus_orthonormal_device", "tt_nos",
 )
 
 
@@ -97,6 +98,9 @@ def lib():
         "tt_sinograms_f64_device": [_P, _P, _int, _int, _F, _int, _I32, _int, _P, _P, _P],
         "tt_circus_f64_device": [_P, _P, _int, _int, _int, ctypes.POINTER(PFunctionalC), _int,
                                  _P, _P],
+        "tt_circus_orthonormal_device": [_P, _P, _int, _int, _int, ctypes.POINTER(PFunctionalC),
+                                         _int, _P, _I32, _P],
+        "tt_nos": [_P, _F, _int, _int, _F, _I32, _I32],
     }
     for name, args in sig.items():
         fn = getattr(l, name)

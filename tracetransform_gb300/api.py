@@ -236,6 +236,19 @@ def getCircusFunctions(sinogram, pfunctionals: Sequence,
     return [out[p * cols:(p + 1) * cols].copy() for p in range(len(pfs))]
 
 
+def nearest_orthonormal_sinogram(sinogram, plan: Optional[Plan] = None):
+    """(nos, new_center) of c++/src/circus.cpp:68-102 for one N x A sinogram:
+    the columns aligned on their weighted medians and replaced by the polar
+    factor U V^T (device Jacobi SVD in double)."""
+    sinogram = np.asarray(sinogram, dtype=np.float32)
+    rows, cols = sinogram.shape
+    out = np.zeros(2 * rows * cols, np.float32)
+    m, c = ctypes.c_int32(), ctypes.c_int32()
+    check(lib().tt_nos(_handle(plan), fptr(_colmajor(sinogram)), rows, cols, fptr(out),
+                       ctypes.byref(m), ctypes.byref(c)))
+    return out[: m.value * cols].reshape((m.value, cols), order="F"), c.value
+
+
 def rotate(image, angle_degrees: float, plan: Optional[Plan] = None) -> np.ndarray:
     """rotate(image, ((cols-1)/2, (rows-1)/2), deg2rad(angle)) of
     c++/src/auxiliary.cpp:223-255, bit-identical to the reference."""

@@ -27,6 +27,7 @@
 #endif
 
 using tt::CircusArgs;
+using tt::NosDesc;
 using tt::SinoArgs;
 
 namespace {
@@ -163,95 +164,6 @@ std::vector<float> resize_image(const float *in, int in_rows, int in_cols, int r
     return out;
 }
 
-int find_weighted_median(const float *x, int n) {
-    float sum = 0.f;
-    for (int i = 0; i < n; i++)
-        sum += x[i];
-    float integral = 0.f;
-    for (int i = 0; i < n; i++) {
-        integral += x[i];
-        if (2 * integral >= sum)
-            return i;
-    }
-    return n - 1;
-}
-
-// Nearest orthonormal sinogram (c++/src/circus.cpp:68-102): per-column median
-// offsets, alignment into (rows + padding) x cols, then the polar factor
-// U V^T of the aligned matrix, here from a one-sided Jacobi SVD in double.
-tt_status nearest_orthonormal(const float *sino, int rows, int cols, std::vector<float> &out,
-                              int *out_rows, int *new_center) {
-    const int center = (int)std::floor((rows - 1) / 2.0);
-    std::vector<int> offset(cols);
-    for (int p = 0; p < cols; p++)
-        offset[p] = find_weighted_median(sino + (size_t)p * rows, rows) - center;
-    const int mn = *std::min_element(offset.begin(), offset.end());
-    const int mx = *std::max_element(offset.begin(), offset.end());
-    const int m = rows + std::abs(mx) + std::abs(mn);
-    if (m < cols)
-        return fail(TT_ERR_UNSUPPORTED,
-                    "nearest orthonormal sinogram needs at least as many rows (%d) as angles (%d)",
-                    m, cols);
-    *new_center = center + mx;
-    *out_rows = m;
-    std::vector<double> a((size_t)m * cols, 0.0), v((size_t)cols * cols, 0.0);
-    for (int col = 0; col < cols; col++)
-        for (int row = 0; row < rows; row++)
-            a[(size_t)(mx + row - offset[col]) + (size_t)col * m] = sino[(size_t)row + (size_t)col * rows];
-    for (int i = 0; i < cols; i++)
-        v[(size_t)i * cols + i] = 1.0;
-    for (int sweep = 0; sweep < 60; sweep++) {
-        double off = 0.0;
-        for (int p = 0; p < cols - 1; p++) {
-            for (int q = p + 1; q < cols; q++) {
-                double *ap = &a[(size_t)p * m], *aq = &a[(size_t)q * m];
-                double al = 0, be = 0, ga = 0;
-                for (int i = 0; i < m; i++) {
-                    al += ap[i] * ap[i];
-                    be += aq[i] * aq[i];
-                    ga += ap[i] * aq[i];
-                }
-                if (ga == 0 || std::fabs(ga) <= 1e-15 * std::sqrt(al * be))
-                    continue;
-                off = std::max(off, std::fabs(ga) / std::sqrt(al * be));
-                const double zeta = (be - al) / (2 * ga);
-                const double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1 + zeta * zeta));
-                const double c = 1 / std::sqrt(1 + t * t), s = c * t;
-                for (int i = 0; i < m; i++) {
-                    const double x = ap[i], y = aq[i];
-                    ap[i] = c * x - s * y;
-                    aq[i] = s * x + c * y;
-                }
-                double *vp = &v[(size_t)p * cols], *vq = &v[(size_t)q * cols];
-                for (int i = 0; i < cols; i++) {
-                    const double x = vp[i], y = vq[i];
-                    vp[i] = c * x - s * y;
-                    vq[i] = s * x + c * y;
-                }
-            }
-        }
-        if (off < 1e-15)
-            break;
-    }
-    for (int k = 0; k < cols; k++) {
-        double nrm = 0;
-        double *ak = &a[(size_t)k * m];
-        for (int i = 0; i < m; i++)
-            nrm += ak[i] * ak[i];
-        nrm = std::sqrt(nrm);
-        for (int i = 0; i < m; i++)
-            ak[i] = nrm > 0 ? ak[i] / nrm : 0.0;
-    }
-    out.assign((size_t)m * cols, 0.f);
-    for (int j = 0; j < cols; j++)
-        for (int i = 0; i < m; i++) {
-            double acc = 0;
-            for (int k = 0; k < cols; k++)
-                acc += a[i + (size_t)k * m] * v[j + (size_t)k * cols];
-            out[i + (size_t)j * m] = (float)acc;
-        }
-    return TT_OK;
-}
 
 } // namespace
 
@@ -266,6 +178,15 @@ struct tt_plan {
     std::map<std::vector<float>, float2 *> trig;        // angle list -> (c, s)
     std::map<std::vector<long>, const float **> herm_ptrs;
     DevBuf in, sino, circ, sig, region, nos, batch_in, batch_out, params;
+    // nearest orthonormal sinogram scratch (double matrices, V, norms, ...)
+    DevBuf nos_a, nos_work, nos_desc, nos_off;
+    // the QR and one Jacobi sweep as graphs, for the buffers and sizes they
+    // were captured with
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<const void *> key;
+    } nos_factor_graph, nos_sweep_graph;
+    cudaStream_t capture_stream = nullptr;
     SourceTexture src;
     tt::BatchEngine *batch = nullptr;
     // backward / double-precision tables
@@ -352,8 +273,14 @@ struct tt_plan {
         src.release();
         for (void *p : owned)
             cudaFree(p);
-        for (DevBuf *b : {&in, &sino, &circ, &sig, &region, &nos, &batch_in, &batch_out, &params})
+        for (DevBuf *b : {&in, &sino, &circ, &sig, &region, &nos, &batch_in, &batch_out, &params,
+                          &nos_a, &nos_work, &nos_desc, &nos_off})
             cudaFree(b->p);
+        for (Graph *g : {&nos_factor_graph, &nos_sweep_graph})
+            if (g->exec)
+                cudaGraphExecDestroy(g->exec);
+        if (capture_stream)
+            cudaStreamDestroy(capture_stream);
         if (stream)
             cudaStreamDestroy(stream);
         cudaSetDevice(prev);
@@ -362,6 +289,32 @@ struct tt_plan {
     tt_status alloc(void **p, size_t bytes) {
         TT_CUDA(cudaMalloc(p, bytes > 0 ? bytes : 1));
         owned.push_back(*p);
+        return TT_OK;
+    }
+    // Capture fn's launches on the plan's capture stream as g (unless g was
+    // captured with the same key) so that they replay as one graph launch.
+    template <typename F> tt_status graph(Graph &g, const std::vector<const void *> &key, F fn) {
+        if (g.exec && g.key == key)
+            return TT_OK;
+        if (g.exec) {
+            TT_CUDA(cudaGraphExecDestroy(g.exec));
+            g.exec = nullptr;
+        }
+        if (!capture_stream)
+            TT_CUDA(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking));
+        TT_CUDA(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal));
+        const cudaError_t le = fn(capture_stream);
+        cudaGraph_t gr = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(capture_stream, &gr);
+        cudaError_t ie = cudaSuccess;
+        if (le == cudaSuccess && ce == cudaSuccess)
+            ie = cudaGraphInstantiate(&g.exec, gr, 0);
+        if (gr)
+            cudaGraphDestroy(gr);
+        TT_CUDA(le);
+        TT_CUDA(ce);
+        TT_CUDA(ie);
+        g.key = key;
         return TT_OK;
     }
     tt_status ensure(DevBuf &b, size_t bytes) {
@@ -666,6 +619,99 @@ tt_status run_circus(tt_plan *p, const float *d_sino, int rows, int cols, int n_
         return fail(TT_ERR_UNSUPPORTED, "sinogram length %d exceeds the shared-memory column buffers",
                     rows);
     TT_CUDA(tt::launch_circus(a, st));
+    return TT_OK;
+}
+
+// Nearest orthonormal sinograms (c++/src/circus.cpp:68-102) of n_sino device
+// sinograms of rows x cols: results in p->nos, desc[s].out_off / .m per
+// sinogram, centers[s] the new Hermite centers.  One host synchronisation:
+// the aligned matrices' sizes depend on the weighted medians.
+tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sino,
+                  cudaStream_t st, std::vector<NosDesc> &desc, std::vector<int> &centers) {
+    const int center = (int)std::floor((rows - 1) / 2.0);
+    const size_t ncol = (size_t)cols * n_sino;
+    TT_CHECK(p->ensure(p->nos_off, sizeof(int) * std::max<size_t>(ncol, 1)));
+    TT_CUDA(tt::launch_nos_offsets(d_sino, rows, cols, n_sino, center, (int *)p->nos_off.p, st));
+    std::vector<int> off(ncol);
+    TT_CUDA(cudaMemcpyAsync(off.data(), p->nos_off.p, sizeof(int) * ncol, cudaMemcpyDeviceToHost,
+                            st));
+    TT_CUDA(cudaStreamSynchronize(st));
+    desc.assign(n_sino, NosDesc{});
+    centers.assign(n_sino, 0);
+    size_t a_elems = 0;
+    int max_m = 0;
+    for (int s = 0; s < n_sino; s++) {
+        const int *o = off.data() + (size_t)s * cols;
+        const int mn = *std::min_element(o, o + cols), mx = *std::max_element(o, o + cols);
+        const int m = rows + std::abs(mx) + std::abs(mn);
+        if (m < cols)
+            return fail(TT_ERR_UNSUPPORTED,
+                        "nearest orthonormal sinogram needs at least as many rows (%d) as angles "
+                        "(%d)", m, cols);
+        desc[s].a_off = desc[s].out_off = (long long)a_elems;
+        desc[s].m = m;
+        desc[s].mx = mx;
+        centers[s] = center + mx;
+        a_elems += (size_t)m * cols;
+        max_m = std::max(max_m, m);
+    }
+    TT_CHECK(p->ensure(p->nos_a, sizeof(double) * a_elems));
+    TT_CHECK(p->ensure(p->nos_desc, sizeof(NosDesc) * n_sino));
+    TT_CHECK(p->ensure(p->nos, sizeof(float) * a_elems));
+    if (tt::nos_apply_smem(max_m) > 227 * 1024)
+        return fail(TT_ERR_UNSUPPORTED, "nearest orthonormal sinogram of %d rows is too tall", max_m);
+    // scratch: 3 double + 1 int vectors of n, 3 float n x n matrices, 1 float vector
+    const size_t nv = ncol, nm = (size_t)cols * cols * n_sino;
+    TT_CHECK(p->ensure(p->nos_work, sizeof(double) * 3 * nv + sizeof(int) * nv +
+                                        sizeof(float) * (3 * nm + nv) + sizeof(unsigned) * n_sino +
+                                        64));
+    tt::NosWork w;
+    {
+        char *q = (char *)p->nos_work.p;
+        w.norms = (double *)q;
+        w.orig = w.norms + nv;
+        w.tau = w.orig + nv;
+        w.X = (float *)(w.tau + nv);
+        w.V = w.X + nm;
+        w.P = w.V + nm;
+        w.inv = w.P + nm;
+        w.perm = (int *)(w.inv + nv);
+        w.off_bits = (unsigned *)(w.perm + nv);
+    }
+    TT_CUDA(cudaMemcpyAsync(p->nos_desc.p, desc.data(), sizeof(NosDesc) * n_sino,
+                            cudaMemcpyHostToDevice, st));
+    double *A = (double *)p->nos_a.p;
+    const NosDesc *d_desc = (const NosDesc *)p->nos_desc.p;
+    TT_CUDA(tt::launch_nos_align(d_sino, rows, cols, n_sino, d_desc, (const int *)p->nos_off.p,
+                                 A, a_elems, st));
+    // QR (2 cols + 2 launches) and one Jacobi sweep (about cols launches),
+    // each captured once per buffer set and size and replayed
+    const std::vector<const void *> key = {A, d_desc, p->nos_work.p,
+                                           (const void *)(size_t)cols,
+                                           (const void *)(size_t)n_sino};
+    TT_CHECK(p->graph(p->nos_factor_graph, key, [&](cudaStream_t cs) {
+        return tt::launch_nos_factor(A, d_desc, cols, n_sino, w, cs);
+    }));
+    TT_CHECK(p->graph(p->nos_sweep_graph, key, [&](cudaStream_t cs) {
+        return tt::launch_nos_sweep(cols, n_sino, w, cs);
+    }));
+    TT_CUDA(cudaGraphLaunch(p->nos_factor_graph.exec, st));
+    std::vector<unsigned> bits(n_sino);
+    for (int sweep = 0; sweep < 40; sweep++) {
+        TT_CUDA(cudaGraphLaunch(p->nos_sweep_graph.exec, st));
+        TT_CUDA(cudaMemcpyAsync(bits.data(), w.off_bits, sizeof(unsigned) * n_sino,
+                                cudaMemcpyDeviceToHost, st));
+        TT_CUDA(cudaStreamSynchronize(st));
+        float worst = 0.f;
+        for (unsigned b : bits) {
+            float v;
+            std::memcpy(&v, &b, sizeof v);
+            worst = std::max(worst, v);
+        }
+        if (worst < tt::nos_sweep_done_bound())
+            break;
+    }
+    TT_CUDA(tt::launch_nos_assemble(A, d_desc, cols, n_sino, max_m, w, (float *)p->nos.p, st));
     return TT_OK;
 }
 
@@ -1029,6 +1075,56 @@ tt_status tt_circus_device(tt_plan *plan, const float *d_sino, int rows, int col
                       pick_stream(p, stream));
 }
 
+tt_status tt_circus_orthonormal_device(tt_plan *plan, const float *d_sino, int rows, int cols,
+                                       int n_sino, const tt_pfunctional *pfuncs, int n_p,
+                                       float *d_out, int32_t *centers, void *stream) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    unsigned need;
+    TT_CHECK(check_pfuncs(pfuncs, n_p, false, &need));
+    for (int i = 0; i < n_p; i++)
+        if (pfuncs[i].kind != TT_P_HERMITE)
+            return fail(TT_ERR_INVALID_ARG, "the orthonormal circus takes Hermite P-functionals "
+                                            "only");
+    if (rows <= 0 || cols < 0 || n_sino < 0 || !d_sino || (n_p > 0 && !d_out))
+        return fail(TT_ERR_INVALID_ARG, "bad sinogram stack %dx%dx%d", n_sino, rows, cols);
+    if (n_sino == 0 || cols == 0)
+        return TT_OK;
+    cudaStream_t st = pick_stream(p, stream);
+    std::vector<NosDesc> desc;
+    std::vector<int> c;
+    TT_CHECK(run_nos(p, d_sino, rows, cols, n_sino, st, desc, c));
+    for (int s = 0; s < n_sino; s++) {
+        const int32_t c32 = c[s];
+        TT_CHECK(run_circus(p, (const float *)p->nos.p + desc[s].out_off, desc[s].m, cols, 1,
+                            pfuncs, n_p, &c32, need, d_out + (size_t)s * n_p * cols, st));
+        if (centers)
+            centers[s] = c32;
+    }
+    return TT_OK;
+}
+
+tt_status tt_nos(tt_plan *plan, const float *sinogram, int rows, int cols, float *out,
+                 int32_t *out_rows, int32_t *new_center) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    if (rows <= 0 || cols <= 0 || !sinogram || !out || !out_rows || !new_center)
+        return fail(TT_ERR_INVALID_ARG, "bad sinogram %dx%d or NULL output", rows, cols);
+    cudaStream_t st = p->stream;
+    TT_CHECK(p->ensure(p->sino, sizeof(float) * (size_t)rows * cols));
+    TT_CUDA(cudaMemcpyAsync(p->sino.p, sinogram, sizeof(float) * (size_t)rows * cols,
+                            cudaMemcpyHostToDevice, st));
+    std::vector<NosDesc> desc;
+    std::vector<int> c;
+    TT_CHECK(run_nos(p, (const float *)p->sino.p, rows, cols, 1, st, desc, c));
+    TT_CUDA(cudaMemcpyAsync(out, p->nos.p, sizeof(float) * (size_t)desc[0].m * cols,
+                            cudaMemcpyDeviceToHost, st));
+    TT_CUDA(cudaStreamSynchronize(st));
+    *out_rows = desc[0].m;
+    *new_center = c[0];
+    return TT_OK;
+}
+
 tt_status tt_zscore_device(tt_plan *plan, const float *d_in, int n_vec, int len, float *d_out,
                            void *stream) {
     tt_plan *p;
@@ -1179,22 +1275,15 @@ tt_status tt_transform(tt_plan *plan, const float *image, int rows, int cols,
         TT_CHECK(run_circus(p, (const float *)p->sino.p, n, A, n_t, pfuncs, n_p, nullptr, pneed,
                             (float *)p->circ.p, st));
     } else {
-        // nearest orthonormal sinogram per T (host), then Hermite circus
-        std::vector<float> h_sino(sino_elems);
-        TT_CUDA(cudaMemcpyAsync(h_sino.data(), p->sino.p, sizeof(float) * sino_elems,
-                                cudaMemcpyDeviceToHost, st));
-        TT_CUDA(cudaStreamSynchronize(st));
+        // nearest orthonormal sinogram per T (device), then the Hermite circus
+        std::vector<NosDesc> desc;
+        std::vector<int> centers;
+        TT_CHECK(run_nos(p, (const float *)p->sino.p, n, A, n_t, st, desc, centers));
         for (int t = 0; t < n_t; t++) {
-            std::vector<float> nos;
-            int m = 0, center = 0;
-            TT_CHECK(nearest_orthonormal(h_sino.data() + (size_t)t * n * A, n, A, nos, &m, &center));
-            TT_CHECK(p->ensure(p->nos, sizeof(float) * nos.size()));
-            TT_CUDA(cudaMemcpyAsync(p->nos.p, nos.data(), sizeof(float) * nos.size(),
-                                    cudaMemcpyHostToDevice, st));
-            const int32_t c32 = center;
-            TT_CHECK(run_circus(p, (const float *)p->nos.p, m, A, 1, pfuncs, n_p, &c32, pneed,
-                                (float *)p->circ.p + (size_t)t * n_p * A, st));
-            TT_CUDA(cudaStreamSynchronize(st));
+            const int32_t c32 = centers[t];
+            TT_CHECK(run_circus(p, (const float *)p->nos.p + desc[t].out_off, desc[t].m, A, 1,
+                                pfuncs, n_p, &c32, pneed, (float *)p->circ.p + (size_t)t * n_p * A,
+                                st));
         }
     }
     if (signatures)

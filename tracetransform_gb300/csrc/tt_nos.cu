@@ -1,0 +1,556 @@
+// tt_nos.cu -- nearest orthonormal sinogram on the device.
+//
+// The reference's orthonormal mode (c++/src/circus.cpp:68-102) shifts every
+// sinogram column by its weighted-median offset into an m x A matrix
+// (m = N + padding) and replaces it by the polar factor U V^T of its SVD,
+// computed by Eigen's float JacobiSVD with a column-pivoting Householder QR
+// preconditioner.  Here, for n_sino sinograms at once, the same structure
+// with the precision split that GB300's rates call for (FP64 ~1/64 of FP32):
+//
+//   nos_offsets   per column: weighted median row - center, with the
+//                 reference's sequential float sums (one thread per column)
+//   nos_align     the shifted columns into a zeroed m x A double matrix
+//   QR            column-pivoting Householder QR, A P = Q R, in double (the
+//                 only double-precision stage: it fixes the small singular
+//                 directions that a float factorisation would lose); per
+//                 column step one pivot/reflector launch and one trailing-
+//                 update launch, LAPACK-style (reflector below the diagonal,
+//                 tau, partial column norms downdated and recomputed when
+//                 cancellation sets in)
+//   Jacobi        one-sided Jacobi on X = R^T in float (R^T of a pivoted QR is
+//                 graded, so float rotations keep relative accuracy): round-
+//                 robin rounds of A/2 disjoint column pairs, one warp per
+//                 pair, V accumulated; X V = U_X S, so polar(R) = V U_X^T
+//   assemble      P = V U_X^T (float) with one Newton-Schulz step to clean
+//                 its orthogonality, then polar(A P) = Q [P; 0] applied
+//                 reflector by reflector per group of columns in shared
+//                 memory, and the column permutation undone
+//
+// Against the oracle's double one-sided Jacobi on the aligned matrix the
+// result agrees to ~3e-5 absolute (entries up to ~0.7) for condition numbers
+// up to ~1e6; Eigen's float SVD of the same matrices is far less accurate.
+// Every launch is bounded; there is no grid-wide wait.
+#include "tt_common.cuh"
+#include "tt_internal.h"
+
+namespace tt {
+namespace {
+
+__global__ void nos_offsets_kernel(const float *__restrict__ sino, int rows, int n_cols,
+                                   int center, int *__restrict__ offsets) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= n_cols)
+        return;
+    const float *x = sino + (size_t)idx * rows;
+    float sum = 0.f;
+    for (int i = 0; i < rows; i++)
+        sum = __fadd_rn(sum, x[i]);
+    float integral = 0.f;
+    int m = rows - 1;
+    for (int i = 0; i < rows; i++) {
+        integral = __fadd_rn(integral, x[i]);
+        if (2.f * integral >= sum) {
+            m = i;
+            break;
+        }
+    }
+    offsets[idx] = m - center;
+}
+
+// grid (cols, n_sino); A_s must be zeroed before.
+__global__ void nos_align_kernel(const float *__restrict__ sino, int rows, int cols,
+                                 const NosDesc *__restrict__ desc,
+                                 const int *__restrict__ offsets, double *__restrict__ A) {
+    const int col = blockIdx.x, s = blockIdx.y;
+    const NosDesc d = desc[s];
+    const int shift = d.mx - offsets[(size_t)s * cols + col];
+    const float *src = sino + ((size_t)s * cols + col) * rows;
+    double *dst = A + d.a_off + (size_t)col * d.m + shift;
+    for (int r = threadIdx.x; r < rows; r += blockDim.x)
+        dst[r] = (double)src[r];
+}
+
+template <typename T, int kThreads> __device__ __forceinline__ T block_sum(T v, T *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(TT_FULL_MASK, v, o);
+    if (lane == 0)
+        red[warp] = v;
+    __syncthreads();
+    T t = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; w++)
+        t += red[w];
+    __syncthreads();
+    return t;
+}
+
+// ---- column-pivoting Householder QR (double) ------------------------------
+
+constexpr int kQrThreads = 256;
+
+// Squared column norms (partial and reference copy) and the identity
+// permutation.  grid (n, n_sino).
+__global__ void __launch_bounds__(kQrThreads)
+qr_init_kernel(const double *__restrict__ A, const NosDesc *__restrict__ desc, int n,
+               double *__restrict__ norms, double *__restrict__ orig, int *__restrict__ perm) {
+    __shared__ double red[kQrThreads / 32];
+    const int j = blockIdx.x, s = blockIdx.y;
+    const NosDesc d = desc[s];
+    const double *a = A + d.a_off + (size_t)j * d.m;
+    double v = 0;
+    for (int i = threadIdx.x; i < d.m; i += kQrThreads)
+        v += a[i] * a[i];
+    v = block_sum<double, kQrThreads>(v, red);
+    if (threadIdx.x == 0) {
+        norms[(size_t)s * n + j] = v;
+        orig[(size_t)s * n + j] = v;
+        perm[(size_t)s * n + j] = j;
+    }
+}
+
+// Step k, one CTA per sinogram: pivot = the remaining column of largest
+// partial norm (lowest index on ties), swapped into place; then the
+// reflector H = I - tau v v^T with H A[k:, k] = (beta, 0, ...): beta on the
+// diagonal, v[1:] below it (v[0] = 1 implicit).
+__global__ void __launch_bounds__(kQrThreads)
+qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n, int k,
+                double *__restrict__ norms, double *__restrict__ orig, int *__restrict__ perm,
+                double *__restrict__ tau) {
+    __shared__ double red[kQrThreads / 32];
+    __shared__ double bv[kQrThreads / 32];
+    __shared__ int bi[kQrThreads / 32];
+    __shared__ int piv;
+    const int s = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const NosDesc d = desc[s];
+    double *As = A + d.a_off;
+    double *nr = norms + (size_t)s * n, *og = orig + (size_t)s * n;
+    int *pm = perm + (size_t)s * n;
+    // argmax of the partial norms over j >= k
+    double best = -1;
+    int bidx = n;
+    for (int j = k + threadIdx.x; j < n; j += kQrThreads) {
+        const double v = nr[j];
+        if (v > best || (v == best && j < bidx)) {
+            best = v;
+            bidx = j;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_xor_sync(TT_FULL_MASK, best, o);
+        const int oi = __shfl_xor_sync(TT_FULL_MASK, bidx, o);
+        if (ov > best || (ov == best && oi < bidx)) {
+            best = ov;
+            bidx = oi;
+        }
+    }
+    if (lane == 0) {
+        bv[warp] = best;
+        bi[warp] = bidx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = bv[0];
+        int ix = bi[0];
+        for (int w = 1; w < kQrThreads / 32; w++)
+            if (bv[w] > b || (bv[w] == b && bi[w] < ix)) {
+                b = bv[w];
+                ix = bi[w];
+            }
+        piv = ix < n ? ix : k;
+    }
+    __syncthreads();
+    const int jp = piv;
+    if (jp != k) {
+        double *ca = As + (size_t)k * d.m, *cb = As + (size_t)jp * d.m;
+        for (int i = threadIdx.x; i < d.m; i += kQrThreads) {
+            const double t = ca[i];
+            ca[i] = cb[i];
+            cb[i] = t;
+        }
+        if (threadIdx.x == 0) {
+            double t = nr[k];
+            nr[k] = nr[jp];
+            nr[jp] = t;
+            t = og[k];
+            og[k] = og[jp];
+            og[jp] = t;
+            const int q = pm[k];
+            pm[k] = pm[jp];
+            pm[jp] = q;
+        }
+    }
+    __syncthreads();
+    // reflector of x = A[k:m, k]
+    double *x = As + (size_t)k * d.m;
+    double xn = 0;
+    for (int i = k + 1 + threadIdx.x; i < d.m; i += kQrThreads)
+        xn += x[i] * x[i];
+    xn = block_sum<double, kQrThreads>(xn, red);
+    const double alpha = x[k];
+    if (xn == 0) { // already (alpha, 0, ...): H = I
+        if (threadIdx.x == 0)
+            tau[(size_t)s * n + k] = 0;
+        return;
+    }
+    const double beta = -copysign(sqrt(alpha * alpha + xn), alpha);
+    const double scale = 1 / (alpha - beta);
+    for (int i = k + 1 + threadIdx.x; i < d.m; i += kQrThreads)
+        x[i] *= scale;
+    if (threadIdx.x == 0) {
+        tau[(size_t)s * n + k] = (beta - alpha) / beta;
+        x[k] = beta;
+    }
+}
+
+// Step k, one CTA per trailing column j = k + 1 + blockIdx.x: A[k:, j] -=
+// tau v (v . A[k:, j]), then the partial norm loses A[k, j]^2 -- recomputed
+// from the column when that leaves less than ~sqrt(eps) of the original.
+__global__ void __launch_bounds__(kQrThreads)
+qr_update_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n, int k,
+                 double *__restrict__ norms, double *__restrict__ orig,
+                 const double *__restrict__ tau) {
+    __shared__ double red[kQrThreads / 32];
+    const int j = k + 1 + blockIdx.x, s = blockIdx.y;
+    const NosDesc d = desc[s];
+    double *As = A + d.a_off;
+    const double *v = As + (size_t)k * d.m;
+    double *c = As + (size_t)j * d.m;
+    const double t = tau[(size_t)s * n + k];
+    if (t != 0) {
+        double w = 0;
+        for (int i = k + 1 + threadIdx.x; i < d.m; i += kQrThreads)
+            w += v[i] * c[i];
+        w = block_sum<double, kQrThreads>(w, red) + c[k];
+        const double tw = t * w;
+        for (int i = k + 1 + threadIdx.x; i < d.m; i += kQrThreads)
+            c[i] -= tw * v[i];
+        __syncthreads();
+        if (threadIdx.x == 0)
+            c[k] -= tw;
+        __syncthreads();
+    }
+    double *nr = norms + (size_t)s * n, *og = orig + (size_t)s * n;
+    const double a = c[k];
+    double n2 = nr[j] - a * a;
+    if (n2 <= 1.5e-8 * og[j]) { // uniform: every thread read the same values
+        double r = 0;
+        for (int i = k + 1 + threadIdx.x; i < d.m; i += kQrThreads)
+            r += c[i] * c[i];
+        n2 = block_sum<double, kQrThreads>(r, red);
+        if (threadIdx.x == 0)
+            og[j] = n2;
+    }
+    if (threadIdx.x == 0)
+        nr[j] = n2;
+}
+
+// ---- one-sided Jacobi on X = R^T (float) ----------------------------------
+
+// X[i + j n] = R[j, i] (upper triangle of the QR result), V = I.
+// grid (ceil(n * n / 256), n_sino).
+__global__ void nos_rt_kernel(const double *__restrict__ A, const NosDesc *__restrict__ desc,
+                              int n, float *__restrict__ X, float *__restrict__ V) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nn = (long long)n * n;
+    if (e >= nn)
+        return;
+    const int s = blockIdx.y, i = (int)(e % n), j = (int)(e / n);
+    const NosDesc d = desc[s];
+    X[s * nn + e] = j <= i ? (float)A[d.a_off + j + (size_t)i * d.m] : 0.f;
+    V[s * nn + e] = i == j ? 1.f : 0.f;
+}
+
+constexpr int kJacThreads = 128;
+constexpr int kJacPairs = kJacThreads / 32; // one warp per column pair
+
+// A pair is rotated when |x_p . x_q| > kJacTol |x_p| |x_q| -- a few times the
+// rounding of a float dot product over n terms split across a warp -- and a
+// sweep that rotates none (or whose largest rotated pair is below
+// kJacDone) ends the iteration.
+constexpr float kJacTol = 1e-6f, kJacDone = 1e-5f;
+
+// grid (ceil(n_pad / 2 / kJacPairs), n_sino); warp k of the grid takes pair
+// k of round r.  Pairs of round r over players 0 .. P-1 (P = n_pad, even):
+// (P-1, r) and ((r + k) mod (P-1), (r - k) mod (P-1)), k = 1 .. P/2 - 1; a
+// player >= n is the odd case's bye.  The rotation is the cyclic Jacobi one.
+__global__ void __launch_bounds__(kJacThreads)
+rt_jacobi_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int n_pad, int round,
+                       unsigned *__restrict__ off_bits) {
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * kJacPairs + (threadIdx.x >> 5), s = blockIdx.y, P1 = n_pad - 1;
+    if (k >= n_pad / 2)
+        return;
+    int p, q;
+    if (k == 0) {
+        p = P1;
+        q = round;
+    } else {
+        p = (round + k) % P1;
+        q = (round - k + P1) % P1;
+    }
+    if (p > q) {
+        const int t = p;
+        p = q;
+        q = t;
+    }
+    if (q >= n)
+        return;
+    const size_t nn = (size_t)n * n;
+    float *xp = X + s * nn + (size_t)p * n, *xq = X + s * nn + (size_t)q * n;
+    float al = 0.f, be = 0.f, ga = 0.f;
+    for (int i = lane; i < n; i += 32) {
+        const float x = xp[i], y = xq[i];
+        al = fmaf(x, x, al);
+        be = fmaf(y, y, be);
+        ga = fmaf(x, y, ga);
+    }
+    al = warp_sum(al);
+    be = warp_sum(be);
+    ga = warp_sum(ga);
+    const float nrm = sqrtf(al) * sqrtf(be);
+    if (ga == 0.f || fabsf(ga) <= kJacTol * nrm)
+        return;
+    if (lane == 0)
+        atomicMax(off_bits + s, __float_as_uint(fabsf(ga) / nrm));
+    const float zeta = (be - al) / (2.f * ga);
+    const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+    const float c = rsqrtf(1.f + t * t), sn = c * t;
+    for (int i = lane; i < n; i += 32) {
+        const float x = xp[i], y = xq[i];
+        xp[i] = c * x - sn * y;
+        xq[i] = sn * x + c * y;
+    }
+    float *vp = V + s * nn + (size_t)p * n, *vq = V + s * nn + (size_t)q * n;
+    for (int i = lane; i < n; i += 32) {
+        const float x = vp[i], y = vq[i];
+        vp[i] = c * x - sn * y;
+        vq[i] = sn * x + c * y;
+    }
+}
+
+// ---- assembly ---------------------------------------------------------------
+
+// 1 / |x_k| per column of the converged X (0 for a zero column).  grid
+// (ceil(n / 4), n_sino), one warp per column.
+__global__ void rt_invnorm_kernel(const float *__restrict__ X, int n, float *__restrict__ inv) {
+    const int k = blockIdx.x * 4 + (threadIdx.x >> 5), s = blockIdx.y, lane = threadIdx.x & 31;
+    if (k >= n)
+        return;
+    const float *x = X + (size_t)s * n * n + (size_t)k * n;
+    float v = 0.f;
+    for (int i = lane; i < n; i += 32)
+        v = fmaf(x[i], x[i], v);
+    v = warp_sum(v);
+    if (lane == 0)
+        inv[(size_t)s * n + k] = v > 0.f ? rsqrtf(v) : 0.f;
+}
+
+// X[:, k] *= inv[k]: the columns of X become U_X.  grid (ceil(n n / 256), n_sino).
+__global__ void rt_scale_kernel(float *__restrict__ X, const float *__restrict__ inv, int n) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nn = (long long)n * n;
+    if (e < nn)
+        X[blockIdx.y * nn + e] *= inv[(size_t)blockIdx.y * n + (int)(e / n)];
+}
+
+// C = alpha op(A) op(B) + beta D for n x n column-major float matrices per
+// sinogram, op given by strides: op(A)(i, k) = A[i ai + k ak], op(B)(k, j) =
+// B[k bk + j bj].  32 x 32 output tiles (256 threads, 4 outputs each), k in
+// shared-memory steps of 32.  grid (ceil(n / 32), ceil(n / 32), n_sino).
+__global__ void __launch_bounds__(256)
+rt_gemm_kernel(const float *__restrict__ A, int ai, int ak, const float *__restrict__ B, int bk,
+               int bj, const float *__restrict__ D, float alpha, float beta, int n,
+               float *__restrict__ C) {
+    __shared__ float as[32][33], bs[32][33];
+    const int ti = threadIdx.x & 31, tj = threadIdx.x >> 5; // tj 0..7
+    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+    const size_t off = (size_t)blockIdx.z * n * n;
+    A += off;
+    B += off;
+    C += off;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int k0 = 0; k0 < n; k0 += 32) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+            const int r = e & 31, kk = e >> 5, k = k0 + kk;
+            as[kk][r] = (k < n && i0 + r < n) ? A[(size_t)(i0 + r) * ai + (size_t)k * ak] : 0.f;
+            bs[kk][r] = (k < n && j0 + r < n) ? B[(size_t)k * bk + (size_t)(j0 + r) * bj] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < 32; kk++) {
+            const float a = as[kk][ti];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                acc[u] = fmaf(a, bs[kk][tj + 8 * u], acc[u]);
+        }
+    }
+    const int i = i0 + ti;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const int j = j0 + tj + 8 * u;
+        if (i < n && j < n) {
+            const size_t e = i + (size_t)j * n;
+            C[e] = beta != 0.f ? alpha * acc[u] + beta * D[off + e] : alpha * acc[u];
+        }
+    }
+}
+
+constexpr int kQThreads = 256, kQCols = 4; // columns of Y per CTA
+
+// Y = Q [P; 0] = H_0 H_1 ... H_{n-1} [P; 0] for kQCols columns of P per CTA
+// (shared memory: kQCols x m floats), then out[:, perm[j]] = Y[:, j].
+// grid (ceil(n / kQCols), n_sino).
+__global__ void __launch_bounds__(kQThreads)
+nos_apply_q_kernel(const double *__restrict__ A, const NosDesc *__restrict__ desc,
+                   const double *__restrict__ tau, const int *__restrict__ perm,
+                   const float *__restrict__ P, int n, float *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float *y = reinterpret_cast<float *>(smraw);
+    __shared__ float red[kQThreads / 32][kQCols];
+    const int s = blockIdx.y, j0 = blockIdx.x * kQCols;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const NosDesc d = desc[s];
+    const int m = d.m, nc = min(kQCols, n - j0);
+    const size_t nn = (size_t)n * n;
+    for (int c = 0; c < kQCols; c++)
+        for (int i = threadIdx.x; i < m; i += kQThreads)
+            y[c * m + i] = (c < nc && i < n) ? P[s * nn + i + (size_t)(j0 + c) * n] : 0.f;
+    const double *As = A + d.a_off, *ts = tau + (size_t)s * n;
+    for (int k = n - 1; k >= 0; k--) {
+        const float t = (float)ts[k];
+        if (t == 0.f)
+            continue; // uniform
+        const double *v = As + (size_t)k * m;
+        __syncthreads();
+        float w[kQCols];
+#pragma unroll
+        for (int c = 0; c < kQCols; c++)
+            w[c] = 0.f;
+        for (int i = k + 1 + threadIdx.x; i < m; i += kQThreads) {
+            const float vi = (float)v[i];
+#pragma unroll
+            for (int c = 0; c < kQCols; c++)
+                w[c] = fmaf(vi, y[c * m + i], w[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < kQCols; c++) {
+            w[c] = warp_sum(w[c]);
+            if (lane == 0)
+                red[warp][c] = w[c];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < kQCols; c++) {
+            float tot = y[c * m + k];
+            for (int u = 0; u < kQThreads / 32; u++)
+                tot += red[u][c];
+            w[c] = t * tot;
+        }
+        __syncthreads(); // everyone has read y[.., k] and red
+        for (int i = k + 1 + threadIdx.x; i < m; i += kQThreads) {
+            const float vi = (float)v[i];
+#pragma unroll
+            for (int c = 0; c < kQCols; c++)
+                y[c * m + i] = fmaf(-w[c], vi, y[c * m + i]);
+        }
+        if (threadIdx.x < kQCols)
+            y[threadIdx.x * m + k] -= w[threadIdx.x];
+    }
+    __syncthreads();
+    const int *pm = perm + (size_t)s * n;
+    for (int c = 0; c < nc; c++) {
+        float *o = out + d.out_off + (size_t)pm[j0 + c] * m;
+        for (int i = threadIdx.x; i < m; i += kQThreads)
+            o[i] = y[c * m + i];
+    }
+}
+
+} // namespace
+
+cudaError_t launch_nos_offsets(const float *sino, int rows, int cols, int n_sino, int center,
+                               int *offsets, cudaStream_t st) {
+    const long long n = (long long)cols * n_sino;
+    if (n <= 0)
+        return cudaSuccess;
+    nos_offsets_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(sino, rows, (int)n, center,
+                                                                      offsets);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nos_align(const float *sino, int rows, int cols, int n_sino,
+                             const NosDesc *desc, const int *offsets, double *A, size_t a_elems,
+                             cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(A, 0, sizeof(double) * a_elems, st);
+    if (e != cudaSuccess)
+        return e;
+    nos_align_kernel<<<dim3(cols, n_sino), 128, 0, st>>>(sino, rows, cols, desc, offsets, A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nos_factor(double *A, const NosDesc *desc, int n, int n_sino,
+                              const NosWork &w, cudaStream_t st) {
+    qr_init_kernel<<<dim3(n, n_sino), kQrThreads, 0, st>>>(A, desc, n, w.norms, w.orig, w.perm);
+    for (int k = 0; k < n; k++) {
+        qr_pivot_kernel<<<n_sino, kQrThreads, 0, st>>>(A, desc, n, k, w.norms, w.orig, w.perm,
+                                                       w.tau);
+        if (k + 1 < n)
+            qr_update_kernel<<<dim3(n - k - 1, n_sino), kQrThreads, 0, st>>>(A, desc, n, k,
+                                                                            w.norms, w.orig,
+                                                                            w.tau);
+    }
+    const long long nn = (long long)n * n;
+    nos_rt_kernel<<<dim3((unsigned)((nn + 255) / 256), n_sino), 256, 0, st>>>(A, desc, n, w.X,
+                                                                              w.V);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, cudaStream_t st) {
+    const int n_pad = n + (n & 1);
+    cudaError_t e = cudaMemsetAsync(w.off_bits, 0, sizeof(unsigned) * n_sino, st);
+    if (e != cudaSuccess)
+        return e;
+    const dim3 grid((n_pad / 2 + kJacPairs - 1) / kJacPairs, n_sino);
+    for (int r = 0; r < n_pad - 1; r++)
+        rt_jacobi_round_kernel<<<grid, kJacThreads, 0, st>>>(w.X, w.V, n, n_pad, r, w.off_bits);
+    return cudaGetLastError();
+}
+
+float nos_sweep_done_bound() { return kJacDone; }
+
+size_t nos_apply_smem(int max_m) { return sizeof(float) * (size_t)kQCols * max_m; }
+
+cudaError_t launch_nos_assemble(const double *A, const NosDesc *desc, int n, int n_sino,
+                                int max_m, const NosWork &w, float *out, cudaStream_t st) {
+    const long long nn = (long long)n * n;
+    const dim3 ge((unsigned)((nn + 255) / 256), n_sino), gt((n + 31) / 32, (n + 31) / 32, n_sino);
+    rt_invnorm_kernel<<<dim3((n + 3) / 4, n_sino), 128, 0, st>>>(w.X, n, w.inv);
+    rt_scale_kernel<<<ge, 256, 0, st>>>(w.X, w.inv, n);
+    // P = V U^T, then one Newton-Schulz step P <- P (3 I - P^T P) / 2 (in the
+    // V buffer), which removes the symmetric part of P's distance from
+    // orthogonality left by the float sweeps' stopping bound; S = P^T P goes
+    // to the X buffer
+    rt_gemm_kernel<<<gt, 256, 0, st>>>(w.V, 1, n, w.X, n, 1, nullptr, 1.f, 0.f, n, w.P);
+    rt_gemm_kernel<<<gt, 256, 0, st>>>(w.P, n, 1, w.P, 1, n, nullptr, 1.f, 0.f, n, w.X);
+    rt_gemm_kernel<<<gt, 256, 0, st>>>(w.P, 1, n, w.X, 1, n, w.P, -0.5f, 1.5f, n, w.V);
+    static size_t limit = 0;
+    if (limit == 0) {
+        limit = dynamic_smem_limit((const void *)nos_apply_q_kernel);
+        cudaError_t e = cudaFuncSetAttribute(nos_apply_q_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)limit);
+        if (e != cudaSuccess)
+            return e;
+    }
+    const size_t smem = nos_apply_smem(max_m);
+    if (smem > limit)
+        return cudaErrorInvalidValue;
+    nos_apply_q_kernel<<<dim3((n + kQCols - 1) / kQCols, n_sino), kQThreads, smem, st>>>(
+        A, desc, w.tau, w.perm, w.V, n, out);
+    return cudaGetLastError();
+}
+
+} // namespace tt
