@@ -43,11 +43,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "sinograms/sec"
+HERMITE = [1, 2, 3, 4, 5]
 WORKLOADS = {
-    # name: (rows, cols, n_blobs, sigma, seed, angle_step, T list, P list)
-    "single256": (256, 256, 8, (8, 40), 1, 1.0, [0, 1, 2, 3, 4, 5], [1, 2, 3]),
-    "single1024": (1024, 1024, 32, (16, 160), 2, 1.0, [0, 1, 2, 3, 4, 5, 6, 7], [1, 2, 3]),
-    "single4096": (4096, 4096, 256, (32, 640), 6, 0.5, [0, 1, 2, 3, 4, 5, 6, 7], [1, 2, 3]),
+    # name: (rows, cols, n_blobs, sigma, seed, angle_step, T list, P list,
+    #        Hermite orders of the orthonormal circus beside P1-P3)
+    "single256": (256, 256, 8, (8, 40), 1, 1.0, [0, 1, 2, 3, 4, 5], [1, 2, 3], []),
+    "single1024": (1024, 1024, 32, (16, 160), 2, 1.0, [0, 1, 2, 3, 4, 5, 6, 7], [1, 2, 3],
+                   HERMITE),
+    "single4096": (4096, 4096, 256, (32, 640), 6, 0.5, [0, 1, 2, 3, 4, 5, 6, 7], [1, 2, 3],
+                   HERMITE),
 }
 DEFAULT_WORKLOAD = "single1024"
 L2_FLUSH_BYTES = 256 << 20
@@ -65,6 +69,9 @@ def parse_args():
     ap.add_argument("--kernel-only", type=int, default=0, metavar="CALLS",
                     help="for profiler captures: run only the fused sinogram kernel CALLS "
                          "times on the workload and exit (prints no bench line)")
+    ap.add_argument("--profile-steps", type=int, default=0, metavar="STEPS",
+                    help="for profiler launch lists: run the workload's full device step "
+                         "(sinograms, circus, z-scores, Hermite circus) STEPS times and exit")
     ap.add_argument("--tfuncs", default=None,
                     help="comma-separated T-functional ids overriding the workload's")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
@@ -74,7 +81,7 @@ def parse_args():
 
 def make_image(name):
     from tracetransform_gb300.synthetic import blob_image
-    rows, cols, nb, sigma, seed, step, tfs, pfs = WORKLOADS[name]
+    rows, cols, nb, sigma, seed, step, tfs, pfs, _ = WORKLOADS[name]
     img = blob_image(rows, cols, nb, sigma, (40, 200), seed)
     n_ang = int(np.floor(360.0 / step))
     angles = (np.arange(n_ang, dtype=np.float64) * step).astype(np.float32)
@@ -85,7 +92,10 @@ def config_dict(name, n, angles, tfs, pfs, world):
     rows, cols = WORKLOADS[name][:2]
     return {"workload": name, "image": f"{rows}x{cols}", "padded": n, "angles": len(angles),
             "angle_step_deg": WORKLOADS[name][5], "t_functionals": tfs,
-            "p_functionals": pfs, "images_per_step_per_gpu": 1,
+            "p_functionals": pfs, "hermite_orders": WORKLOADS[name][8],
+            "hermite": ("orthonormal circus on each sinogram's nearest orthonormal sinogram "
+                        "(device QR + Jacobi), beside P1-P3") if WORKLOADS[name][8] else None,
+            "images_per_step_per_gpu": 1,
             "l2": "flushed between timed steps (256 MiB write)",
             "parallelism": f"replicas{world}" if world > 1 else "single"}
 
@@ -95,27 +105,50 @@ def config_dict(name, n, angles, tfs, pfs, world):
 # ---------------------------------------------------------------------------
 
 def cpu_sample(img, angles, tfs, pfs, target_s, threads=0):
-    """Time the oracle on a growing subset of angles until it takes target_s;
-    returns (seconds per full transform, sample description, threads)."""
+    """Time the oracle on a growing subset of angles (all angles, repeated,
+    once the subset is complete) until it takes target_s; returns (seconds per
+    full transform, sample description, threads)."""
     from oracle import oracle as O
     O.build()
     padded = O.pad(img)
     nthreads = threads or os.cpu_count() or 1
     k = min(len(angles), max(1, nthreads))
+    reps = 1
     while True:
         sub = angles[:: max(1, len(angles) // k)][:k]
         t0 = time.perf_counter()
-        sino = O.sinograms(padded, sub, tfs, threads)
-        for t in range(sino.shape[0]):
-            O.circus(sino[t], [(p, 0, 0) for p in pfs], threads)
+        for _ in range(reps):
+            sino = O.sinograms(padded, sub, tfs, threads)
+            for t in range(sino.shape[0]):
+                O.circus(sino[t], [(p, 0, 0) for p in pfs], threads)
         dt = time.perf_counter() - t0
-        if dt >= target_s or len(sub) >= len(angles):
+        if dt >= target_s:
             break
-        k = min(len(angles), int(k * max(2.0, 1.2 * target_s / max(dt, 1e-3))))
-    per_image = dt * len(angles) / len(sub)
-    desc = (f"{len(sub)} of {len(angles)} angles of the same image (all T and P "
-            f"functionals), {dt:.1f} s, scaled by {len(angles) / len(sub):.2f}")
+        grow = max(2.0, 1.2 * target_s / max(dt, 1e-3))
+        if len(sub) >= len(angles):
+            reps = int(reps * grow)
+        else:
+            k = min(len(angles), int(k * grow))
+    per_image = dt / reps * len(angles) / len(sub)
+    desc = (f"{reps} x {len(sub)} of {len(angles)} angles of the same image (all T and P "
+            f"functionals), {dt:.1f} s, scaled by {len(angles) / len(sub) / reps:.3f}")
     return per_image, desc, nthreads
+
+
+def cpu_hermite_seconds(img, angles, tfs, orders):
+    """The oracle's nearest orthonormal sinogram (double Jacobi, one thread)
+    and Hermite circus for the first T-functional's full sinogram, scaled by
+    the number of T-functionals."""
+    from oracle import oracle as O
+    O.build()
+    sino = O.sinograms(O.pad(img), angles, [tfs[0]])[0]
+    t0 = time.perf_counter()
+    nos, c = O.nos(sino)
+    O.circus(nos, [(0, o, c) for o in orders])
+    dt = time.perf_counter() - t0
+    return dt * len(tfs), (f"orthonormal circus: nearest orthonormal sinogram + Hermite "
+                           f"{orders} of one {sino.shape[0]}x{sino.shape[1]} sinogram, "
+                           f"{dt:.1f} s, x{len(tfs)}")
 
 
 def run_reference(args, world, rank):
@@ -126,13 +159,17 @@ def run_reference(args, world, rank):
     O.build()
     n = O.pad_geometry(*img.shape)[0]
     target = max(1.0, args.cpu_seconds / max(1, args.steps))
+    herm = WORKLOADS[args.workload][8]
+    herm_s, herm_desc = cpu_hermite_seconds(img, angles, tfs, herm) if herm else (0.0, "")
     per = []
     desc = ""
     threads = os.cpu_count() or 1
     for i in range(args.warmup + args.steps):
         t, desc, threads = cpu_sample(img, angles, tfs, pfs, target)
         if i >= args.warmup:
-            per.append(t)
+            per.append(t + herm_s)
+    if herm:
+        desc += "; plus, timed once and added to every step, the " + herm_desc
     sec = statistics.median(per)
     value = len(tfs) / sec
     line = {"metric": METRIC, "value": value, "unit": "sinograms/s", "n_gpus": world,
@@ -240,6 +277,8 @@ def run_engine(args, world, rank, local_rank):
     sino = torch.empty((len(tfs), A, n), dtype=torch.float32, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     pf = [(p, 0, -1) for p in pfs]
+    herm = WORKLOADS[args.workload][8]
+    herm_out = torch.empty((len(tfs), len(herm), A), dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
     def step(ev_sino=None):
@@ -249,7 +288,11 @@ def run_engine(args, world, rank, local_rank):
         if ev_sino:
             ev_sino[1].record(stream)
         circ = eng.circus(sino, pf)
-        return eng.zscore(circ)
+        sig = eng.zscore(circ)
+        if herm:  # the orthonormal (Hermite) circus beside P1-P3
+            hc, _ = eng.circus_orthonormal(sino, herm, out=herm_out)
+            return sig, circ, hc, eng.zscore(hc)
+        return sig, circ
 
     for _ in range(args.warmup):
         step()
@@ -275,7 +318,15 @@ def run_engine(args, world, rank, local_rank):
     kern_ms = [a.elapsed_time(b) for a, b in ks]
     ms = sum(step_ms) / len(step_ms)
     ms = max_over_ranks(ms, world)
-    launches = 3 * args.steps
+    # sinograms, circus, z-score; with the Hermite circus: weighted-median
+    # offsets, alignment, QR (qr_init, n pivot + n - 1 update launches, R^T),
+    # the sweeps (n - 1 + (n & 1) rounds each), assembly (6), one circus
+    # launch per sinogram and a z-score
+    launches = 3
+    if herm:
+        n_pad = A + (A & 1)
+        launches += 2 + (2 * A + 1) + eng.last_sweeps * (n_pad - 1) + 6 + len(tfs) + 1
+    launches *= args.steps
 
     # end to end through the C ABI drop-in, pinned host buffers
     lib = _native.lib()
@@ -290,8 +341,24 @@ def run_engine(args, world, rank, local_rank):
     fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float))
     step_deg = WORKLOADS[args.workload][5]
 
+    h_herm = torch.empty(len(tfs) * len(herm) * A, dtype=torch.float32).pin_memory()
+    h_hsig = torch.empty_like(h_herm).pin_memory()
+
     def e2e_step():
-        if float(step_deg) == int(step_deg):
+        if herm:  # device entry points (tt_transform keeps the reference's
+            # rule that regular and orthonormal P-functionals do not mix)
+            d = h_img.to(dev, non_blocking=True).view(cols, rows)
+            eng.sinograms(d, rows, cols, angles, tfs, out=sino)
+            c = eng.circus(sino, pf)
+            z = eng.zscore(c)
+            hc, _ = eng.circus_orthonormal(sino, herm, out=herm_out)
+            hz = eng.zscore(hc)
+            h_circ.copy_(c.view(-1), non_blocking=True)
+            h_sig.copy_(z.view(-1), non_blocking=True)
+            h_herm.copy_(hc.view(-1), non_blocking=True)
+            h_hsig.copy_(hz.view(-1), non_blocking=True)
+            torch.cuda.synchronize()
+        elif float(step_deg) == int(step_deg):
             _native.check(lib.tt_transform(eng.plan.handle, fp(h_img), rows, cols, int(step_deg),
                                            _native.iptr(ids), len(ids), pfa, len(pfs), fp(h_circ),
                                            fp(h_sig)))
@@ -332,7 +399,7 @@ def run_engine(args, world, rank, local_rank):
         "config": config_dict(args.workload, n, angles, tfs, pfs, world),
         "e2e": {"value": world * len(tfs) / e2e_s, "unit": "sinograms/s",
                 "h2d_bytes_per_step": int(rows * cols * 4),
-                "d2h_bytes_per_step": int(2 * n_out * 4)},
+                "d2h_bytes_per_step": int(2 * (n_out + h_herm.numel()) * 4)},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "sino_kernel", "achieved": achieved,
                      "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
@@ -342,8 +409,14 @@ def run_engine(args, world, rank, local_rank):
                      "kernel_ms": kern_s * 1e3},
         "clocks": clk,
     }
+    if herm:
+        line["hermite_sweeps"] = eng.last_sweeps
     if not args.no_cpu_baseline:
         per, desc, cores = cpu_sample(img, angles, tfs, pfs, args.cpu_seconds)
+        if herm:
+            hs, hd = cpu_hermite_seconds(img, angles, tfs, herm)
+            per += hs
+            desc += "; plus the " + hd
         line["cpu_baseline"] = {"value": len(tfs) / per, "unit": "sinograms/s", "cores": cores,
                                 "kind": "port", "sample": desc}
     print(json.dumps(line), flush=True)
@@ -697,10 +770,28 @@ def run_kernel_only(args):
     torch.cuda.synchronize()
 
 
+def run_profile_steps(args):
+    import torch
+    from tracetransform_gb300.device import Engine, to_colmajor
+    img, angles, tfs, pfs = make_image(args.workload)
+    herm = WORKLOADS[args.workload][8]
+    eng = Engine(0)
+    dev = to_colmajor(torch.from_numpy(np.ascontiguousarray(img)).cuda())
+    for _ in range(args.profile_steps):
+        sino = eng.sinograms(dev, img.shape[0], img.shape[1], angles, tfs)
+        eng.zscore(eng.circus(sino, [(p, 0, -1) for p in pfs]))
+        if herm:
+            eng.zscore(eng.circus_orthonormal(sino, herm)[0])
+    torch.cuda.synchronize()
+
+
 def main():
     args = parse_args()
     if args.kernel_only:
         run_kernel_only(args)
+        return
+    if args.profile_steps:
+        run_profile_steps(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

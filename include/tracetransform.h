@@ -166,18 +166,21 @@ tt_status tt_circus_device(tt_plan *plan, const float *d_sino, int rows, int col
 
 /* Orthonormal (Hermite) circus functions of n_sino stacked rows x cols
  * sinograms (as tt_sinograms_device wrote them): each sinogram's nearest
- * orthonormal sinogram (c++/src/circus.cpp:68-102; here a parallel one-sided
- * Jacobi SVD in double on the device), then the Hermite P-functionals with
- * the center it yields (c++/src/transform.cpp:75-85).  pfuncs must all be
- * TT_P_HERMITE (their centers are ignored).  d_out: n_sino x n_p x cols;
- * centers (host, may be NULL): the n_sino centers used.  The reference runs
- * this only on images stretched to tt_ortho_size; here it takes sinograms of
- * any size, so a Hermite circus can sit beside P1-P3 of the regular
- * sinograms.  Synchronises the stream once (the aligned matrices' sizes
- * depend on the weighted medians) and then once per Jacobi sweep. */
+ * orthonormal sinogram (c++/src/circus.cpp:68-102; here a column-pivoting
+ * QR in double, a one-sided Jacobi SVD of R^T in float and Q applied on the
+ * device), then the Hermite P-functionals with the center it yields
+ * (c++/src/transform.cpp:75-85).  pfuncs must all be TT_P_HERMITE (their
+ * centers are ignored).  d_out: n_sino x n_p x cols; centers (host, may be
+ * NULL): the n_sino centers used.  The reference runs this only on images
+ * stretched to tt_ortho_size; here it takes sinograms of any size, so a
+ * Hermite circus can sit beside P1-P3 of the regular sinograms.
+ * Synchronises the stream once (the aligned matrices' sizes depend on the
+ * weighted medians) and then once per Jacobi sweep; *sweeps (may be NULL)
+ * receives the number of sweeps. */
 tt_status tt_circus_orthonormal_device(tt_plan *plan, const float *d_sino, int rows, int cols,
                                        int n_sino, const tt_pfunctional *pfuncs, int n_p,
-                                       float *d_out, int32_t *centers, void *stream);
+                                       float *d_out, int32_t *centers, int32_t *sweeps,
+                                       void *stream);
 
 /* Replaces nearest_orthonormal_sinogram(const Eigen::MatrixXf&, unsigned
  * int& new_center) (c++/src/circus.cpp:68-102) for one rows x cols host

@@ -99,7 +99,7 @@ def lib():
         "tt_circus_f64_device": [_P, _P, _int, _int, _int, ctypes.POINTER(PFunctionalC), _int,
                                  _P, _P],
         "tt_circus_orthonormal_device": [_P, _P, _int, _int, _int, ctypes.POINTER(PFunctionalC),
-                                         _int, _P, _I32, _P],
+                                         _int, _P, _I32, _I32, _P],
         "tt_nos": [_P, _F, _int, _int, _F, _I32, _I32],
     }
     for name, args in sig.items():

@@ -627,7 +627,8 @@ tt_status run_circus(tt_plan *p, const float *d_sino, int rows, int cols, int n_
 // sinogram, centers[s] the new Hermite centers.  One host synchronisation:
 // the aligned matrices' sizes depend on the weighted medians.
 tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sino,
-                  cudaStream_t st, std::vector<NosDesc> &desc, std::vector<int> &centers) {
+                  cudaStream_t st, std::vector<NosDesc> &desc, std::vector<int> &centers,
+                  int *sweeps = nullptr) {
     const int center = (int)std::floor((rows - 1) / 2.0);
     const size_t ncol = (size_t)cols * n_sino;
     TT_CHECK(p->ensure(p->nos_off, sizeof(int) * std::max<size_t>(ncol, 1)));
@@ -658,8 +659,12 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
     TT_CHECK(p->ensure(p->nos_a, sizeof(double) * a_elems));
     TT_CHECK(p->ensure(p->nos_desc, sizeof(NosDesc) * n_sino));
     TT_CHECK(p->ensure(p->nos, sizeof(float) * a_elems));
-    if (tt::nos_apply_smem(max_m) > 227 * 1024)
-        return fail(TT_ERR_UNSUPPORTED, "nearest orthonormal sinogram of %d rows is too tall", max_m);
+    if (max_m > tt::nos_max_rows() || tt::nos_apply_smem(max_m) > 227 * 1024)
+        return fail(TT_ERR_UNSUPPORTED,
+                    "nearest orthonormal sinogram of %d aligned rows exceeds %d", max_m,
+                    tt::nos_max_rows());
+    if (cols > 1024)
+        return fail(TT_ERR_UNSUPPORTED, "orthonormal circus of %d angles exceeds 1024", cols);
     // scratch: 3 double + 1 int vectors of n, 3 float n x n matrices, 1 float vector
     const size_t nv = ncol, nm = (size_t)cols * cols * n_sino;
     TT_CHECK(p->ensure(p->nos_work, sizeof(double) * 3 * nv + sizeof(int) * nv +
@@ -688,16 +693,23 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
     // each captured once per buffer set and size and replayed
     const std::vector<const void *> key = {A, d_desc, p->nos_work.p,
                                            (const void *)(size_t)cols,
-                                           (const void *)(size_t)n_sino};
+                                           (const void *)(size_t)n_sino,
+                                           (const void *)(size_t)(max_m <= 2048   ? 0
+                                                                  : max_m <= 4096 ? 1
+                                                                                  : 2)};
     TT_CHECK(p->graph(p->nos_factor_graph, key, [&](cudaStream_t cs) {
-        return tt::launch_nos_factor(A, d_desc, cols, n_sino, w, cs);
+        return tt::launch_nos_factor(A, d_desc, cols, n_sino, max_m, w, cs);
     }));
     TT_CHECK(p->graph(p->nos_sweep_graph, key, [&](cudaStream_t cs) {
         return tt::launch_nos_sweep(cols, n_sino, w, cs);
     }));
     TT_CUDA(cudaGraphLaunch(p->nos_factor_graph.exec, st));
     std::vector<unsigned> bits(n_sino);
+    if (sweeps)
+        *sweeps = 0;
     for (int sweep = 0; sweep < 40; sweep++) {
+        if (sweeps)
+            *sweeps = sweep + 1;
         TT_CUDA(cudaGraphLaunch(p->nos_sweep_graph.exec, st));
         TT_CUDA(cudaMemcpyAsync(bits.data(), w.off_bits, sizeof(unsigned) * n_sino,
                                 cudaMemcpyDeviceToHost, st));
@@ -1077,7 +1089,8 @@ tt_status tt_circus_device(tt_plan *plan, const float *d_sino, int rows, int col
 
 tt_status tt_circus_orthonormal_device(tt_plan *plan, const float *d_sino, int rows, int cols,
                                        int n_sino, const tt_pfunctional *pfuncs, int n_p,
-                                       float *d_out, int32_t *centers, void *stream) {
+                                       float *d_out, int32_t *centers, int32_t *sweeps,
+                                       void *stream) {
     tt_plan *p;
     TT_CHECK(resolve_plan(plan, &p));
     unsigned need;
@@ -1093,7 +1106,10 @@ tt_status tt_circus_orthonormal_device(tt_plan *plan, const float *d_sino, int r
     cudaStream_t st = pick_stream(p, stream);
     std::vector<NosDesc> desc;
     std::vector<int> c;
-    TT_CHECK(run_nos(p, d_sino, rows, cols, n_sino, st, desc, c));
+    int nsw = 0;
+    TT_CHECK(run_nos(p, d_sino, rows, cols, n_sino, st, desc, c, &nsw));
+    if (sweeps)
+        *sweeps = nsw;
     for (int s = 0; s < n_sino; s++) {
         const int32_t c32 = c[s];
         TT_CHECK(run_circus(p, (const float *)p->nos.p + desc[s].out_off, desc[s].m, cols, 1,

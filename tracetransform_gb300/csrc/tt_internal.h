@@ -116,8 +116,9 @@ cudaError_t launch_nos_align(const float *sino, int rows, int cols, int n_sino,
                              const NosDesc *desc, const int *offsets, double *A, size_t a_elems,
                              cudaStream_t st);
 // QR of the aligned matrices and X = R^T, V = I (2 n + 2 launches).
-cudaError_t launch_nos_factor(double *A, const NosDesc *desc, int n, int n_sino,
+cudaError_t launch_nos_factor(double *A, const NosDesc *desc, int n, int n_sino, int max_m,
                               const NosWork &w, cudaStream_t st);
+int nos_max_rows(); // aligned rows the QR kernels hold in registers
 // One Jacobi sweep on X (n - 1 + (n & 1) launches).
 cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, cudaStream_t st);
 float nos_sweep_done_bound();

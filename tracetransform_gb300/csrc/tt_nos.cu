@@ -110,10 +110,15 @@ qr_init_kernel(const double *__restrict__ A, const NosDesc *__restrict__ desc, i
     }
 }
 
+// Element slots: thread t holds rows t + kQrThreads u (u < K, K kQrThreads >=
+// m) of a column in registers, so a column is read once with all loads in
+// flight and written once.
+
 // Step k, one CTA per sinogram: pivot = the remaining column of largest
 // partial norm (lowest index on ties), swapped into place; then the
 // reflector H = I - tau v v^T with H A[k:, k] = (beta, 0, ...): beta on the
 // diagonal, v[1:] below it (v[0] = 1 implicit).
+template <int K>
 __global__ void __launch_bounds__(kQrThreads)
 qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n, int k,
                 double *__restrict__ norms, double *__restrict__ orig, int *__restrict__ perm,
@@ -122,8 +127,10 @@ qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n,
     __shared__ double bv[kQrThreads / 32];
     __shared__ int bi[kQrThreads / 32];
     __shared__ int piv;
+    __shared__ double s_alpha;
     const int s = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const NosDesc d = desc[s];
+    const int m = d.m;
     double *As = A + d.a_off;
     double *nr = norms + (size_t)s * n, *og = orig + (size_t)s * n;
     int *pm = perm + (size_t)s * n;
@@ -163,12 +170,24 @@ qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n,
     }
     __syncthreads();
     const int jp = piv;
+    double *x = As + (size_t)k * m;
+    double xv[K];
     if (jp != k) {
-        double *ca = As + (size_t)k * d.m, *cb = As + (size_t)jp * d.m;
-        for (int i = threadIdx.x; i < d.m; i += kQrThreads) {
-            const double t = ca[i];
-            ca[i] = cb[i];
-            cb[i] = t;
+        double *cb = As + (size_t)jp * m;
+        double ov[K];
+#pragma unroll
+        for (int u = 0; u < K; u++) {
+            const int i = threadIdx.x + kQrThreads * u;
+            xv[u] = i < m ? cb[i] : 0.0;
+            ov[u] = i < m ? x[i] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < K; u++) {
+            const int i = threadIdx.x + kQrThreads * u;
+            if (i < m) {
+                x[i] = xv[u];
+                cb[i] = ov[u];
+            }
         }
         if (threadIdx.x == 0) {
             double t = nr[k];
@@ -181,15 +200,25 @@ qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n,
             pm[k] = pm[jp];
             pm[jp] = q;
         }
+    } else {
+#pragma unroll
+        for (int u = 0; u < K; u++) {
+            const int i = threadIdx.x + kQrThreads * u;
+            xv[u] = i < m ? x[i] : 0.0;
+        }
     }
-    __syncthreads();
     // reflector of x = A[k:m, k]
-    double *x = As + (size_t)k * d.m;
     double xn = 0;
-    for (int i = k + 1 + threadIdx.x; i < d.m; i += kQrThreads)
-        xn += x[i] * x[i];
-    xn = block_sum<double, kQrThreads>(xn, red);
-    const double alpha = x[k];
+#pragma unroll
+    for (int u = 0; u < K; u++) {
+        const int i = threadIdx.x + kQrThreads * u;
+        if (i > k && i < m)
+            xn += xv[u] * xv[u];
+        if (i == k)
+            s_alpha = xv[u];
+    }
+    xn = block_sum<double, kQrThreads>(xn, red); // its barriers publish s_alpha
+    const double alpha = s_alpha;
     if (xn == 0) { // already (alpha, 0, ...): H = I
         if (threadIdx.x == 0)
             tau[(size_t)s * n + k] = 0;
@@ -197,17 +226,22 @@ qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n,
     }
     const double beta = -copysign(sqrt(alpha * alpha + xn), alpha);
     const double scale = 1 / (alpha - beta);
-    for (int i = k + 1 + threadIdx.x; i < d.m; i += kQrThreads)
-        x[i] *= scale;
-    if (threadIdx.x == 0) {
-        tau[(size_t)s * n + k] = (beta - alpha) / beta;
-        x[k] = beta;
+#pragma unroll
+    for (int u = 0; u < K; u++) {
+        const int i = threadIdx.x + kQrThreads * u;
+        if (i > k && i < m)
+            x[i] = xv[u] * scale;
+        if (i == k)
+            x[i] = beta;
     }
+    if (threadIdx.x == 0)
+        tau[(size_t)s * n + k] = (beta - alpha) / beta;
 }
 
 // Step k, one CTA per trailing column j = k + 1 + blockIdx.x: A[k:, j] -=
 // tau v (v . A[k:, j]), then the partial norm loses A[k, j]^2 -- recomputed
 // from the column when that leaves less than ~sqrt(eps) of the original.
+template <int K>
 __global__ void __launch_bounds__(kQrThreads)
 qr_update_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n, int k,
                  double *__restrict__ norms, double *__restrict__ orig,
@@ -215,30 +249,45 @@ qr_update_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n
     __shared__ double red[kQrThreads / 32];
     const int j = k + 1 + blockIdx.x, s = blockIdx.y;
     const NosDesc d = desc[s];
+    const int m = d.m;
     double *As = A + d.a_off;
-    const double *v = As + (size_t)k * d.m;
-    double *c = As + (size_t)j * d.m;
+    const double *v = As + (size_t)k * m;
+    double *c = As + (size_t)j * m;
     const double t = tau[(size_t)s * n + k];
-    if (t != 0) {
+    double vv[K], cv[K];
+#pragma unroll
+    for (int u = 0; u < K; u++) {
+        const int i = threadIdx.x + kQrThreads * u;
+        const bool in = i > k && i < m;
+        vv[u] = in ? v[i] : 0.0;
+        cv[u] = in ? c[i] : 0.0;
+    }
+    double ck = c[k];
+    if (t != 0) { // uniform
         double w = 0;
-        for (int i = k + 1 + threadIdx.x; i < d.m; i += kQrThreads)
-            w += v[i] * c[i];
-        w = block_sum<double, kQrThreads>(w, red) + c[k];
+#pragma unroll
+        for (int u = 0; u < K; u++)
+            w += vv[u] * cv[u];
+        w = block_sum<double, kQrThreads>(w, red) + ck;
         const double tw = t * w;
-        for (int i = k + 1 + threadIdx.x; i < d.m; i += kQrThreads)
-            c[i] -= tw * v[i];
-        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < K; u++) {
+            const int i = threadIdx.x + kQrThreads * u;
+            cv[u] -= tw * vv[u];
+            if (i > k && i < m)
+                c[i] = cv[u];
+        }
+        ck -= tw;
         if (threadIdx.x == 0)
-            c[k] -= tw;
-        __syncthreads();
+            c[k] = ck;
     }
     double *nr = norms + (size_t)s * n, *og = orig + (size_t)s * n;
-    const double a = c[k];
-    double n2 = nr[j] - a * a;
-    if (n2 <= 1.5e-8 * og[j]) { // uniform: every thread read the same values
+    double n2 = nr[j] - ck * ck;
+    if (n2 <= 1.5e-8 * og[j]) { // uniform: every thread holds the same values
         double r = 0;
-        for (int i = k + 1 + threadIdx.x; i < d.m; i += kQrThreads)
-            r += c[i] * c[i];
+#pragma unroll
+        for (int u = 0; u < K; u++)
+            r += cv[u] * cv[u];
         n2 = block_sum<double, kQrThreads>(r, red);
         if (threadIdx.x == 0)
             og[j] = n2;
@@ -276,6 +325,9 @@ constexpr float kJacTol = 1e-6f, kJacDone = 1e-5f;
 // k of round r.  Pairs of round r over players 0 .. P-1 (P = n_pad, even):
 // (P-1, r) and ((r + k) mod (P-1), (r - k) mod (P-1)), k = 1 .. P/2 - 1; a
 // player >= n is the odd case's bye.  The rotation is the cyclic Jacobi one.
+// Lane l holds elements l + 32 u (u < K, K >= n / 32) of both columns in
+// registers, so each column is loaded once with all loads in flight.
+template <int K>
 __global__ void __launch_bounds__(kJacThreads)
 rt_jacobi_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int n_pad, int round,
                        unsigned *__restrict__ off_bits) {
@@ -300,12 +352,19 @@ rt_jacobi_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int 
         return;
     const size_t nn = (size_t)n * n;
     float *xp = X + s * nn + (size_t)p * n, *xq = X + s * nn + (size_t)q * n;
+    float x[K], y[K];
+#pragma unroll
+    for (int u = 0; u < K; u++) {
+        const int i = lane + 32 * u;
+        x[u] = i < n ? xp[i] : 0.f;
+        y[u] = i < n ? xq[i] : 0.f;
+    }
     float al = 0.f, be = 0.f, ga = 0.f;
-    for (int i = lane; i < n; i += 32) {
-        const float x = xp[i], y = xq[i];
-        al = fmaf(x, x, al);
-        be = fmaf(y, y, be);
-        ga = fmaf(x, y, ga);
+#pragma unroll
+    for (int u = 0; u < K; u++) {
+        al = fmaf(x[u], x[u], al);
+        be = fmaf(y[u], y[u], be);
+        ga = fmaf(x[u], y[u], ga);
     }
     al = warp_sum(al);
     be = warp_sum(be);
@@ -318,16 +377,23 @@ rt_jacobi_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int 
     const float zeta = (be - al) / (2.f * ga);
     const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
     const float c = rsqrtf(1.f + t * t), sn = c * t;
-    for (int i = lane; i < n; i += 32) {
-        const float x = xp[i], y = xq[i];
-        xp[i] = c * x - sn * y;
-        xq[i] = sn * x + c * y;
-    }
     float *vp = V + s * nn + (size_t)p * n, *vq = V + s * nn + (size_t)q * n;
-    for (int i = lane; i < n; i += 32) {
-        const float x = vp[i], y = vq[i];
-        vp[i] = c * x - sn * y;
-        vq[i] = sn * x + c * y;
+    float a[K], b[K];
+#pragma unroll
+    for (int u = 0; u < K; u++) {
+        const int i = lane + 32 * u;
+        a[u] = i < n ? vp[i] : 0.f;
+        b[u] = i < n ? vq[i] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < K; u++) {
+        const int i = lane + 32 * u;
+        if (i < n) {
+            xp[i] = c * x[u] - sn * y[u];
+            xq[i] = sn * x[u] + c * y[u];
+            vp[i] = c * a[u] - sn * b[u];
+            vq[i] = sn * a[u] + c * b[u];
+        }
     }
 }
 
@@ -491,17 +557,31 @@ cudaError_t launch_nos_align(const float *sino, int rows, int cols, int n_sino,
     return cudaGetLastError();
 }
 
-cudaError_t launch_nos_factor(double *A, const NosDesc *desc, int n, int n_sino,
-                              const NosWork &w, cudaStream_t st) {
-    qr_init_kernel<<<dim3(n, n_sino), kQrThreads, 0, st>>>(A, desc, n, w.norms, w.orig, w.perm);
+template <int K>
+static void qr_steps(double *A, const NosDesc *desc, int n, int n_sino, const NosWork &w,
+                     cudaStream_t st) {
     for (int k = 0; k < n; k++) {
-        qr_pivot_kernel<<<n_sino, kQrThreads, 0, st>>>(A, desc, n, k, w.norms, w.orig, w.perm,
-                                                       w.tau);
+        qr_pivot_kernel<K><<<n_sino, kQrThreads, 0, st>>>(A, desc, n, k, w.norms, w.orig, w.perm,
+                                                          w.tau);
         if (k + 1 < n)
-            qr_update_kernel<<<dim3(n - k - 1, n_sino), kQrThreads, 0, st>>>(A, desc, n, k,
-                                                                            w.norms, w.orig,
-                                                                            w.tau);
+            qr_update_kernel<K><<<dim3(n - k - 1, n_sino), kQrThreads, 0, st>>>(
+                A, desc, n, k, w.norms, w.orig, w.tau);
     }
+}
+
+int nos_max_rows() { return 32 * kQrThreads; }
+
+cudaError_t launch_nos_factor(double *A, const NosDesc *desc, int n, int n_sino, int max_m,
+                              const NosWork &w, cudaStream_t st) {
+    if (max_m > nos_max_rows())
+        return cudaErrorInvalidValue;
+    qr_init_kernel<<<dim3(n, n_sino), kQrThreads, 0, st>>>(A, desc, n, w.norms, w.orig, w.perm);
+    if (max_m <= 8 * kQrThreads)
+        qr_steps<8>(A, desc, n, n_sino, w, st);
+    else if (max_m <= 16 * kQrThreads)
+        qr_steps<16>(A, desc, n, n_sino, w, st);
+    else
+        qr_steps<32>(A, desc, n, n_sino, w, st);
     const long long nn = (long long)n * n;
     nos_rt_kernel<<<dim3((unsigned)((nn + 255) / 256), n_sino), 256, 0, st>>>(A, desc, n, w.X,
                                                                               w.V);
@@ -514,8 +594,15 @@ cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, cudaStream_t s
     if (e != cudaSuccess)
         return e;
     const dim3 grid((n_pad / 2 + kJacPairs - 1) / kJacPairs, n_sino);
+    auto kern = n <= 256 ? rt_jacobi_round_kernel<8>
+              : n <= 512 ? rt_jacobi_round_kernel<16>
+              : n <= 768 ? rt_jacobi_round_kernel<24>
+              : n <= 1024 ? rt_jacobi_round_kernel<32>
+              : nullptr;
+    if (!kern)
+        return cudaErrorInvalidValue; // more than 1024 angles
     for (int r = 0; r < n_pad - 1; r++)
-        rt_jacobi_round_kernel<<<grid, kJacThreads, 0, st>>>(w.X, w.V, n, n_pad, r, w.off_bits);
+        kern<<<grid, kJacThreads, 0, st>>>(w.X, w.V, n, n_pad, r, w.off_bits);
     return cudaGetLastError();
 }
 

@@ -108,15 +108,18 @@ class Engine:
     def circus_orthonormal(self, sino: torch.Tensor, orders: Sequence[int],
                            out: Optional[torch.Tensor] = None):
         """Hermite circus of each sinogram's nearest orthonormal sinogram:
-        (nS, A, N) -> ((nS, len(orders), A), centers)."""
+        (nS, A, N) -> ((nS, len(orders), A), centers); self.last_sweeps holds
+        the Jacobi sweeps the call took."""
         ns, a, n = sino.shape
         if out is None:
             out = torch.empty((ns, len(orders), a), dtype=torch.float32, device=sino.device)
         centers = np.zeros(max(ns, 1), np.int32)
+        sweeps = ctypes.c_int32(0)
         check(lib().tt_circus_orthonormal_device(
             self.plan.handle, _ptr(sino), n, a, ns, _pf([(0, int(o), -1) for o in orders]),
             len(orders), _ptr(out), centers.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
-            _stream(sino)))
+            ctypes.byref(sweeps), _stream(sino)))
+        self.last_sweeps = sweeps.value
         return out, centers[:ns]
 
     def zscore(self, circus: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
