@@ -773,6 +773,34 @@ def run_kernel_only(args):
 def run_profile_steps(args):
     import torch
     from tracetransform_gb300.device import Engine, to_colmajor
+    if args.workload == "batch512":
+        imgs, steps = make_batch()
+        bufs = [np.ascontiguousarray(im.ravel(order="F")) for im in imgs]
+        offsets = np.zeros(len(bufs), np.int64)
+        offsets[1:] = np.cumsum([b.size for b in bufs])[:-1]
+        flat = torch.from_numpy(np.concatenate(bufs)).cuda()
+        eng = Engine(0)
+        for _ in range(args.profile_steps):
+            eng.transform_batch(flat, offsets, [im.shape[0] for im in imgs],
+                                [im.shape[1] for im in imgs], steps, BATCH_T,
+                                [(p, -1, -1) for p in BATCH_P])
+        torch.cuda.synchronize()
+        return
+    if args.workload == "grad64":
+        import tracetransform_gb300 as tt
+        from tracetransform_gb300 import autograd as tta
+        angles = tt.angles_from_step(1)
+        imgs = torch.from_numpy(make_grad_batch(10)).cuda()
+        with torch.no_grad():
+            target = tta.circus(torch.from_numpy(make_grad_batch(5000)).cuda(), angles, GRAD_T,
+                                GRAD_P)
+        scale = target.abs().mean(dim=(0, 3), keepdim=True)
+        for _ in range(args.profile_steps):
+            x = imgs.clone().requires_grad_(True)
+            torch.nn.functional.mse_loss(tta.circus(x, angles, GRAD_T, GRAD_P) / scale,
+                                         target / scale).backward()
+        torch.cuda.synchronize()
+        return
     img, angles, tfs, pfs = make_image(args.workload)
     herm = WORKLOADS[args.workload][8]
     eng = Engine(0)
