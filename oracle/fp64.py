@@ -116,13 +116,20 @@ def tfunctionals(img: np.ndarray, tfuncs) -> np.ndarray:
     return np.stack(out)
 
 
-def sinograms(padded: np.ndarray, angles_deg, tfuncs) -> np.ndarray:
-    """(nT, N, A) sinograms in double."""
+def sinograms(padded: np.ndarray, angles_deg, tfuncs, with_medians: bool = False):
+    """(nT, N, A) sinograms in double; with_medians also returns the
+    weighted-median rows of x and of sqrt(x) per (column, angle), (N, A) each."""
     n = padded.shape[0]
     out = np.zeros((len(tfuncs), n, len(angles_deg)))
+    m1 = np.zeros((n, len(angles_deg)), np.int64)
+    m2 = np.zeros_like(m1)
     for a, ang in enumerate(angles_deg):
-        out[:, :, a] = tfunctionals(rotate(padded, ang), tfuncs)
-    return out
+        img = rotate(padded, ang)
+        out[:, :, a] = tfunctionals(img, tfuncs)
+        if with_medians:
+            m1[:, a] = weighted_median(img)
+            m2[:, a] = weighted_median(np.sqrt(np.maximum(img, 0)))
+    return (out, m1, m2) if with_medians else out
 
 
 def circus(sino: np.ndarray, pfuncs) -> np.ndarray:

@@ -669,7 +669,7 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
     const size_t nv = ncol, nm = (size_t)cols * cols * n_sino;
     TT_CHECK(p->ensure(p->nos_work, sizeof(double) * 3 * nv + sizeof(int) * nv +
                                         sizeof(float) * (3 * nm + nv) + sizeof(unsigned) * n_sino +
-                                        64));
+                                        sizeof(float) * n_sino + 64));
     tt::NosWork w;
     {
         char *q = (char *)p->nos_work.p;
@@ -682,6 +682,7 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
         w.inv = w.P + nm;
         w.perm = (int *)(w.inv + nv);
         w.off_bits = (unsigned *)(w.perm + nv);
+        w.tiny = (float *)(w.off_bits + n_sino);
     }
     TT_CUDA(cudaMemcpyAsync(p->nos_desc.p, desc.data(), sizeof(NosDesc) * n_sino,
                             cudaMemcpyHostToDevice, st));
@@ -704,7 +705,12 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
         return tt::launch_nos_sweep(cols, n_sino, w, cs);
     }));
     TT_CUDA(cudaGraphLaunch(p->nos_factor_graph.exec, st));
+    // Stop when the largest rotated pair's cosine is below the done bound, or
+    // when it has stopped falling (quadratic convergence takes it down by
+    // orders of magnitude per sweep; a plateau below 1e-3 is the float
+    // rounding floor of the rotated columns, which grows with sqrt(A)).
     std::vector<unsigned> bits(n_sino);
+    float prev = 1.f;
     if (sweeps)
         *sweeps = 0;
     for (int sweep = 0; sweep < 40; sweep++) {
@@ -720,8 +726,9 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
             std::memcpy(&v, &b, sizeof v);
             worst = std::max(worst, v);
         }
-        if (worst < tt::nos_sweep_done_bound())
+        if (worst < tt::nos_sweep_done_bound() || (worst < 1e-3f && worst > 0.25f * prev))
             break;
+        prev = worst;
     }
     TT_CUDA(tt::launch_nos_assemble(A, d_desc, cols, n_sino, max_m, w, (float *)p->nos.p, st));
     return TT_OK;

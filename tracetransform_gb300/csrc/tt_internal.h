@@ -109,6 +109,7 @@ struct NosWork {
     float *X, *V, *P;           // n_sino x n x n each (R^T, Jacobi V, polar(R))
     float *inv;                 // n_sino x n
     unsigned *off_bits;         // n_sino: largest rotated |cos| of a sweep (float bits)
+    float *tiny;                // n_sino: squared column norm below which a direction is null
 };
 cudaError_t launch_nos_offsets(const float *sino, int rows, int cols, int n_sino, int center,
                                int *offsets, cudaStream_t st);

@@ -298,16 +298,28 @@ qr_update_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n
 
 // ---- one-sided Jacobi on X = R^T (float) ----------------------------------
 
-// X[i + j n] = R[j, i] (upper triangle of the QR result), V = I.
+// Directions of R whose norm is below kNullRel |R[0, 0]| (|R[0, 0]| is the
+// largest column norm of the aligned matrix) are below the double precision
+// of the input: they take no rotations and no part in U, as the oracle
+// treats exactly-zero directions.
+constexpr double kNullRel = 1e-15;
+
+// X[i + j n] = R[j, i] (upper triangle of the QR result), V = I, and the
+// null-direction bound tiny[s] = (kNullRel R[0, 0])^2.
 // grid (ceil(n * n / 256), n_sino).
 __global__ void nos_rt_kernel(const double *__restrict__ A, const NosDesc *__restrict__ desc,
-                              int n, float *__restrict__ X, float *__restrict__ V) {
+                              int n, float *__restrict__ X, float *__restrict__ V,
+                              float *__restrict__ tiny) {
     const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long nn = (long long)n * n;
     if (e >= nn)
         return;
     const int s = blockIdx.y, i = (int)(e % n), j = (int)(e / n);
     const NosDesc d = desc[s];
+    if (e == 0) {
+        const double r = kNullRel * A[d.a_off];
+        tiny[s] = (float)(r * r);
+    }
     X[s * nn + e] = j <= i ? (float)A[d.a_off + j + (size_t)i * d.m] : 0.f;
     V[s * nn + e] = i == j ? 1.f : 0.f;
 }
@@ -330,7 +342,7 @@ constexpr float kJacTol = 1e-6f, kJacDone = 1e-5f;
 template <int K>
 __global__ void __launch_bounds__(kJacThreads)
 rt_jacobi_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int n_pad, int round,
-                       unsigned *__restrict__ off_bits) {
+                       unsigned *__restrict__ off_bits, const float *__restrict__ tiny) {
     const int lane = threadIdx.x & 31;
     const int k = blockIdx.x * kJacPairs + (threadIdx.x >> 5), s = blockIdx.y, P1 = n_pad - 1;
     if (k >= n_pad / 2)
@@ -369,9 +381,9 @@ rt_jacobi_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int 
     al = warp_sum(al);
     be = warp_sum(be);
     ga = warp_sum(ga);
-    const float nrm = sqrtf(al) * sqrtf(be);
-    if (ga == 0.f || fabsf(ga) <= kJacTol * nrm)
-        return;
+    const float nrm = sqrtf(al) * sqrtf(be), tn = tiny[s];
+    if (!(al > tn) || !(be > tn) || ga == 0.f || fabsf(ga) <= kJacTol * nrm)
+        return; // a null direction, or already orthogonal
     if (lane == 0)
         atomicMax(off_bits + s, __float_as_uint(fabsf(ga) / nrm));
     const float zeta = (be - al) / (2.f * ga);
@@ -399,9 +411,10 @@ rt_jacobi_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int 
 
 // ---- assembly ---------------------------------------------------------------
 
-// 1 / |x_k| per column of the converged X (0 for a zero column).  grid
+// 1 / |x_k| per column of the converged X (0 for a null direction).  grid
 // (ceil(n / 4), n_sino), one warp per column.
-__global__ void rt_invnorm_kernel(const float *__restrict__ X, int n, float *__restrict__ inv) {
+__global__ void rt_invnorm_kernel(const float *__restrict__ X, int n, const float *__restrict__ tiny,
+                                  float *__restrict__ inv) {
     const int k = blockIdx.x * 4 + (threadIdx.x >> 5), s = blockIdx.y, lane = threadIdx.x & 31;
     if (k >= n)
         return;
@@ -411,7 +424,7 @@ __global__ void rt_invnorm_kernel(const float *__restrict__ X, int n, float *__r
         v = fmaf(x[i], x[i], v);
     v = warp_sum(v);
     if (lane == 0)
-        inv[(size_t)s * n + k] = v > 0.f ? rsqrtf(v) : 0.f;
+        inv[(size_t)s * n + k] = v > tiny[s] ? rsqrtf(v) : 0.f;
 }
 
 // X[:, k] *= inv[k]: the columns of X become U_X.  grid (ceil(n n / 256), n_sino).
@@ -584,7 +597,7 @@ cudaError_t launch_nos_factor(double *A, const NosDesc *desc, int n, int n_sino,
         qr_steps<32>(A, desc, n, n_sino, w, st);
     const long long nn = (long long)n * n;
     nos_rt_kernel<<<dim3((unsigned)((nn + 255) / 256), n_sino), 256, 0, st>>>(A, desc, n, w.X,
-                                                                              w.V);
+                                                                              w.V, w.tiny);
     return cudaGetLastError();
 }
 
@@ -602,7 +615,7 @@ cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, cudaStream_t s
     if (!kern)
         return cudaErrorInvalidValue; // more than 1024 angles
     for (int r = 0; r < n_pad - 1; r++)
-        kern<<<grid, kJacThreads, 0, st>>>(w.X, w.V, n, n_pad, r, w.off_bits);
+        kern<<<grid, kJacThreads, 0, st>>>(w.X, w.V, n, n_pad, r, w.off_bits, w.tiny);
     return cudaGetLastError();
 }
 
@@ -614,7 +627,7 @@ cudaError_t launch_nos_assemble(const double *A, const NosDesc *desc, int n, int
                                 int max_m, const NosWork &w, float *out, cudaStream_t st) {
     const long long nn = (long long)n * n;
     const dim3 ge((unsigned)((nn + 255) / 256), n_sino), gt((n + 31) / 32, (n + 31) / 32, n_sino);
-    rt_invnorm_kernel<<<dim3((n + 3) / 4, n_sino), 128, 0, st>>>(w.X, n, w.inv);
+    rt_invnorm_kernel<<<dim3((n + 3) / 4, n_sino), 128, 0, st>>>(w.X, n, w.tiny, w.inv);
     rt_scale_kernel<<<ge, 256, 0, st>>>(w.X, w.inv, n);
     // P = V U^T, then one Newton-Schulz step P <- P (3 I - P^T P) / 2 (in the
     // V buffer), which removes the symmetric part of P's distance from
