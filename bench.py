@@ -320,12 +320,13 @@ def run_engine(args, world, rank, local_rank):
     ms = max_over_ranks(ms, world)
     # sinograms, circus, z-score; with the Hermite circus: weighted-median
     # offsets, alignment, QR (qr_init, n pivot + n - 1 update launches, R^T),
-    # the sweeps (n - 1 + (n & 1) rounds each), assembly (6), one circus
+    # the sweeps (one launch per block round), assembly (6), one circus
     # launch per sinogram and a z-score
     launches = 3
     if herm:
-        n_pad = A + (A & 1)
-        launches += 2 + (2 * A + 1) + eng.last_sweeps * (n_pad - 1) + 6 + len(tfs) + 1
+        nb = (A + 7) // 8  # 8-column blocks, nbp - 1 block rounds per sweep
+        nbp = nb + (nb & 1)
+        launches += 2 + (2 * A + 1) + eng.last_sweeps * (nbp - 1) + 6 + len(tfs) + 1
     launches *= args.steps
 
     # end to end through the C ABI drop-in, pinned host buffers

@@ -18,9 +18,10 @@
 //                 tau, partial column norms downdated and recomputed when
 //                 cancellation sets in)
 //   Jacobi        one-sided Jacobi on X = R^T in float (R^T of a pivoted QR is
-//                 graded, so float rotations keep relative accuracy): round-
-//                 robin rounds of A/2 disjoint column pairs, one warp per
-//                 pair, V accumulated; X V = U_X S, so polar(R) = V U_X^T
+//                 graded, so float rotations keep relative accuracy), two-
+//                 level: round-robin rounds of column-block pairs, each pair
+//                 swept in one CTA's shared memory, V accumulated;
+//                 X V = U_X S, so polar(R) = V U_X^T
 //   assemble      P = V U_X^T (float) with one Newton-Schulz step to clean
 //                 its orthogonality, then polar(A P) = Q [P; 0] applied
 //                 reflector by reflector per group of columns in shared
@@ -324,30 +325,24 @@ __global__ void nos_rt_kernel(const double *__restrict__ A, const NosDesc *__res
     V[s * nn + e] = i == j ? 1.f : 0.f;
 }
 
-constexpr int kJacThreads = 128;
-constexpr int kJacPairs = kJacThreads / 32; // one warp per column pair
-
 // A pair is rotated when |x_p . x_q| > kJacTol |x_p| |x_q| -- a few times the
 // rounding of a float dot product over n terms split across a warp -- and a
 // sweep that rotates none (or whose largest rotated pair is below
 // kJacDone) ends the iteration.
 constexpr float kJacTol = 1e-6f, kJacDone = 1e-5f;
 
-// grid (ceil(n_pad / 2 / kJacPairs), n_sino); warp k of the grid takes pair
-// k of round r.  Pairs of round r over players 0 .. P-1 (P = n_pad, even):
-// (P-1, r) and ((r + k) mod (P-1), (r - k) mod (P-1)), k = 1 .. P/2 - 1; a
-// player >= n is the odd case's bye.  The rotation is the cyclic Jacobi one.
-// Lane l holds elements l + 32 u (u < K, K >= n / 32) of both columns in
-// registers, so each column is loaded once with all loads in flight.
-template <int K>
-__global__ void __launch_bounds__(kJacThreads)
-rt_jacobi_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int n_pad, int round,
-                       unsigned *__restrict__ off_bits, const float *__restrict__ tiny) {
-    const int lane = threadIdx.x & 31;
-    const int k = blockIdx.x * kJacPairs + (threadIdx.x >> 5), s = blockIdx.y, P1 = n_pad - 1;
-    if (k >= n_pad / 2)
-        return;
-    int p, q;
+// Two-level (block) Jacobi.  The n columns form blocks of kBJ; a sweep is a
+// round-robin tournament of the blocks (nbp - 1 rounds for nbp blocks, a bye
+// when odd), and in each outer round a CTA copies its block pair -- 2 kBJ
+// columns of X and of V -- into shared memory and runs one inner sweep over
+// all their pairs (2 kBJ - 1 inner rounds of kBJ disjoint pairs, one warp per
+// pair, __syncthreads between rounds) before writing them back.  A sweep is
+// nbp - 1 launches instead of n - 1, and the rotations are those of the
+// cyclic Jacobi method.
+constexpr int kBJ = 8, kBCols = 2 * kBJ, kBThreads = 32 * kBJ;
+
+__device__ __forceinline__ void round_robin(int players, int round, int k, int &p, int &q) {
+    const int P1 = players - 1;
     if (k == 0) {
         p = P1;
         q = round;
@@ -360,51 +355,108 @@ rt_jacobi_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int 
         p = q;
         q = t;
     }
-    if (q >= n)
-        return;
+}
+
+// grid (nbp / 2, n_sino), kBThreads threads, dynamic shared memory 2 kBCols n
+// floats.  Lane l holds elements l + 32 u (u < K, 32 K >= n) of a column.
+template <int K>
+__global__ void __launch_bounds__(kBThreads)
+rt_block_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int nbp, int round,
+                      unsigned *__restrict__ off_bits, const float *__restrict__ tiny) {
+    extern __shared__ __align__(16) float bsm[];
+    float *Xl = bsm, *Vl = bsm + (size_t)kBCols * n;
+    const int s = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nb = (n + kBJ - 1) / kBJ;
+    int bp, bq;
+    round_robin(nbp, round, blockIdx.x, bp, bq);
+    if (bq >= nb)
+        return; // the bye
     const size_t nn = (size_t)n * n;
-    float *xp = X + s * nn + (size_t)p * n, *xq = X + s * nn + (size_t)q * n;
-    float x[K], y[K];
+    float *Xg = X + s * nn, *Vg = V + s * nn;
+    // warp w stages local columns w (block bp) and w + kBJ (block bq) of X and
+    // V, all 4 K loads of a lane in flight at once
+    const int c0 = bp * kBJ + warp, c1 = bq * kBJ + warp;
+    {
+        float a[K], b[K], c[K], d[K];
 #pragma unroll
-    for (int u = 0; u < K; u++) {
-        const int i = lane + 32 * u;
-        x[u] = i < n ? xp[i] : 0.f;
-        y[u] = i < n ? xq[i] : 0.f;
-    }
-    float al = 0.f, be = 0.f, ga = 0.f;
+        for (int u = 0; u < K; u++) {
+            const int i = lane + 32 * u;
+            a[u] = (i < n && c0 < n) ? Xg[(size_t)c0 * n + i] : 0.f;
+            b[u] = (i < n && c1 < n) ? Xg[(size_t)c1 * n + i] : 0.f;
+            c[u] = (i < n && c0 < n) ? Vg[(size_t)c0 * n + i] : 0.f;
+            d[u] = (i < n && c1 < n) ? Vg[(size_t)c1 * n + i] : 0.f;
+        }
 #pragma unroll
-    for (int u = 0; u < K; u++) {
-        al = fmaf(x[u], x[u], al);
-        be = fmaf(y[u], y[u], be);
-        ga = fmaf(x[u], y[u], ga);
+        for (int u = 0; u < K; u++) {
+            const int i = lane + 32 * u;
+            if (i < n) {
+                Xl[(size_t)warp * n + i] = a[u];
+                Xl[(size_t)(warp + kBJ) * n + i] = b[u];
+                Vl[(size_t)warp * n + i] = c[u];
+                Vl[(size_t)(warp + kBJ) * n + i] = d[u];
+            }
+        }
     }
-    al = warp_sum(al);
-    be = warp_sum(be);
-    ga = warp_sum(ga);
-    const float nrm = sqrtf(al) * sqrtf(be), tn = tiny[s];
-    if (!(al > tn) || !(be > tn) || ga == 0.f || fabsf(ga) <= kJacTol * nrm)
-        return; // a null direction, or already orthogonal
-    if (lane == 0)
-        atomicMax(off_bits + s, __float_as_uint(fabsf(ga) / nrm));
-    const float zeta = (be - al) / (2.f * ga);
-    const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-    const float c = rsqrtf(1.f + t * t), sn = c * t;
-    float *vp = V + s * nn + (size_t)p * n, *vq = V + s * nn + (size_t)q * n;
-    float a[K], b[K];
+    __syncthreads();
+    const float tn = tiny[s];
+    float wmax = 0.f;
+    for (int ir = 0; ir < kBCols - 1; ir++) {
+        int p, q;
+        round_robin(kBCols, ir, warp, p, q);
+        float *xp = Xl + (size_t)p * n, *xq = Xl + (size_t)q * n;
+        float x[K], y[K];
 #pragma unroll
-    for (int u = 0; u < K; u++) {
-        const int i = lane + 32 * u;
-        a[u] = i < n ? vp[i] : 0.f;
-        b[u] = i < n ? vq[i] : 0.f;
+        for (int u = 0; u < K; u++) {
+            const int i = lane + 32 * u;
+            x[u] = i < n ? xp[i] : 0.f;
+            y[u] = i < n ? xq[i] : 0.f;
+        }
+        float al = 0.f, be = 0.f, ga = 0.f;
+#pragma unroll
+        for (int u = 0; u < K; u++) {
+            al = fmaf(x[u], x[u], al);
+            be = fmaf(y[u], y[u], be);
+            ga = fmaf(x[u], y[u], ga);
+        }
+        al = warp_sum(al);
+        be = warp_sum(be);
+        ga = warp_sum(ga);
+        const float nrm = sqrtf(al) * sqrtf(be);
+        // a null direction (or an empty slot past n), or already orthogonal
+        if (al > tn && be > tn && ga != 0.f && fabsf(ga) > kJacTol * nrm) {
+            wmax = fmaxf(wmax, fabsf(ga) / nrm);
+            const float zeta = (be - al) / (2.f * ga);
+            const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+            const float c = rsqrtf(1.f + t * t), sn = c * t;
+            float *vp = Vl + (size_t)p * n, *vq = Vl + (size_t)q * n;
+#pragma unroll
+            for (int u = 0; u < K; u++) {
+                const int i = lane + 32 * u;
+                if (i < n) {
+                    const float a = vp[i], b = vq[i];
+                    xp[i] = c * x[u] - sn * y[u];
+                    xq[i] = sn * x[u] + c * y[u];
+                    vp[i] = c * a - sn * b;
+                    vq[i] = sn * a + c * b;
+                }
+            }
+        }
+        __syncthreads();
     }
+    if (lane == 0 && wmax > 0.f)
+        atomicMax(off_bits + s, __float_as_uint(wmax));
 #pragma unroll
     for (int u = 0; u < K; u++) {
         const int i = lane + 32 * u;
         if (i < n) {
-            xp[i] = c * x[u] - sn * y[u];
-            xq[i] = sn * x[u] + c * y[u];
-            vp[i] = c * a[u] - sn * b[u];
-            vq[i] = sn * a[u] + c * b[u];
+            if (c0 < n) {
+                Xg[(size_t)c0 * n + i] = Xl[(size_t)warp * n + i];
+                Vg[(size_t)c0 * n + i] = Vl[(size_t)warp * n + i];
+            }
+            if (c1 < n) {
+                Xg[(size_t)c1 * n + i] = Xl[(size_t)(warp + kBJ) * n + i];
+                Vg[(size_t)c1 * n + i] = Vl[(size_t)(warp + kBJ) * n + i];
+            }
         }
     }
 }
@@ -601,22 +653,41 @@ cudaError_t launch_nos_factor(double *A, const NosDesc *desc, int n, int n_sino,
     return cudaGetLastError();
 }
 
+template <int K> static cudaError_t block_rounds(int n, int n_sino, const NosWork &w,
+                                                 cudaStream_t st) {
+    const int nb = (n + kBJ - 1) / kBJ, nbp = nb + (nb & 1);
+    const size_t smem = sizeof(float) * 2 * kBCols * (size_t)n;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(rt_block_round_kernel<K>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)dynamic_smem_limit(
+                                                 (const void *)rt_block_round_kernel<K>));
+        if (e != cudaSuccess)
+            return e;
+        attr = true;
+    }
+    if (smem > dynamic_smem_limit((const void *)rt_block_round_kernel<K>))
+        return cudaErrorInvalidValue;
+    for (int r = 0; r < nbp - 1; r++)
+        rt_block_round_kernel<K><<<dim3(nbp / 2, n_sino), kBThreads, smem, st>>>(
+            w.X, w.V, n, nbp, r, w.off_bits, w.tiny);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, cudaStream_t st) {
-    const int n_pad = n + (n & 1);
     cudaError_t e = cudaMemsetAsync(w.off_bits, 0, sizeof(unsigned) * n_sino, st);
     if (e != cudaSuccess)
         return e;
-    const dim3 grid((n_pad / 2 + kJacPairs - 1) / kJacPairs, n_sino);
-    auto kern = n <= 256 ? rt_jacobi_round_kernel<8>
-              : n <= 512 ? rt_jacobi_round_kernel<16>
-              : n <= 768 ? rt_jacobi_round_kernel<24>
-              : n <= 1024 ? rt_jacobi_round_kernel<32>
-              : nullptr;
-    if (!kern)
-        return cudaErrorInvalidValue; // more than 1024 angles
-    for (int r = 0; r < n_pad - 1; r++)
-        kern<<<grid, kJacThreads, 0, st>>>(w.X, w.V, n, n_pad, r, w.off_bits, w.tiny);
-    return cudaGetLastError();
+    if (n <= 256)
+        return block_rounds<8>(n, n_sino, w, st);
+    if (n <= 512)
+        return block_rounds<16>(n, n_sino, w, st);
+    if (n <= 768)
+        return block_rounds<24>(n, n_sino, w, st);
+    if (n <= 1024)
+        return block_rounds<32>(n, n_sino, w, st);
+    return cudaErrorInvalidValue; // more than 1024 angles
 }
 
 float nos_sweep_done_bound() { return kJacDone; }
