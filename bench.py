@@ -6,8 +6,13 @@
 
 A step is one pass of the hot path over one image: the fused rotate +
 T-functional kernel (all sinograms), the P-functional kernel (all circus
-functions) and the z-score kernel.  The metric is sinograms per second
+functions) and the z-score kernel, plus -- for the 1024^2 and 4096^2
+workloads -- the orthonormal Hermite circus (nearest orthonormal sinogram of
+every sinogram, Hermite orders 1-5).  The metric is sinograms per second
 (sinograms = images x T-functionals).  Prints one JSON line (rank 0).
+Other workloads: batch512 (512 uneven images through the batched engine
+against the plain per-image path) and grad64 (forward + backward of an MSE
+loss over 64 images through tracetransform_gb300.autograd).
 
 * value      device-resident throughput: the image already in HBM, CUDA events
              around each step, L2 flushed (256 MiB write) between steps
