@@ -421,13 +421,24 @@ rt_block_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int n
         al = warp_sum(al);
         be = warp_sum(be);
         ga = warp_sum(ga);
-        const float nrm = sqrtf(al) * sqrtf(be);
+        // cos of the pair = |ga| / (|x_p| |x_q|); rotation parameters from
+        // the (2-ulp) hardware reciprocal square root: the rotation only has
+        // to be orthogonal (c^2 + s^2 = 1 to float precision), not exact
+        const float cosv = fabsf(ga) * (rsqrtf(al) * rsqrtf(be));
         // a null direction (or an empty slot past n), or already orthogonal
-        if (al > tn && be > tn && ga != 0.f && fabsf(ga) > kJacTol * nrm) {
-            wmax = fmaxf(wmax, fabsf(ga) / nrm);
-            const float zeta = (be - al) / (2.f * ga);
-            const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-            const float c = rsqrtf(1.f + t * t), sn = c * t;
+        if (al > tn && be > tn && ga != 0.f && cosv > kJacTol) {
+            wmax = fmaxf(wmax, cosv);
+            const float zeta = __fdividef(be - al, 2.f * ga);
+            const float az = fabsf(zeta);
+            float t;
+            if (az < 1e15f) {
+                const float z2 = fmaf(zeta, zeta, 1.f);
+                t = __fdividef(1.f, az + z2 * rsqrtf(z2));
+            } else {
+                t = __fdividef(0.5f, az);
+            }
+            t = zeta >= 0.f ? t : -t;
+            const float c = rsqrtf(fmaf(t, t, 1.f)), sn = c * t;
             float *vp = Vl + (size_t)p * n, *vq = Vl + (size_t)q * n;
 #pragma unroll
             for (int u = 0; u < K; u++) {
@@ -681,6 +692,8 @@ cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, cudaStream_t s
         return e;
     if (n <= 256)
         return block_rounds<8>(n, n_sino, w, st);
+    if (n <= 384)
+        return block_rounds<12>(n, n_sino, w, st);
     if (n <= 512)
         return block_rounds<16>(n, n_sino, w, st);
     if (n <= 768)
