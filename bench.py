@@ -417,15 +417,66 @@ def run_engine(args, world, rank, local_rank):
     }
     if herm:
         line["hermite_sweeps"] = eng.last_sweeps
+    line["images_per_s"] = line["value"] / len(tfs)
+    if args.workload in BACKWARD_TIMED:
+        line["backward"] = backward_timing(eng, img_dev, rows, cols, angles,
+                                           max(2, min(args.steps, 3)))
     if not args.no_cpu_baseline:
         per, desc, cores = cpu_sample(img, angles, tfs, pfs, args.cpu_seconds)
+        per1, desc1, _ = cpu_sample(img, angles, tfs, pfs, args.cpu_seconds, threads=1)
         if herm:
             hs, hd = cpu_hermite_seconds(img, angles, tfs, herm)
             per += hs
+            per1 += hs
             desc += "; plus the " + hd
+            desc1 += "; plus the " + hd
         line["cpu_baseline"] = {"value": len(tfs) / per, "unit": "sinograms/s", "cores": cores,
                                 "kind": "port", "sample": desc}
+        line["cpu_baseline_1thread"] = {"value": len(tfs) / per1, "unit": "sinograms/s",
+                                        "cores": 1, "kind": "port", "sample": desc1}
     print(json.dumps(line), flush=True)
+
+
+BACKWARD_TIMED = {"single4096"}
+
+
+def backward_timing(eng, img_dev, rows, cols, angles, steps):
+    """Forward (T0-T2 sinograms with their medians, P1/P3 circus) and backward
+    (P-stage adjoint, then the rotation adjoint with the rotations
+    recomputed) of the differentiable functionals on the workload's image,
+    timed with CUDA events on the launching stream."""
+    import torch
+    tf, pf = [0, 1, 2], [(1, -1, -1), (3, -1, -1)]
+    stream = torch.cuda.current_stream()
+
+    def fwd():
+        sino, med = eng.sinograms(img_dev, rows, cols, angles, tf, medians=True)
+        return sino, med, eng.circus(sino, pf)
+
+    def bwd(sino, med, g):
+        gs = eng.circus_backward(sino, pf, g)
+        return eng.sinograms_backward(gs, med, rows, cols, angles, tf)
+
+    sino, med, circ = fwd()
+    grad = torch.ones_like(circ)
+    bwd(sino, med, grad)
+    torch.cuda.synchronize()
+    f_ms, b_ms = [], []
+    for _ in range(steps):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record(stream)
+        sino, med, circ = fwd()
+        e[1].record(stream)
+        bwd(sino, med, grad)
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        f_ms.append(e[0].elapsed_time(e[1]))
+        b_ms.append(e[1].elapsed_time(e[2]))
+    f, b = statistics.mean(f_ms), statistics.mean(b_ms)
+    return {"t_functionals": tf, "p_functionals": [1, 3], "forward_ms": f, "backward_ms": b,
+            "backward_over_forward": b / f, "steps": steps,
+            "note": "gradient of the sum of the circus functions with respect to the image; "
+                    "rotations recomputed in the adjoint, nothing stored but the medians"}
 
 
 BATCH_T, BATCH_P = [0, 1, 2, 3, 4, 5], [1, 2, 3]
@@ -549,6 +600,7 @@ def run_batch(args, world, rank, local_rank):
                                     "tt_circus_device + tt_zscore_device per image; e2e: one "
                                     "tt_transform (host buffers) per image"},
         "batched_over_plain": plain_ms / ms,
+        "images_per_s": world * len(imgs) / (ms / 1e3),
         "gpu_launches": 3 * args.steps,
         "roofline": {"bound": "hbm", "kernel": "batch graph (sino + circus + zscore)",
                      "achieved": achieved, "peak": peak, "peak_source": peak_kind,
@@ -726,6 +778,7 @@ def run_grad(args, world, rank, local_rank):
         "config": grad_config(world),
         "forward_ms": statistics.mean(fwd), "backward_ms": statistics.mean(bwd),
         "backward_over_forward": statistics.mean(bwd) / statistics.mean(fwd),
+        "images_per_s": world * GRAD_IMAGES / (ms / 1e3),
         "e2e": {"value": world * n_sino / e2e_s, "unit": "sinograms/s",
                 "h2d_bytes_per_step": int(h_imgs.numel() * 4),
                 "d2h_bytes_per_step": int(h_grad.numel() * 4 + 4), "loss": lv},
