@@ -656,7 +656,7 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
         a_elems += (size_t)m * cols;
         max_m = std::max(max_m, m);
     }
-    TT_CHECK(p->ensure(p->nos_a, sizeof(double) * a_elems));
+    TT_CHECK(p->ensure(p->nos_a, sizeof(float2) * a_elems));
     TT_CHECK(p->ensure(p->nos_desc, sizeof(NosDesc) * n_sino));
     TT_CHECK(p->ensure(p->nos, sizeof(float) * a_elems));
     if (max_m > tt::nos_max_rows() || tt::nos_apply_smem(max_m) > 227 * 1024)
@@ -686,7 +686,7 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
     }
     TT_CUDA(cudaMemcpyAsync(p->nos_desc.p, desc.data(), sizeof(NosDesc) * n_sino,
                             cudaMemcpyHostToDevice, st));
-    double *A = (double *)p->nos_a.p;
+    float2 *A = (float2 *)p->nos_a.p; // double-float pairs
     const NosDesc *d_desc = (const NosDesc *)p->nos_desc.p;
     TT_CUDA(tt::launch_nos_align(d_sino, rows, cols, n_sino, d_desc, (const int *)p->nos_off.p,
                                  A, a_elems, st));

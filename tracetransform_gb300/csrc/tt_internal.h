@@ -97,7 +97,7 @@ cudaError_t launch_circus_f64(const double *sino, int rows, int cols, int n_sino
 
 // Nearest orthonormal sinogram (tt_nos.cu): one aligned matrix per sinogram.
 struct NosDesc {
-    long long a_off;   // into the double m x cols matrices
+    long long a_off;   // into the double-float m x cols matrices
     long long out_off; // into the float results
     int m;             // rows + |max offset| + |min offset|
     int mx;            // max offset
@@ -114,17 +114,17 @@ struct NosWork {
 cudaError_t launch_nos_offsets(const float *sino, int rows, int cols, int n_sino, int center,
                                int *offsets, cudaStream_t st);
 cudaError_t launch_nos_align(const float *sino, int rows, int cols, int n_sino,
-                             const NosDesc *desc, const int *offsets, double *A, size_t a_elems,
+                             const NosDesc *desc, const int *offsets, float2 *A, size_t a_elems,
                              cudaStream_t st);
 // QR of the aligned matrices and X = R^T, V = I (2 n + 2 launches).
-cudaError_t launch_nos_factor(double *A, const NosDesc *desc, int n, int n_sino, int max_m,
+cudaError_t launch_nos_factor(float2 *A, const NosDesc *desc, int n, int n_sino, int max_m,
                               const NosWork &w, cudaStream_t st);
 int nos_max_rows(); // aligned rows the QR kernels hold in registers
 // One Jacobi sweep on X (n - 1 + (n & 1) launches).
 cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, cudaStream_t st);
 float nos_sweep_done_bound();
 size_t nos_apply_smem(int max_m);
-cudaError_t launch_nos_assemble(const double *A, const NosDesc *desc, int n, int n_sino,
+cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int n_sino,
                                 int max_m, const NosWork &w, float *out, cudaStream_t st);
 
 // Record a failure for tt_last_error() on this thread; returns status.

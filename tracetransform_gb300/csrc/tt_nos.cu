@@ -9,10 +9,12 @@
 //
 //   nos_offsets   per column: weighted median row - center, with the
 //                 reference's sequential float sums (one thread per column)
-//   nos_align     the shifted columns into a zeroed m x A double matrix
-//   QR            column-pivoting Householder QR, A P = Q R, in double (the
-//                 only double-precision stage: it fixes the small singular
-//                 directions that a float factorisation would lose); per
+//   nos_align     the shifted columns into a zeroed m x A matrix of
+//                 double-float pairs (hi + lo, ~48 significant bits)
+//   QR            column-pivoting Householder QR, A P = Q R, in double-float
+//                 (the only stage beyond float precision: it fixes the small
+//                 singular directions that a float factorisation would lose;
+//                 the O(m A) work per step runs on the FP32 pipes); per
 //                 column step one pivot/reflector launch and one trailing-
 //                 update launch, LAPACK-style (reflector below the diagonal,
 //                 tau, partial column norms downdated and recomputed when
@@ -58,17 +60,53 @@ __global__ void nos_offsets_kernel(const float *__restrict__ sino, int rows, int
     offsets[idx] = m - center;
 }
 
+// ---- double-float arithmetic -------------------------------------------------
+//
+// The aligned matrices hold each element as an unevaluated sum hi + lo of two
+// floats (~48 significant bits).  The QR's O(m n) work -- dot products and
+// trailing updates -- runs on these pairs with error-free float transforms
+// (Knuth's two-sum, the FMA two-product, Dekker's renormalisation), i.e. on
+// the FP32 pipes, which GB300 runs far faster than FP64.  Scalars (norms,
+// reflector coefficients) stay in double.
+
+__device__ __forceinline__ float2 df_quick(float a, float b) { // |a| >= |b|
+    const float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float s = a.x + b.x, bb = s - a.x;
+    const float e = (a.x - (s - bb)) + (b.x - bb);
+    return df_quick(s, e + a.y + b.y);
+}
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return df_quick(p, e);
+}
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ double df_to_d(float2 a) { return (double)a.x + (double)a.y; }
+__device__ __forceinline__ float2 d_to_df(double d) {
+    const float hi = __double2float_rn(d);
+    return make_float2(hi, __double2float_rn(d - (double)hi));
+}
+__device__ __forceinline__ float2 df_shfl_xor(float2 v, int o) {
+    return make_float2(__shfl_xor_sync(TT_FULL_MASK, v.x, o),
+                       __shfl_xor_sync(TT_FULL_MASK, v.y, o));
+}
+
 // grid (cols, n_sino); A_s must be zeroed before.
 __global__ void nos_align_kernel(const float *__restrict__ sino, int rows, int cols,
                                  const NosDesc *__restrict__ desc,
-                                 const int *__restrict__ offsets, double *__restrict__ A) {
+                                 const int *__restrict__ offsets, float2 *__restrict__ A) {
     const int col = blockIdx.x, s = blockIdx.y;
     const NosDesc d = desc[s];
     const int shift = d.mx - offsets[(size_t)s * cols + col];
     const float *src = sino + ((size_t)s * cols + col) * rows;
-    double *dst = A + d.a_off + (size_t)col * d.m + shift;
+    float2 *dst = A + d.a_off + (size_t)col * d.m + shift;
     for (int r = threadIdx.x; r < rows; r += blockDim.x)
-        dst[r] = (double)src[r];
+        dst[r] = make_float2(src[r], 0.f);
 }
 
 template <typename T, int kThreads> __device__ __forceinline__ T block_sum(T v, T *red) {
@@ -87,22 +125,40 @@ template <typename T, int kThreads> __device__ __forceinline__ T block_sum(T v, 
     return t;
 }
 
-// ---- column-pivoting Householder QR (double) ------------------------------
+template <int kThreads> __device__ __forceinline__ float2 block_sum_df(float2 v, float2 *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = df_add(v, df_shfl_xor(v, o));
+    if (lane == 0)
+        red[warp] = v;
+    __syncthreads();
+    float2 t = red[0];
+#pragma unroll
+    for (int w = 1; w < kThreads / 32; w++)
+        t = df_add(t, red[w]);
+    __syncthreads();
+    return t;
+}
+
+// ---- column-pivoting Householder QR (double-float) ---------------------------
 
 constexpr int kQrThreads = 256;
 
-// Squared column norms (partial and reference copy) and the identity
+// Squared column norms (partial and reference copy, double) and the identity
 // permutation.  grid (n, n_sino).
 __global__ void __launch_bounds__(kQrThreads)
-qr_init_kernel(const double *__restrict__ A, const NosDesc *__restrict__ desc, int n,
+qr_init_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n,
                double *__restrict__ norms, double *__restrict__ orig, int *__restrict__ perm) {
     __shared__ double red[kQrThreads / 32];
     const int j = blockIdx.x, s = blockIdx.y;
     const NosDesc d = desc[s];
-    const double *a = A + d.a_off + (size_t)j * d.m;
+    const float2 *a = A + d.a_off + (size_t)j * d.m;
     double v = 0;
-    for (int i = threadIdx.x; i < d.m; i += kQrThreads)
-        v += a[i] * a[i];
+    for (int i = threadIdx.x; i < d.m; i += kQrThreads) {
+        const double x = df_to_d(a[i]);
+        v += x * x;
+    }
     v = block_sum<double, kQrThreads>(v, red);
     if (threadIdx.x == 0) {
         norms[(size_t)s * n + j] = v;
@@ -118,10 +174,11 @@ qr_init_kernel(const double *__restrict__ A, const NosDesc *__restrict__ desc, i
 // Step k, one CTA per sinogram: pivot = the remaining column of largest
 // partial norm (lowest index on ties), swapped into place; then the
 // reflector H = I - tau v v^T with H A[k:, k] = (beta, 0, ...): beta on the
-// diagonal, v[1:] below it (v[0] = 1 implicit).
+// diagonal, v[1:] below it (v[0] = 1 implicit).  Per step this is O(m), so
+// its arithmetic is plain double.
 template <int K>
 __global__ void __launch_bounds__(kQrThreads)
-qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n, int k,
+qr_pivot_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, int k,
                 double *__restrict__ norms, double *__restrict__ orig, int *__restrict__ perm,
                 double *__restrict__ tau) {
     __shared__ double red[kQrThreads / 32];
@@ -132,7 +189,7 @@ qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n,
     const int s = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const NosDesc d = desc[s];
     const int m = d.m;
-    double *As = A + d.a_off;
+    float2 *As = A + d.a_off;
     double *nr = norms + (size_t)s * n, *og = orig + (size_t)s * n;
     int *pm = perm + (size_t)s * n;
     // argmax of the partial norms over j >= k
@@ -171,16 +228,16 @@ qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n,
     }
     __syncthreads();
     const int jp = piv;
-    double *x = As + (size_t)k * m;
-    double xv[K];
+    float2 *x = As + (size_t)k * m;
+    float2 xv[K];
     if (jp != k) {
-        double *cb = As + (size_t)jp * m;
-        double ov[K];
+        float2 *cb = As + (size_t)jp * m;
+        float2 ov[K];
 #pragma unroll
         for (int u = 0; u < K; u++) {
             const int i = threadIdx.x + kQrThreads * u;
-            xv[u] = i < m ? cb[i] : 0.0;
-            ov[u] = i < m ? x[i] : 0.0;
+            xv[u] = i < m ? cb[i] : make_float2(0.f, 0.f);
+            ov[u] = i < m ? x[i] : make_float2(0.f, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < K; u++) {
@@ -205,7 +262,7 @@ qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n,
 #pragma unroll
         for (int u = 0; u < K; u++) {
             const int i = threadIdx.x + kQrThreads * u;
-            xv[u] = i < m ? x[i] : 0.0;
+            xv[u] = i < m ? x[i] : make_float2(0.f, 0.f);
         }
     }
     // reflector of x = A[k:m, k]
@@ -213,10 +270,11 @@ qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n,
 #pragma unroll
     for (int u = 0; u < K; u++) {
         const int i = threadIdx.x + kQrThreads * u;
+        const double xd = df_to_d(xv[u]);
         if (i > k && i < m)
-            xn += xv[u] * xv[u];
+            xn += xd * xd;
         if (i == k)
-            s_alpha = xv[u];
+            s_alpha = xd;
     }
     xn = block_sum<double, kQrThreads>(xn, red); // its barriers publish s_alpha
     const double alpha = s_alpha;
@@ -231,65 +289,70 @@ qr_pivot_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n,
     for (int u = 0; u < K; u++) {
         const int i = threadIdx.x + kQrThreads * u;
         if (i > k && i < m)
-            x[i] = xv[u] * scale;
+            x[i] = d_to_df(df_to_d(xv[u]) * scale);
         if (i == k)
-            x[i] = beta;
+            x[i] = d_to_df(beta);
     }
     if (threadIdx.x == 0)
         tau[(size_t)s * n + k] = (beta - alpha) / beta;
 }
 
 // Step k, one CTA per trailing column j = k + 1 + blockIdx.x: A[k:, j] -=
-// tau v (v . A[k:, j]), then the partial norm loses A[k, j]^2 -- recomputed
-// from the column when that leaves less than ~sqrt(eps) of the original.
+// tau v (v . A[k:, j]) in double-float, then the partial norm loses
+// A[k, j]^2 -- recomputed from the column when that leaves less than
+// ~sqrt(eps) of the original.
 template <int K>
 __global__ void __launch_bounds__(kQrThreads)
-qr_update_kernel(double *__restrict__ A, const NosDesc *__restrict__ desc, int n, int k,
+qr_update_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, int k,
                  double *__restrict__ norms, double *__restrict__ orig,
                  const double *__restrict__ tau) {
-    __shared__ double red[kQrThreads / 32];
+    __shared__ float2 red[kQrThreads / 32];
+    __shared__ double redd[kQrThreads / 32];
     const int j = k + 1 + blockIdx.x, s = blockIdx.y;
     const NosDesc d = desc[s];
     const int m = d.m;
-    double *As = A + d.a_off;
-    const double *v = As + (size_t)k * m;
-    double *c = As + (size_t)j * m;
+    float2 *As = A + d.a_off;
+    const float2 *v = As + (size_t)k * m;
+    float2 *c = As + (size_t)j * m;
     const double t = tau[(size_t)s * n + k];
-    double vv[K], cv[K];
+    float2 vv[K], cv[K];
 #pragma unroll
     for (int u = 0; u < K; u++) {
         const int i = threadIdx.x + kQrThreads * u;
         const bool in = i > k && i < m;
-        vv[u] = in ? v[i] : 0.0;
-        cv[u] = in ? c[i] : 0.0;
+        vv[u] = in ? v[i] : make_float2(0.f, 0.f);
+        cv[u] = in ? c[i] : make_float2(0.f, 0.f);
     }
-    double ck = c[k];
+    float2 ck = c[k];
     if (t != 0) { // uniform
-        double w = 0;
+        float2 w = make_float2(0.f, 0.f);
 #pragma unroll
         for (int u = 0; u < K; u++)
-            w += vv[u] * cv[u];
-        w = block_sum<double, kQrThreads>(w, red) + ck;
-        const double tw = t * w;
+            w = df_add(w, df_mul(vv[u], cv[u]));
+        w = df_add(block_sum_df<kQrThreads>(w, red), ck);
+        const float2 ntw = df_neg(df_mul(d_to_df(t), w));
 #pragma unroll
         for (int u = 0; u < K; u++) {
             const int i = threadIdx.x + kQrThreads * u;
-            cv[u] -= tw * vv[u];
+            cv[u] = df_add(cv[u], df_mul(ntw, vv[u]));
             if (i > k && i < m)
                 c[i] = cv[u];
         }
-        ck -= tw;
+        ck = df_add(ck, ntw);
         if (threadIdx.x == 0)
             c[k] = ck;
     }
     double *nr = norms + (size_t)s * n, *og = orig + (size_t)s * n;
-    double n2 = nr[j] - ck * ck;
+    const double ckd = df_to_d(ck);
+    double n2 = nr[j] - ckd * ckd;
     if (n2 <= 1.5e-8 * og[j]) { // uniform: every thread holds the same values
         double r = 0;
 #pragma unroll
-        for (int u = 0; u < K; u++)
-            r += cv[u] * cv[u];
-        n2 = block_sum<double, kQrThreads>(r, red);
+        for (int u = 0; u < K; u++) {
+            const double cd = df_to_d(cv[u]);
+            r += cd * cd;
+        }
+        n2 = block_sum<double, kQrThreads>(r, redd);
         if (threadIdx.x == 0)
             og[j] = n2;
     }
@@ -308,7 +371,7 @@ constexpr double kNullRel = 1e-15;
 // X[i + j n] = R[j, i] (upper triangle of the QR result), V = I, and the
 // null-direction bound tiny[s] = (kNullRel R[0, 0])^2.
 // grid (ceil(n * n / 256), n_sino).
-__global__ void nos_rt_kernel(const double *__restrict__ A, const NosDesc *__restrict__ desc,
+__global__ void nos_rt_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc,
                               int n, float *__restrict__ X, float *__restrict__ V,
                               float *__restrict__ tiny) {
     const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -318,10 +381,10 @@ __global__ void nos_rt_kernel(const double *__restrict__ A, const NosDesc *__res
     const int s = blockIdx.y, i = (int)(e % n), j = (int)(e / n);
     const NosDesc d = desc[s];
     if (e == 0) {
-        const double r = kNullRel * A[d.a_off];
+        const double r = kNullRel * df_to_d(A[d.a_off]);
         tiny[s] = (float)(r * r);
     }
-    X[s * nn + e] = j <= i ? (float)A[d.a_off + j + (size_t)i * d.m] : 0.f;
+    X[s * nn + e] = j <= i ? (float)df_to_d(A[d.a_off + j + (size_t)i * d.m]) : 0.f;
     V[s * nn + e] = i == j ? 1.f : 0.f;
 }
 
@@ -547,7 +610,7 @@ constexpr int kQThreads = 256, kQCols = 4; // columns of Y per CTA
 // (shared memory: kQCols x m floats), then out[:, perm[j]] = Y[:, j].
 // grid (ceil(n / kQCols), n_sino).
 __global__ void __launch_bounds__(kQThreads)
-nos_apply_q_kernel(const double *__restrict__ A, const NosDesc *__restrict__ desc,
+nos_apply_q_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc,
                    const double *__restrict__ tau, const int *__restrict__ perm,
                    const float *__restrict__ P, int n, float *__restrict__ out) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -561,19 +624,20 @@ nos_apply_q_kernel(const double *__restrict__ A, const NosDesc *__restrict__ des
     for (int c = 0; c < kQCols; c++)
         for (int i = threadIdx.x; i < m; i += kQThreads)
             y[c * m + i] = (c < nc && i < n) ? P[s * nn + i + (size_t)(j0 + c) * n] : 0.f;
-    const double *As = A + d.a_off, *ts = tau + (size_t)s * n;
+    const float2 *As = A + d.a_off;
+    const double *ts = tau + (size_t)s * n;
     for (int k = n - 1; k >= 0; k--) {
         const float t = (float)ts[k];
         if (t == 0.f)
             continue; // uniform
-        const double *v = As + (size_t)k * m;
+        const float2 *v = As + (size_t)k * m;
         __syncthreads();
         float w[kQCols];
 #pragma unroll
         for (int c = 0; c < kQCols; c++)
             w[c] = 0.f;
         for (int i = k + 1 + threadIdx.x; i < m; i += kQThreads) {
-            const float vi = (float)v[i];
+            const float vi = (v[i].x + v[i].y);
 #pragma unroll
             for (int c = 0; c < kQCols; c++)
                 w[c] = fmaf(vi, y[c * m + i], w[c]);
@@ -594,7 +658,7 @@ nos_apply_q_kernel(const double *__restrict__ A, const NosDesc *__restrict__ des
         }
         __syncthreads(); // everyone has read y[.., k] and red
         for (int i = k + 1 + threadIdx.x; i < m; i += kQThreads) {
-            const float vi = (float)v[i];
+            const float vi = (v[i].x + v[i].y);
 #pragma unroll
             for (int c = 0; c < kQCols; c++)
                 y[c * m + i] = fmaf(-w[c], vi, y[c * m + i]);
@@ -624,9 +688,9 @@ cudaError_t launch_nos_offsets(const float *sino, int rows, int cols, int n_sino
 }
 
 cudaError_t launch_nos_align(const float *sino, int rows, int cols, int n_sino,
-                             const NosDesc *desc, const int *offsets, double *A, size_t a_elems,
+                             const NosDesc *desc, const int *offsets, float2 *A, size_t a_elems,
                              cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(A, 0, sizeof(double) * a_elems, st);
+    cudaError_t e = cudaMemsetAsync(A, 0, sizeof(float2) * a_elems, st);
     if (e != cudaSuccess)
         return e;
     nos_align_kernel<<<dim3(cols, n_sino), 128, 0, st>>>(sino, rows, cols, desc, offsets, A);
@@ -634,7 +698,7 @@ cudaError_t launch_nos_align(const float *sino, int rows, int cols, int n_sino,
 }
 
 template <int K>
-static void qr_steps(double *A, const NosDesc *desc, int n, int n_sino, const NosWork &w,
+static void qr_steps(float2 *A, const NosDesc *desc, int n, int n_sino, const NosWork &w,
                      cudaStream_t st) {
     for (int k = 0; k < n; k++) {
         qr_pivot_kernel<K><<<n_sino, kQrThreads, 0, st>>>(A, desc, n, k, w.norms, w.orig, w.perm,
@@ -647,7 +711,7 @@ static void qr_steps(double *A, const NosDesc *desc, int n, int n_sino, const No
 
 int nos_max_rows() { return 32 * kQrThreads; }
 
-cudaError_t launch_nos_factor(double *A, const NosDesc *desc, int n, int n_sino, int max_m,
+cudaError_t launch_nos_factor(float2 *A, const NosDesc *desc, int n, int n_sino, int max_m,
                               const NosWork &w, cudaStream_t st) {
     if (max_m > nos_max_rows())
         return cudaErrorInvalidValue;
@@ -707,7 +771,7 @@ float nos_sweep_done_bound() { return kJacDone; }
 
 size_t nos_apply_smem(int max_m) { return sizeof(float) * (size_t)kQCols * max_m; }
 
-cudaError_t launch_nos_assemble(const double *A, const NosDesc *desc, int n, int n_sino,
+cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int n_sino,
                                 int max_m, const NosWork &w, float *out, cudaStream_t st) {
     const long long nn = (long long)n * n;
     const dim3 ge((unsigned)((nn + 255) / 256), n_sino), gt((n + 31) / 32, (n + 31) / 32, n_sino);
