@@ -62,3 +62,40 @@ def test_orthonormal_circus_device(oracle_lib):
         want = O.circus(nos, [(0, o, c) for o in (1, 2, 3, 4, 5)])
         scale = np.abs(want).max(axis=1, keepdims=True)
         assert np.abs(got[t] - want).max() <= 1e-3 * scale.max()
+
+
+def test_nos_zero_and_rank_one(oracle_lib):
+    """All-zero sinogram: nothing to orthonormalise, zeros (as the oracle).
+    Constant sinogram (rank one, no shifts): the partial isometry u v^T with
+    unit-norm constant u and v -- every other direction is null and left out,
+    as the oracle leaves out exactly-zero ones."""
+    zero = np.zeros((40, 20), np.float32)
+    got, c = tt.nearest_orthonormal_sinogram(zero)
+    want, wc = oracle_lib.nos(zero)
+    assert got.shape == want.shape and c == wc
+    assert np.abs(got).max() == 0 and np.abs(want).max() == 0
+    const = np.full((40, 20), 3.0, np.float32)
+    got, c = tt.nearest_orthonormal_sinogram(const)
+    m, n = got.shape
+    assert m == 40  # equal columns: equal offsets, no padding rows
+    np.testing.assert_allclose(got, np.full((m, n), 1 / np.sqrt(m * n)), rtol=0, atol=1e-6)
+
+
+def test_orthonormal_circus_rejects():
+    import torch
+    from tracetransform_gb300._native import InvalidArgument, TTError
+    from tracetransform_gb300.device import Engine
+    eng = Engine(0)
+    sino = torch.rand((1, 20, 40), device="cuda")
+    import ctypes
+    from tracetransform_gb300._native import PFunctionalC, check, lib
+    with pytest.raises(InvalidArgument):  # P1 is not an orthonormal functional
+        pf = (PFunctionalC * 1)()
+        pf[0].kind, pf[0].order, pf[0].center = 1, -1, -1
+        out = torch.empty((1, 1, 20), device="cuda")
+        check(lib().tt_circus_orthonormal_device(eng.plan.handle, ctypes.c_void_p(sino.data_ptr()),
+                                                 40, 20, 1, pf, 1, ctypes.c_void_p(out.data_ptr()),
+                                                 None, None, None))
+    wide = torch.rand((1, 1030, 1100), device="cuda")  # more angles than the Jacobi holds
+    with pytest.raises(TTError):
+        eng.circus_orthonormal(wide, [1])
