@@ -124,6 +124,14 @@ tt_status tt_circus(tt_plan *plan, const float *sinogram, int rows, int cols,
 tt_status tt_rotate(tt_plan *plan, const float *image, int rows, int cols, float angle_deg,
                     float *out);
 
+/* Replaces resize(input, rows, cols) (c++/src/auxiliary.cpp:198-221), the
+ * orthonormal mode's stretch (c++/src/transform.cpp:35-41).  image:
+ * in_rows x in_cols, out: rows x cols, both column-major; bit-identical to
+ * the reference, whose outermost output rows and columns stay zero.  Needs
+ * rows, cols >= 1 and in_rows, in_cols >= 1. */
+tt_status tt_resize(tt_plan *plan, const float *image, int in_rows, int in_cols, int rows,
+                    int cols, float *out);
+
 /* Replaces zscore(const Eigen::VectorXf&) (c++/src/auxiliary.cpp:305-318)
  * applied to n_vec consecutive vectors of length len. */
 tt_status tt_zscore(tt_plan *plan, const float *in, int n_vec, int len, float *out);

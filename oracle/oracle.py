@@ -275,3 +275,48 @@ def ref_rotate(image: np.ndarray, angle_deg: float) -> np.ndarray:
         subprocess.run([REF_BIN, "rotate", src, str(rows), str(cols), repr(float(angle_deg)), dst],
                        check=True)
         return np.fromfile(dst, np.float32).reshape((rows, cols), order="F")
+
+
+def ref_resize(image: np.ndarray, rows: int, cols: int) -> np.ndarray:
+    """resize() run by the reference's own sources."""
+    in_rows, in_cols = image.shape
+    with tempfile.TemporaryDirectory() as d:
+        src, dst = os.path.join(d, "img.f32"), os.path.join(d, "out.f32")
+        _f32(image).tofile(src)
+        subprocess.run([REF_BIN, "resize", src, str(in_rows), str(in_cols), str(rows), str(cols),
+                        dst], check=True)
+        return np.fromfile(dst, np.float32).reshape((rows, cols), order="F")
+
+
+def ref_netpbm(text: bytes) -> dict:
+    """readnetpbm / gray2mat / writepgm run by the reference's own sources on
+    the file contents `text`: {"pixels": [...], "gray": [...], "pgm": [...]}
+    per channel, or {"error": message} when the reader throws."""
+    with tempfile.TemporaryDirectory() as d:
+        src, prefix = os.path.join(d, "in.pgm"), os.path.join(d, "out")
+        with open(src, "wb") as f:
+            f.write(text)
+        r = subprocess.run([REF_BIN, "netpbm", src, prefix], capture_output=True)
+        if r.returncode != 0:
+            return {"error": r.stderr.decode().strip()}
+        meta = open(prefix + ".meta").read().split("\n")
+        out = {"pixels": [], "gray": [], "pgm": [], "log": r.stderr.decode()}
+        for i, line in enumerate(l for l in meta[1:] if l.startswith("shape")):
+            rows, cols = (int(v) for v in line.split()[1:])
+            base = f"{prefix}.c{i}"
+            out["pixels"].append(np.fromfile(base + ".i32", np.int32).reshape((rows, cols), order="F"))
+            out["gray"].append(np.fromfile(base + ".gray.f32", np.float32).reshape((rows, cols), order="F"))
+            out["pgm"].append(open(base + ".pgm", "rb").read())
+        return out
+
+
+def ref_mat2gray(image: np.ndarray):
+    """mat2gray run by the reference's own sources: (int32 matrix, writepgm
+    text of it)."""
+    rows, cols = image.shape
+    with tempfile.TemporaryDirectory() as d:
+        src, prefix = os.path.join(d, "img.f32"), os.path.join(d, "out")
+        _f32(image).tofile(src)
+        subprocess.run([REF_BIN, "mat2gray", src, str(rows), str(cols), prefix], check=True)
+        gray = np.fromfile(prefix + ".i32", np.int32).reshape((rows, cols), order="F")
+        return gray, open(prefix + ".pgm", "rb").read()

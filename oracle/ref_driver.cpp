@@ -8,6 +8,14 @@
 //       and writes <prefix>.{padded,sino,nos,circus,sig}.f32 and <prefix>.meta
 //   ttref rotate <img.f32> <rows> <cols> <angle_deg> <out.f32>
 //       rotate() about ((cols-1)/2, (rows-1)/2) (c++/src/rottest.cpp:46-49)
+//   ttref resize <img.f32> <rows> <cols> <out_rows> <out_cols> <out.f32>
+//       resize() (c++/src/auxiliary.cpp:198-221)
+//   ttref netpbm <in.pgm|in.ppm> <prefix>
+//       readnetpbm() (c++/src/auxiliary.cpp:47-99); per channel i writes
+//       <prefix>.c<i>.i32 (the pixels), <prefix>.c<i>.gray.f32 (gray2mat,
+//       :148-157) and <prefix>.c<i>.pgm (writepgm, :101-128); <prefix>.meta
+//   ttref mat2gray <img.f32> <rows> <cols> <prefix>
+//       mat2gray() (:159-178): <prefix>.i32 and writepgm of it, <prefix>.pgm
 //   ttref bench <img.f32> <rows> <cols> <step> <T,..> <P,..|-> <iterations>
 //       demo.cpp's benchmark mode (c++/src/demo.cpp:222-248): one warm-up and
 //       <iterations> timed getTransform(..., false) calls; prints t_i=<s>
@@ -149,6 +157,50 @@ static int do_rotate(int argc, char **argv) {
     return 0;
 }
 
+static int do_resize(int argc, char **argv) {
+    if (argc != 8)
+        return 2;
+    int rows = atoi(argv[3]), cols = atoi(argv[4]);
+    int out_rows = atoi(argv[5]), out_cols = atoi(argv[6]);
+    Eigen::MatrixXf out = resize(read_image(argv[2], rows, cols), out_rows, out_cols);
+    write_floats(argv[7], out.data(), out.size());
+    return 0;
+}
+
+static void write_ints(const std::string &path, const Eigen::MatrixXi &m) {
+    std::ofstream f(path, std::ios::binary);
+    f.write(reinterpret_cast<const char *>(m.data()), sizeof(int) * (size_t)m.size());
+}
+
+static int do_netpbm(int argc, char **argv) {
+    if (argc != 4)
+        return 2;
+    std::string prefix = argv[3];
+    std::vector<Eigen::MatrixXi> components = readnetpbm(argv[2]);
+    std::ofstream meta(prefix + ".meta");
+    meta << "channels " << components.size() << "\n";
+    for (size_t i = 0; i < components.size(); i++) {
+        const std::string base = prefix + ".c" + std::to_string(i);
+        meta << "shape " << components[i].rows() << " " << components[i].cols() << "\n";
+        write_ints(base + ".i32", components[i]);
+        Eigen::MatrixXf gray = gray2mat(components[i]);
+        write_floats(base + ".gray.f32", gray.data(), gray.size());
+        writepgm(base + ".pgm", components[i]);
+    }
+    return 0;
+}
+
+static int do_mat2gray(int argc, char **argv) {
+    if (argc != 6)
+        return 2;
+    int rows = atoi(argv[3]), cols = atoi(argv[4]);
+    std::string prefix = argv[5];
+    Eigen::MatrixXi gray = mat2gray(read_image(argv[2], rows, cols));
+    write_ints(prefix + ".i32", gray);
+    writepgm(prefix + ".pgm", gray);
+    return 0;
+}
+
 static int do_bench(int argc, char **argv) {
     if (argc != 9)
         return 2;
@@ -174,7 +226,7 @@ static int do_bench(int argc, char **argv) {
 
 int main(int argc, char **argv) {
     if (argc < 2) {
-        std::cerr << "usage: ttref transform|rotate|bench ..." << std::endl;
+        std::cerr << "usage: ttref transform|rotate|resize|netpbm|mat2gray|bench ..." << std::endl;
         return 2;
     }
     std::string mode = argv[1];
@@ -186,6 +238,12 @@ int main(int argc, char **argv) {
             rc = do_rotate(argc, argv);
         else if (mode == "bench")
             rc = do_bench(argc, argv);
+        else if (mode == "resize")
+            rc = do_resize(argc, argv);
+        else if (mode == "netpbm")
+            rc = do_netpbm(argc, argv);
+        else if (mode == "mat2gray")
+            rc = do_mat2gray(argc, argv);
     } catch (const std::exception &e) {
         std::cerr << "error: " << e.what() << std::endl;
         return 1;

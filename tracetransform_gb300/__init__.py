@@ -8,13 +8,14 @@ host side.  Build the library with ``python -m tracetransform_gb300.build``.
 from . import api
 from .api import (PFunctional, PFunctionalWrapper, Plan, TFunctional, TFunctionalWrapper,
                   Transformer, ValidationError, angles_from_step, getCircusFunctions,
-                  getSinograms, nearest_orthonormal_sinogram, ortho_size, pad, pad_geometry,
-                  rotate, transform_batch, writecsv, zscore)
+                  getSinograms, gray2mat, mat2gray, nearest_orthonormal_sinogram, ortho_size,
+                  pad, pad_geometry, readnetpbm, resize, rotate, transform_batch, writecsv,
+                  writepgm, zscore)
 
 __all__ = [
     "PFunctional", "PFunctionalWrapper", "Plan", "TFunctional", "TFunctionalWrapper",
     "Transformer", "ValidationError", "angles_from_step", "getCircusFunctions", "getSinograms",
-    "nearest_orthonormal_sinogram", "ortho_size", "pad", "pad_geometry", "rotate",
-    "transform_batch", "writecsv", "zscore",
+    "gray2mat", "mat2gray", "nearest_orthonormal_sinogram", "ortho_size", "pad", "pad_geometry",
+    "readnetpbm", "resize", "rotate", "transform_batch", "writecsv", "writepgm", "zscore",
 ]
 __version__ = "0.1.0"

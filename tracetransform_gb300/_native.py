@@ -21,7 +21,7 @@ STATUS_NAMES = {0: "TT_OK", 1: "TT_ERR_INVALID_ARG", 2: "TT_ERR_UNSUPPORTED", 3:
 EXPORTS = (
     "tt_plan_create", "tt_plan_destroy", "tt_plan_synchronize", "tt_last_error", "tt_version",
     "tt_pad_geometry", "tt_ortho_size", "tt_angles_from_step", "tt_sinograms", "tt_circus",
-    "tt_zscore", "tt_rotate", "tt_transform", "tt_sinograms_device", "tt_circus_device", "tt_zscore_device",
+    "tt_zscore", "tt_rotate", "tt_resize", "tt_transform", "tt_sinograms_device", "tt_circus_device", "tt_zscore_device",
     "tt_circus_zscore_noalloc", "tt_transform_batch", "tt_transform_batch_device",
     "tt_circus_backward_device", "tt_sinograms_backward_device", "tt_sinograms_f64_device",
     "tt_circus_f64_device", "tt_circus_backward_f64_device", "tt_sinograms_backward_f64_device",
@@ -74,6 +74,7 @@ def lib():
         "tt_circus": [_P, _F, _int, _int, ctypes.POINTER(PFunctionalC), _int, _F],
         "tt_zscore": [_P, _F, _int, _int, _F],
         "tt_rotate": [_P, _F, _int, _int, ctypes.c_float, _F],
+        "tt_resize": [_P, _F, _int, _int, _int, _int, _F],
         "tt_transform": [_P, _F, _int, _int, ctypes.c_uint, _I32, _int, ctypes.POINTER(PFunctionalC),
                          _int, _F, _F],
         "tt_sinograms_device": [_P, _P, _int, _int, _int, _int, _int, _int, _F, _int, _I32, _int,

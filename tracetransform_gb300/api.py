@@ -25,7 +25,9 @@ from __future__ import annotations
 
 import ctypes
 import enum
+import logging
 import math
+import re
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence
 
@@ -260,6 +262,18 @@ def rotate(image, angle_degrees: float, plan: Optional[Plan] = None) -> np.ndarr
     return out.reshape((rows, cols), order="F")
 
 
+def resize(image, rows: int, cols: int, plan: Optional[Plan] = None) -> np.ndarray:
+    """resize(input, rows, cols) of c++/src/auxiliary.cpp:198-221 (the
+    orthonormal mode's stretch), bit-identical to the reference."""
+    image = np.asarray(image, dtype=np.float32)
+    if image.ndim != 2:
+        raise ValueError("expected a 2-D matrix")
+    out = np.zeros(int(rows) * int(cols), np.float32)
+    check(lib().tt_resize(_handle(plan), fptr(_colmajor(image)), image.shape[0], image.shape[1],
+                          int(rows), int(cols), fptr(out)))
+    return out.reshape((int(rows), int(cols)), order="F")
+
+
 def zscore(vector, plan: Optional[Plan] = None) -> np.ndarray:
     """(x - mean) / std with n - 1 (c++/src/auxiliary.cpp:305-318)."""
     x = np.ascontiguousarray(np.asarray(vector, dtype=np.float32).ravel())
@@ -284,6 +298,142 @@ def _ostream_float(v: float) -> str:
     if math.isinf(v):
         return "inf" if v > 0 else "-inf"
     return "%g" % v
+
+
+_log = logging.getLogger("tracetransform_gb300")
+_PGM_WS = b" \t\n\r"
+
+
+def _netpbm_skip(buf: bytes, pos: int) -> int:
+    """Whitespace and comment skipping of readNetpbmValue
+    (c++/src/auxiliary.cpp:26-37): a '#' at the start of a value runs to the
+    end of its line."""
+    n = len(buf)
+    while pos < n:
+        ch = buf[pos]
+        if ch == 0x23:  # '#'
+            nl = buf.find(b"\n", pos)
+            pos = n if nl < 0 else nl + 1
+        elif ch in _PGM_WS:
+            pos += 1
+        else:
+            break
+    return pos
+
+
+def _netpbm_header_value(buf: bytes, pos: int, text: bool):
+    """One header value as `stream >> value` reads it after the skip: a token
+    up to the next space for the magic string, a run of digits for a size."""
+    pos = _netpbm_skip(buf, pos)
+    n = len(buf)
+    while pos < n and buf[pos] in b" \t\n\r\x0b\x0c":
+        pos += 1
+    start = pos
+    if text:
+        while pos < n and buf[pos] not in b" \t\n\r\x0b\x0c":
+            pos += 1
+        if pos == start:
+            raise RuntimeError("Error processing file")
+        return buf[start:pos].decode("latin-1"), pos
+    if pos < n and buf[pos] == 0x2B:  # '+'
+        pos += 1
+    digits = pos
+    while pos < n and 0x30 <= buf[pos] <= 0x39:
+        pos += 1
+    if pos == digits:
+        raise RuntimeError("Error processing file")
+    return int(buf[digits:pos]), pos
+
+
+def readnetpbm(filename: str) -> List[np.ndarray]:
+    """readnetpbm of c++/src/auxiliary.cpp:47-99: an ASCII PGM (P2, one
+    channel) or PPM (P3, three channels, interleaved per pixel) file as one
+    int32 rows x cols matrix per channel.  Comments start with '#' and run to
+    the end of the line.  A maxval other than 255 and data after the last
+    pixel only log a warning, as in the reference; a missing or malformed
+    value raises RuntimeError("Error processing file").  Pixel values are
+    read as unsigned 32-bit integers and stored as int32 (so "-1" reads as
+    -1, as the reference's unsigned read followed by its int store gives)."""
+    try:
+        with open(filename, "rb") as f:
+            buf = f.read()
+    except OSError as e:
+        raise RuntimeError("could not open input file") from e
+    magic, pos = _netpbm_header_value(buf, 0, True)
+    if magic == "P2":
+        channels = 1
+    elif magic == "P3":
+        channels = 3
+    else:
+        raise RuntimeError("Invalid Netpbm magic")
+    cols, pos = _netpbm_header_value(buf, pos, False)
+    rows, pos = _netpbm_header_value(buf, pos, False)
+    maxval, pos = _netpbm_header_value(buf, pos, False)
+    if maxval != 255:
+        _log.warning("Pixels not properly clipped to [0,255]")
+    count = rows * cols * channels
+    # past the header a comment can only end a value, so blanking comments
+    # out and splitting on whitespace reads the same values
+    body = re.sub(rb"#[^\n]*\n?", b" ", buf[pos:])
+    tokens = body.split()
+    if len(tokens) < count:
+        raise RuntimeError("Error processing file")
+    if len(tokens) > count:
+        _log.warning("Trailing data at end of image file")
+    try:
+        vals = np.array(tokens[:count]).astype(np.int64) if count else np.zeros(0, np.int64)
+    except ValueError as e:
+        raise RuntimeError("Error processing file") from e
+    if count and (vals.max() > 0xFFFFFFFF or vals.min() < -0xFFFFFFFF):
+        raise RuntimeError("Error processing file")
+    vals = (vals & 0xFFFFFFFF).astype(np.uint32).view(np.int32)
+    pix = vals.reshape(rows, cols, channels)
+    return [np.asfortranarray(pix[:, :, c]) for c in range(channels)]
+
+
+def writepgm(filename: str, data) -> None:
+    """writepgm of c++/src/auxiliary.cpp:101-128: "P2", "cols rows", 255,
+    then the values row by row, each followed by a space, or by a newline
+    once the current line holds more than 66 characters."""
+    data = np.asarray(data)
+    if data.ndim != 2:
+        raise ValueError("expected a 2-D matrix")
+    out = ["P2\n%d %d\n255\n" % (data.shape[1], data.shape[0])]
+    run = 0
+    for v in data.astype(np.int64).ravel(order="C").tolist():
+        t = str(v)
+        run += len(t)
+        if run > 66:
+            out.append(t + "\n")
+            run = 0
+        else:
+            out.append(t + " ")
+            run += 1
+    with open(filename, "w") as f:
+        f.write("".join(out))
+
+
+def gray2mat(data) -> np.ndarray:
+    """gray2mat of c++/src/auxiliary.cpp:148-157: pixel / 255.0 in double,
+    stored as float32 (column-major, as Eigen stores it)."""
+    data = np.asarray(data)
+    return np.asfortranarray((data.astype(np.float64) / 255.0).astype(np.float32))
+
+
+def mat2gray(data) -> np.ndarray:
+    """mat2gray of c++/src/auxiliary.cpp:159-178: scale by 255 / the largest
+    value (at least 0) in double and truncate to int32.  Where that is not a
+    finite int32 (an all-zero matrix divides 0 by 0) the value is INT32_MIN,
+    the result the reference's x86-64 build gives for such a conversion."""
+    data = np.asarray(data, dtype=np.float32)
+    finite = data[~np.isnan(data)]
+    maximum = np.float32(max(0.0, float(finite.max()))) if finite.size else np.float32(0.0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        scaled = data.astype(np.float64) * 255.0 / np.float64(maximum)
+    ok = np.isfinite(scaled) & (scaled > -2147483649.0) & (scaled < 2147483648.0)
+    out = np.full(data.shape, np.iinfo(np.int32).min, np.int32)
+    out[ok] = np.trunc(scaled[ok]).astype(np.int32)
+    return np.asfortranarray(out)
 
 
 def transform_batch_flat(flat: np.ndarray, offsets, rows, cols, angle_stepsizes,
@@ -341,6 +491,12 @@ def transform_batch(images: Sequence, angle_stepsizes: Sequence[int], tfunctiona
     return out
 
 
+def _write_debug_sinograms(basename: str, tfs: List[TFunctionalWrapper], sinograms) -> None:
+    for t, sino in zip(tfs, sinograms):
+        writecsv(f"{basename}-{t.name}.csv", sino)
+        writepgm(f"{basename}-{t.name}.pgm", mat2gray(sino))
+
+
 class Transformer:
     """Transformer of c++/src/transform.hpp:24-38 on the GPU engine."""
 
@@ -355,14 +511,24 @@ class Transformer:
             raise ValidationError("angle step must be >= 1")
 
     def getTransform(self, tfunctionals: Sequence, pfunctionals: Sequence,
-                     write_data: bool = True) -> np.ndarray:
+                     write_data: bool = True, debug: bool = False) -> np.ndarray:
         """Sinograms -> [nearest orthonormal sinogram] -> circus -> z-score.
 
         Returns the A x (nT * nP) signature matrix; with write_data it is also
         written to <basename>.csv.  Hermite centers of pfunctionals are
-        updated in place, as the reference does (transform.cpp:80-84)."""
+        updated in place, as the reference does (transform.cpp:80-84).
+        write_data with debug (the reference's debug log level) also writes
+        each sinogram as <basename>-<T name>.csv and, through mat2gray, .pgm
+        (transform.cpp:61-72)."""
         tfs = _as_tfunctionals(tfunctionals)
         pfs = _as_pfunctionals(pfunctionals)
+        if write_data and debug:
+            img = self._image
+            if self._orthonormal:
+                side = ortho_size(self._angle_stepsize)
+                img = resize(img, side, side, self._plan)
+            _write_debug_sinograms(self._basename, tfs,
+                                   getSinograms(pad(img), self._angle_stepsize, tfs, self._plan))
         n_h = sum(1 for p in pfs if p.functional == PFunctional.Hermite)
         if n_h and n_h != len(pfs):
             raise ValidationError("Cannot mix regular and orthonormal P-functionals")

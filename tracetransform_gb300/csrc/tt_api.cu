@@ -139,31 +139,6 @@ int ortho_side(unsigned step) {
     return (int)std::ceil(ndiag / std::sqrt(2));
 }
 
-// resize() of c++/src/auxiliary.cpp:198-221 (the orthonormal mode's stretch).
-std::vector<float> resize_image(const float *in, int in_rows, int in_cols, int rows, int cols) {
-    std::vector<float> out((size_t)rows * cols, 0.f);
-    const float t00 = ((float)in_rows) / rows, t11 = ((float)in_cols) / cols;
-    for (int col = 1; col < cols - 1; col++) {
-        for (int row = 1; row < rows - 1; row++) {
-            const float px = (float)col + 0.5f, py = (float)row + 0.5f;
-            float qx = px * t00 + py * 0.0f, qy = px * 0.0f + py * t11;
-            qx = qx - 0.5f;
-            qy = qy - 0.5f;
-            if (qx < 0 || qy < 0 || qx >= in_cols - 1 || qy >= in_rows - 1)
-                continue;
-            float xi, yi;
-            const float xf = std::modf(qx, &xi), yf = std::modf(qy, &yi);
-            const size_t x0 = (size_t)xi, y0 = (size_t)yi;
-            const float s00 = in[y0 + x0 * in_rows], s01 = in[y0 + (x0 + 1) * in_rows];
-            const float s10 = in[y0 + 1 + x0 * in_rows], s11 = in[y0 + 1 + (x0 + 1) * in_rows];
-            out[(size_t)row + (size_t)col * rows] = s00 * (1 - xf) * (1 - yf) +
-                                                    s01 * xf * (1 - yf) +
-                                                    s10 * (1 - xf) * yf + s11 * xf * yf;
-        }
-    }
-    return out;
-}
-
 
 } // namespace
 
@@ -177,7 +152,7 @@ struct tt_plan {
     std::map<std::tuple<int, int, int>, float *> herm;  // (n, order, center)
     std::map<std::vector<float>, float2 *> trig;        // angle list -> (c, s)
     std::map<std::vector<long>, const float **> herm_ptrs;
-    DevBuf in, sino, circ, sig, region, nos, batch_in, batch_out, params;
+    DevBuf in, stretch, sino, circ, sig, region, nos, batch_in, batch_out, params;
     // nearest orthonormal sinogram scratch (double matrices, V, norms, ...)
     DevBuf nos_a, nos_work, nos_desc, nos_off;
     // the QR and one Jacobi sweep as graphs, for the buffers and sizes they
@@ -1230,6 +1205,25 @@ tt_status tt_rotate(tt_plan *plan, const float *image, int rows, int cols, float
     return TT_OK;
 }
 
+tt_status tt_resize(tt_plan *plan, const float *image, int in_rows, int in_cols, int rows,
+                    int cols, float *out) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    if (in_rows <= 0 || in_cols <= 0 || rows <= 0 || cols <= 0 || !image || !out)
+        return fail(TT_ERR_INVALID_ARG, "bad resize %dx%d -> %dx%d", in_rows, in_cols, rows,
+                    cols);
+    const size_t in_elems = (size_t)in_rows * in_cols, elems = (size_t)rows * cols;
+    cudaStream_t st = p->stream;
+    TT_CHECK(p->ensure(p->in, sizeof(float) * in_elems));
+    TT_CHECK(p->ensure(p->stretch, sizeof(float) * elems));
+    TT_CUDA(cudaMemcpyAsync(p->in.p, image, sizeof(float) * in_elems, cudaMemcpyHostToDevice, st));
+    TT_CUDA(tt::launch_resize((const float *)p->in.p, in_rows, in_cols, rows, cols,
+                              (float *)p->stretch.p, st));
+    TT_CUDA(cudaMemcpyAsync(out, p->stretch.p, sizeof(float) * elems, cudaMemcpyDeviceToHost, st));
+    TT_CUDA(cudaStreamSynchronize(st));
+    return TT_OK;
+}
+
 tt_status tt_zscore(tt_plan *plan, const float *in, int n_vec, int len, float *out) {
     tt_plan *p;
     TT_CHECK(resolve_plan(plan, &p));
@@ -1267,28 +1261,30 @@ tt_status tt_transform(tt_plan *plan, const float *image, int rows, int cols,
         return fail(TT_ERR_INVALID_ARG, "Cannot mix regular and orthonormal P-functionals");
     const bool ortho = n_herm > 0;
 
-    // Transformer::Transformer: optional stretch, then padding (implicit here)
-    std::vector<float> stretched;
-    const float *img = image;
+    // Transformer::Transformer: optional stretch (on the device), then
+    // padding (implicit in the sampling)
     int ir = rows, ic = cols;
-    if (ortho) {
-        const int side = ortho_side(angle_stepsize);
-        stretched = resize_image(image, rows, cols, side, side);
-        img = stretched.data();
-        ir = ic = side;
-    }
+    if (ortho)
+        ir = ic = ortho_side(angle_stepsize);
     int n, ro, co;
     pad_geometry(ir, ic, &n, &ro, &co);
     std::vector<float> ang = step_angles(angle_stepsize);
     const int A = (int)ang.size();
     const size_t sino_elems = (size_t)n_t * n * A, circ_elems = (size_t)n_t * n_p * A;
     cudaStream_t st = p->stream;
-    TT_CHECK(p->ensure(p->in, sizeof(float) * (size_t)ir * ic));
+    TT_CHECK(p->ensure(p->in, sizeof(float) * (size_t)rows * cols));
     TT_CHECK(p->ensure(p->sino, sizeof(float) * std::max<size_t>(sino_elems, 1)));
     TT_CHECK(p->ensure(p->circ, sizeof(float) * std::max<size_t>(circ_elems, 1)));
     TT_CHECK(p->ensure(p->sig, sizeof(float) * std::max<size_t>(circ_elems, 1)));
-    TT_CUDA(cudaMemcpyAsync(p->in.p, img, sizeof(float) * (size_t)ir * ic, cudaMemcpyHostToDevice, st));
-    TT_CHECK(run_sinograms(p, (const float *)p->in.p, ir, ic, ir, n, ro, co, nullptr, ang.data(), A,
+    TT_CUDA(cudaMemcpyAsync(p->in.p, image, sizeof(float) * (size_t)rows * cols,
+                            cudaMemcpyHostToDevice, st));
+    const float *src = (const float *)p->in.p;
+    if (ortho) {
+        TT_CHECK(p->ensure(p->stretch, sizeof(float) * (size_t)ir * ic));
+        TT_CUDA(tt::launch_resize(src, rows, cols, ir, ic, (float *)p->stretch.p, st));
+        src = (const float *)p->stretch.p;
+    }
+    TT_CHECK(run_sinograms(p, src, ir, ic, ir, n, ro, co, nullptr, ang.data(), A,
                            tfuncs, n_t, tneed, (float *)p->sino.p, nullptr, st));
     if (n_p == 0 || A == 0) {
         TT_CUDA(cudaStreamSynchronize(st));

@@ -183,6 +183,9 @@ int sino_stride(int n, int lines);
 cudaError_t launch_sinograms(const SinoArgs &a, int lines, cudaStream_t stream);
 cudaError_t launch_rotate(cudaTextureObject_t tex, int rows, int cols, float c, float s,
                           float *out, cudaStream_t stream);
+// resize() of the orthonormal mode; column-major device buffers.
+cudaError_t launch_resize(const float *in, int in_rows, int in_cols, int rows, int cols,
+                          float *out, cudaStream_t stream);
 cudaError_t launch_region_bbox(const float *frame, int n, int *d_region,
                                cudaStream_t stream);
 cudaError_t launch_circus(const CircusArgs &a, cudaStream_t stream);

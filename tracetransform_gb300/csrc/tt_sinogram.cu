@@ -480,6 +480,39 @@ __global__ void rotate_kernel(cudaTextureObject_t tex, int rows, int cols, float
     out[i] = v;
 }
 
+// resize() of c++/src/auxiliary.cpp:198-221: the output pixel (row, col)
+// samples the input at ((col + 0.5) t00 - 0.5, (row + 0.5) t11 - 0.5) with
+// t00 = in_rows / rows, t11 = in_cols / cols (the reference scales x by the
+// row ratio and y by the column ratio; the orthonormal mode only resizes
+// square images to squares).  The outermost rows and columns stay zero, as
+// do samples outside the interpolation domain.  Column-major in and out, one
+// thread per output pixel; rounding and operation order as interpolate().
+__global__ void resize_kernel(const float *__restrict__ in, int in_rows, int in_cols, int rows,
+                              int cols, float t00, float t11, float *__restrict__ out) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)rows * cols)
+        return;
+    const int row = (int)(i % rows), col = (int)(i / rows);
+    float v = 0.f;
+    if (row >= 1 && row < rows - 1 && col >= 1 && col < cols - 1) {
+        const float qx = __fsub_rn(__fmul_rn((float)col + 0.5f, t00), 0.5f);
+        const float qy = __fsub_rn(__fmul_rn((float)row + 0.5f, t11), 0.5f);
+        if (qx >= 0.f && qy >= 0.f && qx < (float)(in_cols - 1) && qy < (float)(in_rows - 1)) {
+            const float xi = truncf(qx), yi = truncf(qy);
+            const float xf = __fsub_rn(qx, xi), yf = __fsub_rn(qy, yi);
+            const size_t x0 = (size_t)xi, y0 = (size_t)yi;
+            const float *c0 = in + x0 * in_rows + y0, *c1 = c0 + in_rows;
+            const float omx = __fsub_rn(1.f, xf), omy = __fsub_rn(1.f, yf);
+            const float t0 = __fmul_rn(__fmul_rn(__ldg(c0), omx), omy);
+            const float t1 = __fmul_rn(__fmul_rn(__ldg(c1), xf), omy);
+            const float t2 = __fmul_rn(__fmul_rn(__ldg(c0 + 1), omx), yf);
+            const float t3 = __fmul_rn(__fmul_rn(__ldg(c1 + 1), xf), yf);
+            v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
+        }
+    }
+    out[i] = v;
+}
+
 // Bounding box of the non-zero pixels of an n x n frame.
 __global__ void bbox_init(int *r) {
     r[0] = INT_MAX; // min row
@@ -643,6 +676,17 @@ cudaError_t launch_rotate(cudaTextureObject_t tex, int rows, int cols, float c, 
         return cudaSuccess;
     rotate_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(tex, rows, cols,
                                                                        make_float2(c, s), out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resize(const float *in, int in_rows, int in_cols, int rows, int cols,
+                          float *out, cudaStream_t stream) {
+    const long long total = (long long)rows * cols;
+    if (total == 0)
+        return cudaSuccess;
+    const float t00 = (float)in_rows / (float)rows, t11 = (float)in_cols / (float)cols;
+    resize_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(in, in_rows, in_cols, rows,
+                                                                       cols, t00, t11, out);
     return cudaGetLastError();
 }
 
