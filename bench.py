@@ -324,14 +324,14 @@ def run_engine(args, world, rank, local_rank):
     ms = sum(step_ms) / len(step_ms)
     ms = max_over_ranks(ms, world)
     # sinograms, circus, z-score; with the Hermite circus: weighted-median
-    # offsets, alignment, QR (qr_init, n pivot + n - 1 update launches, R^T),
-    # the sweeps (one launch per block round), assembly (6), one circus
-    # launch per sinogram and a z-score
+    # offsets, alignment, QR (qr_init, one launch per column step, R^T), the
+    # sweeps (one launch per block round), assembly (6), one circus launch
+    # per sinogram and a z-score
     launches = 3
     if herm:
-        nb = (A + 7) // 8  # 8-column blocks, nbp - 1 block rounds per sweep
+        nb = (A + 15) // 16  # 16-column blocks, nbp - 1 block rounds per sweep
         nbp = nb + (nb & 1)
-        launches += 2 + (2 * A + 1) + eng.last_sweeps * (nbp - 1) + 6 + len(tfs) + 1
+        launches += 2 + (A + 2) + eng.last_sweeps * (nbp - 1) + 6 + len(tfs) + 1
     launches *= args.steps
 
     # end to end through the C ABI drop-in, pinned host buffers

@@ -640,22 +640,25 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
                     tt::nos_max_rows());
     if (cols > 1024)
         return fail(TT_ERR_UNSUPPORTED, "orthonormal circus of %d angles exceeds 1024", cols);
-    // scratch: 3 double + 1 int vectors of n, 3 float n x n matrices, 1 float vector
+    // scratch: 6 double + 3 int vectors of n, 3 float n x n matrices, 1 float vector
     const size_t nv = ncol, nm = (size_t)cols * cols * n_sino;
-    TT_CHECK(p->ensure(p->nos_work, sizeof(double) * 3 * nv + sizeof(int) * nv +
+    TT_CHECK(p->ensure(p->nos_work, sizeof(double) * 6 * nv + sizeof(int) * 3 * nv +
                                         sizeof(float) * (3 * nm + nv) + sizeof(unsigned) * n_sino +
                                         sizeof(float) * n_sino + 64));
     tt::NosWork w;
     {
         char *q = (char *)p->nos_work.p;
         w.norms = (double *)q;
-        w.orig = w.norms + nv;
+        w.orig = w.norms + 2 * nv;
         w.tau = w.orig + nv;
-        w.X = (float *)(w.tau + nv);
+        w.beta = w.tau + nv;
+        w.scale = w.beta + nv;
+        w.X = (float *)(w.scale + nv);
         w.V = w.X + nm;
         w.P = w.V + nm;
         w.inv = w.P + nm;
-        w.perm = (int *)(w.inv + nv);
+        w.cmap = (int *)(w.inv + nv);
+        w.perm = w.cmap + 2 * nv;
         w.off_bits = (unsigned *)(w.perm + nv);
         w.tiny = (float *)(w.off_bits + n_sino);
     }
@@ -665,7 +668,7 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
     const NosDesc *d_desc = (const NosDesc *)p->nos_desc.p;
     TT_CUDA(tt::launch_nos_align(d_sino, rows, cols, n_sino, d_desc, (const int *)p->nos_off.p,
                                  A, a_elems, st));
-    // QR (2 cols + 2 launches) and one Jacobi sweep (about cols launches),
+    // QR (cols + 2 launches) and one Jacobi sweep (about cols / 16 launches),
     // each captured once per buffer set and size and replayed
     const std::vector<const void *> key = {A, d_desc, p->nos_work.p,
                                            (const void *)(size_t)cols,

@@ -104,8 +104,10 @@ struct NosDesc {
 };
 // Per-call scratch of the nearest orthonormal sinogram (n = angles).
 struct NosWork {
-    double *norms, *orig, *tau; // n_sino x n each (QR partial norms, reflector scales)
-    int *perm;                  // n_sino x n column permutation
+    double *norms;              // 2 x n_sino x n: QR partial norms by stored column, by step parity
+    double *orig, *tau, *beta, *scale; // n_sino x n each (norms at the last recompute, reflectors)
+    int *cmap;                  // 2 x n_sino x n: position -> stored column, by step parity
+    int *perm;                  // n_sino x n: stored column that ends at each position
     float *X, *V, *P;           // n_sino x n x n each (R^T, Jacobi V, polar(R))
     float *inv;                 // n_sino x n
     unsigned *off_bits;         // n_sino: largest rotated |cos| of a sweep (float bits)
@@ -116,7 +118,7 @@ cudaError_t launch_nos_offsets(const float *sino, int rows, int cols, int n_sino
 cudaError_t launch_nos_align(const float *sino, int rows, int cols, int n_sino,
                              const NosDesc *desc, const int *offsets, float2 *A, size_t a_elems,
                              cudaStream_t st);
-// QR of the aligned matrices and X = R^T, V = I (2 n + 2 launches).
+// QR of the aligned matrices and X = R^T, V = I (n + 2 launches).
 cudaError_t launch_nos_factor(float2 *A, const NosDesc *desc, int n, int n_sino, int max_m,
                               const NosWork &w, cudaStream_t st);
 int nos_max_rows(); // aligned rows the QR kernels hold in registers

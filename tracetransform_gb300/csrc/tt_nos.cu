@@ -14,11 +14,11 @@
 //   QR            column-pivoting Householder QR, A P = Q R, in double-float
 //                 (the only stage beyond float precision: it fixes the small
 //                 singular directions that a float factorisation would lose;
-//                 the O(m A) work per step runs on the FP32 pipes); per
-//                 column step one pivot/reflector launch and one trailing-
-//                 update launch, LAPACK-style (reflector below the diagonal,
-//                 tau, partial column norms downdated and recomputed when
-//                 cancellation sets in)
+//                 the O(m A) work per step runs on the FP32 pipes); one
+//                 launch per column step, in which every CTA picks the pivot
+//                 itself and applies the reflector to its own column,
+//                 LAPACK-style otherwise (tau, partial column norms downdated
+//                 and recomputed when cancellation sets in)
 //   Jacobi        one-sided Jacobi on X = R^T in float (R^T of a pivoted QR is
 //                 graded, so float rotations keep relative accuracy), two-
 //                 level: round-robin rounds of column-block pairs, each pair
@@ -145,11 +145,12 @@ template <int kThreads> __device__ __forceinline__ float2 block_sum_df(float2 v,
 
 constexpr int kQrThreads = 256;
 
-// Squared column norms (partial and reference copy, double) and the identity
-// permutation.  grid (n, n_sino).
+// Squared column norms (partial, by position, in the step-0 half of the
+// double buffer; and the reference copy, by stored column, double) and the
+// identity position map.  grid (n, n_sino).
 __global__ void __launch_bounds__(kQrThreads)
 qr_init_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n,
-               double *__restrict__ norms, double *__restrict__ orig, int *__restrict__ perm) {
+               NosWork w) {
     __shared__ double red[kQrThreads / 32];
     const int j = blockIdx.x, s = blockIdx.y;
     const NosDesc d = desc[s];
@@ -161,50 +162,111 @@ qr_init_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc, i
     }
     v = block_sum<double, kQrThreads>(v, red);
     if (threadIdx.x == 0) {
-        norms[(size_t)s * n + j] = v;
-        orig[(size_t)s * n + j] = v;
-        perm[(size_t)s * n + j] = j;
+        w.norms[(size_t)s * n + j] = v;
+        w.orig[(size_t)s * n + j] = v;
+        w.cmap[(size_t)s * n + j] = j;
     }
 }
 
-// Element slots: thread t holds rows t + kQrThreads u (u < K, K kQrThreads >=
-// m) of a column in registers, so a column is read once with all loads in
-// flight and written once.
+// Most positions one CTA of the column step handles.
+constexpr int kQrMaxCols = 64;
 
-// Step k, one CTA per sinogram: pivot = the remaining column of largest
-// partial norm (lowest index on ties), swapped into place; then the
-// reflector H = I - tau v v^T with H A[k:, k] = (beta, 0, ...): beta on the
-// diagonal, v[1:] below it (v[0] = 1 implicit).  Per step this is O(m), so
-// its arithmetic is plain double.
+// Warp-then-block double-float sum through red[kQrThreads / 32]; one barrier.
+// Consecutive calls must alternate between two red buffers.
+__device__ __forceinline__ float2 qr_block_sum(float2 v, float2 *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = df_add(v, df_shfl_xor(v, o));
+    if (lane == 0)
+        red[warp] = v;
+    __syncthreads();
+    v = red[0];
+#pragma unroll
+    for (int u = 1; u < kQrThreads / 32; u++)
+        v = df_add(v, red[u]);
+    return v;
+}
+
+// Column step k of the pivoted QR in one launch, grid (G, n_sino): CTA b
+// handles positions k + b, k + b + G, ... (G is chosen so that the grid is one
+// wave, and each CTA prefetches its next column while it reduces the current
+// one).
+//
+// Every CTA picks the pivot itself -- the remaining position of largest
+// partial norm, lowest position on ties -- and reads the pivot column
+// x = A[k:, c_p].  The CTA owning position p stores the reflector's scalars
+// (beta = R[k, k], scale = 1 / (alpha - beta), tau); every other column gets
+// H = I - tau v v^T, v = (1, x[k+1:] scale), in place, with
+// v . a = a[k] + scale (x[k+1:] . a[k+1:]), and then its partial norm loses
+// a[k]^2 (recomputed from the column when that leaves less than ~sqrt(eps)
+// of the norm at the last recompute, as LAPACK does).
+//
+// Columns never move: cmap maps positions to stored columns and the pivot
+// swap exchanges two of its entries.  The pivot column is left as it is (its
+// rows above k are R[:k, k], those below k the reflector up to `scale`), so
+// no CTA writes what another reads in the same step; the partial norms (by
+// position) and cmap are double-buffered by step parity.  perm[k] receives
+// the stored column that ends at position k.
+//
+// Element slots: thread t holds rows t + kQrThreads u (u < K, K kQrThreads >=
+// m) of a column in registers, so each column is read once with all loads in
+// flight and written once.  The O(m) sums and updates are double-float; the
+// few scalars double, computed by one lane per warp (FP64 is a slow pipe).
 template <int K>
 __global__ void __launch_bounds__(kQrThreads)
-qr_pivot_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, int k,
-                double *__restrict__ norms, double *__restrict__ orig, int *__restrict__ perm,
-                double *__restrict__ tau) {
-    __shared__ double red[kQrThreads / 32];
-    __shared__ double bv[kQrThreads / 32];
-    __shared__ int bi[kQrThreads / 32];
-    __shared__ int piv;
-    __shared__ double s_alpha;
-    const int s = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, int n_sino,
+               int k, NosWork w) {
+    constexpr int kW = kQrThreads / 32;
+    constexpr bool kPrefetch = K <= 16; // registers for a second column
+    __shared__ long long s_bv[kW];
+    __shared__ int s_bi[kW];
+    __shared__ float2 s_red[2][kW];
+    __shared__ float2 s_red2[kW];
+    __shared__ int s_col[kQrMaxCols];
+    const int s = blockIdx.y, G = gridDim.x, b = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const NosDesc d = desc[s];
     const int m = d.m;
     float2 *As = A + d.a_off;
-    double *nr = norms + (size_t)s * n, *og = orig + (size_t)s * n;
-    int *pm = perm + (size_t)s * n;
-    // argmax of the partial norms over j >= k
-    double best = -1;
+    const size_t cur = (size_t)(k & 1) * n_sino + s, nxt = (size_t)((k + 1) & 1) * n_sino + s;
+    const double *nr = w.norms + cur * n;
+    const int *cm = w.cmap + cur * n;
+    const int j0 = k + b;
+    const int cnt = min((n - j0 + G - 1) / G, kQrMaxCols);
+    for (int t = threadIdx.x; t < cnt; t += kQrThreads)
+        s_col[t] = cm[j0 + t * G];
+
+    // first own column, loaded while the pivot is chosen
+    const int c0 = cm[j0];
+    float2 cv[K];
+    {
+        const float2 *c = As + (size_t)c0 * m;
+#pragma unroll
+        for (int u = 0; u < K; u++) {
+            const int i = threadIdx.x + kQrThreads * u;
+            cv[u] = i > k && i < m ? c[i] : make_float2(0.f, 0.f);
+        }
+    }
+    float2 ck = As[(size_t)c0 * m + k];
+
+    // pivot: argmax of the partial norms over positions k..n-1, compared as
+    // the bit patterns of the (non-negative) doubles on the integer pipe; a
+    // NaN or negative norm counts as 0
+    long long best = -1;
     int bidx = n;
-    for (int j = k + threadIdx.x; j < n; j += kQrThreads) {
-        const double v = nr[j];
-        if (v > best || (v == best && j < bidx)) {
+    for (int jj = k + threadIdx.x; jj < n; jj += kQrThreads) {
+        long long v = __double_as_longlong(nr[jj]);
+        if (v < 0 || v > 0x7FF0000000000000LL)
+            v = 0;
+        if (v > best) { // positions rise per thread: the first maximum stays
             best = v;
-            bidx = j;
+            bidx = jj;
         }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const double ov = __shfl_xor_sync(TT_FULL_MASK, best, o);
+        const long long ov = __shfl_xor_sync(TT_FULL_MASK, best, o);
         const int oi = __shfl_xor_sync(TT_FULL_MASK, bidx, o);
         if (ov > best || (ov == best && oi < bidx)) {
             best = ov;
@@ -212,152 +274,160 @@ qr_pivot_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n,
         }
     }
     if (lane == 0) {
-        bv[warp] = best;
-        bi[warp] = bidx;
+        s_bv[warp] = best;
+        s_bi[warp] = bidx;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double b = bv[0];
-        int ix = bi[0];
-        for (int w = 1; w < kQrThreads / 32; w++)
-            if (bv[w] > b || (bv[w] == b && bi[w] < ix)) {
-                b = bv[w];
-                ix = bi[w];
-            }
-        piv = ix < n ? ix : k;
-    }
-    __syncthreads();
-    const int jp = piv;
-    float2 *x = As + (size_t)k * m;
+    __syncthreads(); // also publishes s_col
+    best = s_bv[0];
+    bidx = s_bi[0];
+#pragma unroll
+    for (int u = 1; u < kW; u++)
+        if (s_bv[u] > best || (s_bv[u] == best && s_bi[u] < bidx)) {
+            best = s_bv[u];
+            bidx = s_bi[u];
+        }
+    const int p = bidx < n ? bidx : k;
+    const int cp = cm[p];
+    const float2 *x = As + (size_t)cp * m;
     float2 xv[K];
-    if (jp != k) {
-        float2 *cb = As + (size_t)jp * m;
-        float2 ov[K];
 #pragma unroll
-        for (int u = 0; u < K; u++) {
-            const int i = threadIdx.x + kQrThreads * u;
-            xv[u] = i < m ? cb[i] : make_float2(0.f, 0.f);
-            ov[u] = i < m ? x[i] : make_float2(0.f, 0.f);
+    for (int u = 0; u < K; u++) {
+        const int i = threadIdx.x + kQrThreads * u;
+        xv[u] = i > k && i < m ? x[i] : make_float2(0.f, 0.f);
+    }
+    const float2 xk = x[k];
+
+    // |x[k+1:]|^2 and, for the first own column, x[k+1:] . a[k+1:]
+    float2 xn = make_float2(0.f, 0.f), xa = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < K; u++) {
+        xn = df_add(xn, df_mul(xv[u], xv[u]));
+        xa = df_add(xa, df_mul(xv[u], cv[u]));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        xn = df_add(xn, df_shfl_xor(xn, o));
+        xa = df_add(xa, df_shfl_xor(xa, o));
+    }
+    if (lane == 0) {
+        s_red[0][warp] = xn;
+        s_red2[warp] = xa;
+    }
+    __syncthreads();
+    xn = s_red[0][0];
+    xa = s_red2[0];
+#pragma unroll
+    for (int u = 1; u < kW; u++) {
+        xn = df_add(xn, s_red[0][u]);
+        xa = df_add(xa, s_red2[u]);
+    }
+    int rb = 1; // s_red[rb] is the next free reduction buffer
+    const bool zero = xn.x == 0.f; // uniform: H = I, x stays as it is
+
+    // reflector scalars in double by lane 0 of each warp, broadcast by shuffle
+    float2 scale_df = make_float2(0.f, 0.f), tau_df = make_float2(0.f, 0.f);
+    if (lane == 0) {
+        const double alpha = df_to_d(xk), x2 = df_to_d(xn);
+        const double beta = zero ? alpha : -copysign(sqrt(alpha * alpha + x2), alpha);
+        const double scale = zero ? 0.0 : 1 / (alpha - beta);
+        const double tau = zero ? 0.0 : (beta - alpha) / beta;
+        if (warp == 0 && (p - k) % G == b) {
+            const size_t o = (size_t)s * n + k;
+            w.beta[o] = beta;
+            w.scale[o] = scale;
+            w.tau[o] = tau;
+            w.perm[o] = cp;
         }
+        scale_df = d_to_df(scale);
+        tau_df = d_to_df(tau);
+    }
+    scale_df = make_float2(__shfl_sync(TT_FULL_MASK, scale_df.x, 0),
+                           __shfl_sync(TT_FULL_MASK, scale_df.y, 0));
+    tau_df = make_float2(__shfl_sync(TT_FULL_MASK, tau_df.x, 0),
+                         __shfl_sync(TT_FULL_MASK, tau_df.y, 0));
+    double *og = w.orig + (size_t)s * n;
+
+    for (int t = 0; t < cnt; t++) {
+        const int j = j0 + t * G, cj = s_col[t];
+        float2 cn[kPrefetch ? K : 1];
+        float2 ckn = make_float2(0.f, 0.f);
+        if (kPrefetch && t + 1 < cnt) {
+            const float2 *c = As + (size_t)s_col[t + 1] * m;
 #pragma unroll
-        for (int u = 0; u < K; u++) {
-            const int i = threadIdx.x + kQrThreads * u;
-            if (i < m) {
-                x[i] = xv[u];
-                cb[i] = ov[u];
+            for (int u = 0; u < (kPrefetch ? K : 1); u++) {
+                const int i = threadIdx.x + kQrThreads * u;
+                cn[u] = i > k && i < m ? c[i] : make_float2(0.f, 0.f);
+            }
+            ckn = c[k];
+        }
+        if (j != p) { // uniform
+            float2 *c = As + (size_t)cj * m;
+            if (t > 0) {
+                float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int u = 0; u < K; u++)
+                    v = df_add(v, df_mul(xv[u], cv[u]));
+                xa = qr_block_sum(v, s_red[rb]);
+                rb ^= 1;
+            }
+            if (!zero) {
+                // a -= tau v (v . a), v . a = a[k] + scale (x[k+1:] . a[k+1:])
+                const float2 vc = df_add(ck, df_mul(scale_df, xa));
+                const float2 ntw = df_neg(df_mul(tau_df, vc));
+                const float2 ntws = df_mul(ntw, scale_df);
+#pragma unroll
+                for (int u = 0; u < K; u++) {
+                    const int i = threadIdx.x + kQrThreads * u;
+                    cv[u] = df_add(cv[u], df_mul(ntws, xv[u]));
+                    if (i > k && i < m)
+                        c[i] = cv[u];
+                }
+                ck = df_add(ck, ntw);
+                if (threadIdx.x == 0)
+                    c[k] = ck;
+            }
+            // partial norm for step k + 1, decided by lane 0 of each warp
+            double n2 = 0;
+            int recompute = 0;
+            if (lane == 0) {
+                const double ckd = df_to_d(ck);
+                n2 = nr[j] - ckd * ckd;
+                recompute = n2 <= 1.5e-8 * og[cj];
+            }
+            if (__shfl_sync(TT_FULL_MASK, recompute, 0)) { // uniform
+                float2 r = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int u = 0; u < K; u++)
+                    r = df_add(r, df_mul(cv[u], cv[u]));
+                r = qr_block_sum(r, s_red[rb]);
+                rb ^= 1;
+                n2 = df_to_d(r);
+                if (threadIdx.x == 0)
+                    og[cj] = n2;
+            }
+            if (threadIdx.x == 0) {
+                const int dest = j == k ? p : j;
+                w.norms[nxt * n + dest] = n2;
+                w.cmap[nxt * n + dest] = cj;
             }
         }
-        if (threadIdx.x == 0) {
-            double t = nr[k];
-            nr[k] = nr[jp];
-            nr[jp] = t;
-            t = og[k];
-            og[k] = og[jp];
-            og[jp] = t;
-            const int q = pm[k];
-            pm[k] = pm[jp];
-            pm[jp] = q;
+        if (t + 1 < cnt) {
+            if (kPrefetch) {
+#pragma unroll
+                for (int u = 0; u < (kPrefetch ? K : 1); u++)
+                    cv[u] = cn[u];
+                ck = ckn;
+            } else {
+                const float2 *c = As + (size_t)s_col[t + 1] * m;
+#pragma unroll
+                for (int u = 0; u < K; u++) {
+                    const int i = threadIdx.x + kQrThreads * u;
+                    cv[u] = i > k && i < m ? c[i] : make_float2(0.f, 0.f);
+                }
+                ck = c[k];
+            }
         }
-    } else {
-#pragma unroll
-        for (int u = 0; u < K; u++) {
-            const int i = threadIdx.x + kQrThreads * u;
-            xv[u] = i < m ? x[i] : make_float2(0.f, 0.f);
-        }
     }
-    // reflector of x = A[k:m, k]
-    double xn = 0;
-#pragma unroll
-    for (int u = 0; u < K; u++) {
-        const int i = threadIdx.x + kQrThreads * u;
-        const double xd = df_to_d(xv[u]);
-        if (i > k && i < m)
-            xn += xd * xd;
-        if (i == k)
-            s_alpha = xd;
-    }
-    xn = block_sum<double, kQrThreads>(xn, red); // its barriers publish s_alpha
-    const double alpha = s_alpha;
-    if (xn == 0) { // already (alpha, 0, ...): H = I
-        if (threadIdx.x == 0)
-            tau[(size_t)s * n + k] = 0;
-        return;
-    }
-    const double beta = -copysign(sqrt(alpha * alpha + xn), alpha);
-    const double scale = 1 / (alpha - beta);
-#pragma unroll
-    for (int u = 0; u < K; u++) {
-        const int i = threadIdx.x + kQrThreads * u;
-        if (i > k && i < m)
-            x[i] = d_to_df(df_to_d(xv[u]) * scale);
-        if (i == k)
-            x[i] = d_to_df(beta);
-    }
-    if (threadIdx.x == 0)
-        tau[(size_t)s * n + k] = (beta - alpha) / beta;
-}
-
-// Step k, one CTA per trailing column j = k + 1 + blockIdx.x: A[k:, j] -=
-// tau v (v . A[k:, j]) in double-float, then the partial norm loses
-// A[k, j]^2 -- recomputed from the column when that leaves less than
-// ~sqrt(eps) of the original.
-template <int K>
-__global__ void __launch_bounds__(kQrThreads)
-qr_update_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, int k,
-                 double *__restrict__ norms, double *__restrict__ orig,
-                 const double *__restrict__ tau) {
-    __shared__ float2 red[kQrThreads / 32];
-    __shared__ double redd[kQrThreads / 32];
-    const int j = k + 1 + blockIdx.x, s = blockIdx.y;
-    const NosDesc d = desc[s];
-    const int m = d.m;
-    float2 *As = A + d.a_off;
-    const float2 *v = As + (size_t)k * m;
-    float2 *c = As + (size_t)j * m;
-    const double t = tau[(size_t)s * n + k];
-    float2 vv[K], cv[K];
-#pragma unroll
-    for (int u = 0; u < K; u++) {
-        const int i = threadIdx.x + kQrThreads * u;
-        const bool in = i > k && i < m;
-        vv[u] = in ? v[i] : make_float2(0.f, 0.f);
-        cv[u] = in ? c[i] : make_float2(0.f, 0.f);
-    }
-    float2 ck = c[k];
-    if (t != 0) { // uniform
-        float2 w = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int u = 0; u < K; u++)
-            w = df_add(w, df_mul(vv[u], cv[u]));
-        w = df_add(block_sum_df<kQrThreads>(w, red), ck);
-        const float2 ntw = df_neg(df_mul(d_to_df(t), w));
-#pragma unroll
-        for (int u = 0; u < K; u++) {
-            const int i = threadIdx.x + kQrThreads * u;
-            cv[u] = df_add(cv[u], df_mul(ntw, vv[u]));
-            if (i > k && i < m)
-                c[i] = cv[u];
-        }
-        ck = df_add(ck, ntw);
-        if (threadIdx.x == 0)
-            c[k] = ck;
-    }
-    double *nr = norms + (size_t)s * n, *og = orig + (size_t)s * n;
-    const double ckd = df_to_d(ck);
-    double n2 = nr[j] - ckd * ckd;
-    if (n2 <= 1.5e-8 * og[j]) { // uniform: every thread holds the same values
-        double r = 0;
-#pragma unroll
-        for (int u = 0; u < K; u++) {
-            const double cd = df_to_d(cv[u]);
-            r += cd * cd;
-        }
-        n2 = block_sum<double, kQrThreads>(r, redd);
-        if (threadIdx.x == 0)
-            og[j] = n2;
-    }
-    if (threadIdx.x == 0)
-        nr[j] = n2;
 }
 
 // ---- one-sided Jacobi on X = R^T (float) ----------------------------------
@@ -372,20 +442,26 @@ constexpr double kNullRel = 1e-15;
 // null-direction bound tiny[s] = (kNullRel R[0, 0])^2.
 // grid (ceil(n * n / 256), n_sino).
 __global__ void nos_rt_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc,
-                              int n, float *__restrict__ X, float *__restrict__ V,
-                              float *__restrict__ tiny) {
+                              int n, NosWork w) {
     const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long nn = (long long)n * n;
     if (e >= nn)
         return;
     const int s = blockIdx.y, i = (int)(e % n), j = (int)(e / n);
     const NosDesc d = desc[s];
+    const double *beta = w.beta + (size_t)s * n;
     if (e == 0) {
-        const double r = kNullRel * df_to_d(A[d.a_off]);
-        tiny[s] = (float)(r * r);
+        const double r = kNullRel * beta[0];
+        w.tiny[s] = (float)(r * r);
     }
-    X[s * nn + e] = j <= i ? (float)df_to_d(A[d.a_off + j + (size_t)i * d.m]) : 0.f;
-    V[s * nn + e] = i == j ? 1.f : 0.f;
+    // R[j, i]: the diagonal from beta, above it the stored column of position i
+    float r = 0.f;
+    if (j == i)
+        r = (float)beta[i];
+    else if (j < i)
+        r = (float)df_to_d(A[d.a_off + j + (size_t)w.perm[(size_t)s * n + i] * d.m]);
+    w.X[s * nn + e] = r;
+    w.V[s * nn + e] = i == j ? 1.f : 0.f;
 }
 
 // A pair is rotated when |x_p . x_q| > kJacTol |x_p| |x_q| -- a few times the
@@ -394,15 +470,26 @@ __global__ void nos_rt_kernel(const float2 *__restrict__ A, const NosDesc *__res
 // kJacDone) ends the iteration.
 constexpr float kJacTol = 1e-6f, kJacDone = 1e-5f;
 
-// Two-level (block) Jacobi.  The n columns form blocks of kBJ; a sweep is a
-// round-robin tournament of the blocks (nbp - 1 rounds for nbp blocks, a bye
-// when odd), and in each outer round a CTA copies its block pair -- 2 kBJ
-// columns of X and of V -- into shared memory and runs one inner sweep over
-// all their pairs (2 kBJ - 1 inner rounds of kBJ disjoint pairs, one warp per
-// pair, __syncthreads between rounds) before writing them back.  A sweep is
-// nbp - 1 launches instead of n - 1, and the rotations are those of the
-// cyclic Jacobi method.
-constexpr int kBJ = 8, kBCols = 2 * kBJ, kBThreads = 32 * kBJ;
+// Two-level (block) Jacobi.  The n columns form blocks of kBJ, and a sweep
+// visits every column pair once, in nbp - 1 launches (rounds of a
+// round-robin tournament of the nbp blocks, a dummy block making nbp even):
+// in each round a CTA copies its block pair -- 2 kBJ columns of X -- into
+// shared memory and rotates the kBJ^2 pairs across the two blocks in kBJ
+// inner rounds of kBJ disjoint pairs (one warp per pair, __syncthreads
+// between inner rounds); the first round of a sweep first rotates the pairs
+// inside each of its two blocks (kBJ - 1 more inner rounds).  A block-cyclic
+// ordering of the cyclic Jacobi method.
+//
+// V does not take part in the inner rounds: their rotations are accumulated
+// into a 2 kBJ x 2 kBJ orthogonal J (in shared memory), and the block's
+// columns of V are multiplied by J once per round, in row chunks staged
+// through shared memory.  Columns sit in shared memory zero-padded to a
+// multiple of 128 rows, so a lane moves 4 consecutive rows per 128-bit
+// access and no row needs a bounds test.  Blocks of 16 keep the grid of 8
+// sinograms of 360 angles within one CTA per SM.
+constexpr int kBJ = 16, kBCols = 2 * kBJ, kBThreads = 32 * kBJ;
+constexpr int kVRows = 256; // rows of V per chunk: 64 groups of 4 rows x 8 groups of 4 columns
+static_assert(kBThreads == (kVRows / 4) * (kBCols / 4), "one 4 x 4 tile of V J per thread");
 
 __device__ __forceinline__ void round_robin(int players, int round, int k, int &p, int &q) {
     const int P1 = players - 1;
@@ -420,116 +507,284 @@ __device__ __forceinline__ void round_robin(int players, int round, int k, int &
     }
 }
 
-// grid (nbp / 2, n_sino), kBThreads threads, dynamic shared memory 2 kBCols n
-// floats.  Lane l holds elements l + 32 u (u < K, 32 K >= n) of a column.
-template <int K>
+// The V block sits whole in shared memory up to 4 slots of 128 rows; larger
+// ones go through a kVRows chunk.
+__host__ __device__ constexpr bool block_round_whole_v(int k4) { return k4 <= 4; }
+
+// Dynamic shared memory of the round kernel with K4 slots of 128 rows
+// (floats): the X block, the V block (or chunk, leading dimension rows + 4)
+// and the two copies of J.
+__host__ __device__ constexpr size_t block_round_smem_floats(int k4) {
+    return (size_t)kBCols * 128 * k4 +
+           (size_t)kBCols * ((block_round_whole_v(k4) ? 128 * k4 : kVRows) + 4) +
+           kBCols * (kBCols + 1) + kBCols * kBCols;
+}
+
+__device__ __forceinline__ float4 f4_lin(float a, float4 x, float b, float4 y) {
+    return make_float4(a * x.x + b * y.x, a * x.y + b * y.y, a * x.z + b * y.z, a * x.w + b * y.w);
+}
+
+// 4-byte asynchronous global -> shared copy; src_bytes 0 writes a zero
+// without reading src.
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, int src_bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src),
+                 "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Columns c of the 2 kBJ block (global column gcol(c), nothing past n) into
+// rows [r0, r0 + rows) of a shared column-major block with leading dimension
+// ld, zero-filled past n, as 4-byte asynchronous copies (coalesced: thread t
+// takes elements t, t + kBThreads, ...).
+template <typename G>
+__device__ __forceinline__ void stage_block_async(float *dst, int ld, const float *src, int n,
+                                                  int r0, int rows, G gcol) {
+    for (int e = threadIdx.x; e < kBCols * rows; e += kBThreads) {
+        const int c = e / rows, r = r0 + e % rows, gc = gcol(c);
+        const bool ok = r < n && gc < n;
+        cp_async4(dst + (size_t)c * ld + (e % rows), ok ? src + (size_t)gc * n + r : src,
+                  ok ? 4 : 0);
+    }
+}
+
+// One Jacobi rotation of the column pair (x, y) held by a warp (lane l
+// holds rows 4 l + 128 u .. + 3): cos of the pair = |x . y| / (|x| |y|);
+// rotated (x and y replaced) unless a column is null (norm^2 <= tn, or a zero
+// column past n) or the pair is already orthogonal to kJacTol.  The
+// rotation parameters come from the (2-ulp) hardware reciprocal square root:
+// the rotation only has to be orthogonal (c^2 + s^2 = 1 to float precision),
+// not exact.  Returns the pair's cos when rotated, else 0.
+template <int K4>
+__device__ __forceinline__ float jacobi_pair(float4 (&x)[K4], float4 (&y)[K4], float tn,
+                                             float &c, float &sn) {
+    float al = 0.f, be = 0.f, ga = 0.f;
+#pragma unroll
+    for (int u = 0; u < K4; u++) {
+        al = fmaf(x[u].x, x[u].x, al);
+        be = fmaf(y[u].x, y[u].x, be);
+        ga = fmaf(x[u].x, y[u].x, ga);
+        al = fmaf(x[u].y, x[u].y, al);
+        be = fmaf(y[u].y, y[u].y, be);
+        ga = fmaf(x[u].y, y[u].y, ga);
+        al = fmaf(x[u].z, x[u].z, al);
+        be = fmaf(y[u].z, y[u].z, be);
+        ga = fmaf(x[u].z, y[u].z, ga);
+        al = fmaf(x[u].w, x[u].w, al);
+        be = fmaf(y[u].w, y[u].w, be);
+        ga = fmaf(x[u].w, y[u].w, ga);
+    }
+    al = warp_sum(al);
+    be = warp_sum(be);
+    ga = warp_sum(ga);
+    const float cosv = fabsf(ga) * (rsqrtf(al) * rsqrtf(be));
+    if (!(al > tn && be > tn && ga != 0.f && cosv > kJacTol))
+        return 0.f; // uniform across the warp
+    const float zeta = __fdividef(be - al, 2.f * ga);
+    const float az = fabsf(zeta);
+    float t;
+    if (az < 1e15f) {
+        const float z2 = fmaf(zeta, zeta, 1.f);
+        t = __fdividef(1.f, az + z2 * rsqrtf(z2));
+    } else {
+        t = __fdividef(0.5f, az);
+    }
+    t = zeta >= 0.f ? t : -t;
+    c = rsqrtf(fmaf(t, t, 1.f));
+    sn = c * t;
+#pragma unroll
+    for (int u = 0; u < K4; u++) {
+        const float4 xo = x[u];
+        x[u] = f4_lin(c, xo, -sn, y[u]);
+        y[u] = f4_lin(sn, xo, c, y[u]);
+    }
+    return cosv;
+}
+
+// grid (nbp / 2, n_sino), kBThreads threads, dynamic shared memory
+// block_round_smem_floats(K4) floats, 128 K4 >= n: lane l holds rows
+// 4 l + 128 u .. + 3 (u < K4) of a column.
+template <int K4>
 __global__ void __launch_bounds__(kBThreads)
 rt_block_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int nbp, int round,
                       unsigned *__restrict__ off_bits, const float *__restrict__ tiny) {
     extern __shared__ __align__(16) float bsm[];
-    float *Xl = bsm, *Vl = bsm + (size_t)kBCols * n;
+    constexpr int NP = 128 * K4; // padded rows
+    constexpr bool kWholeV = block_round_whole_v(K4);
+    constexpr int VR = kWholeV ? NP : kVRows; // rows of the V buffer
+    constexpr int VLD = VR + 4;               // its leading dimension (bank spread)
+    float *Xl = bsm;                          // kBCols x NP
+    float *Vb = Xl + (size_t)kBCols * NP;     // kBCols x VLD
+    float(*Jt)[kBCols + 1] = reinterpret_cast<float(*)[kBCols + 1]>(Vb + kBCols * VLD);
+    float(*Jr)[kBCols] = reinterpret_cast<float(*)[kBCols]>(&Jt[kBCols][0]); // row-major J
     const int s = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nb = (n + kBJ - 1) / kBJ;
     int bp, bq;
     round_robin(nbp, round, blockIdx.x, bp, bq);
-    if (bq >= nb)
-        return; // the bye
+    const bool intra = round == 0; // the sweep's first round also rotates within blocks
+    if (bq >= nb && !intra)
+        return; // the bye (the dummy block's columns are zeros and never rotate)
     const size_t nn = (size_t)n * n;
     float *Xg = X + s * nn, *Vg = V + s * nn;
-    // warp w stages local columns w (block bp) and w + kBJ (block bq) of X and
-    // V, all 4 K loads of a lane in flight at once
-    const int c0 = bp * kBJ + warp, c1 = bq * kBJ + warp;
-    {
-        float a[K], b[K], c[K], d[K];
-#pragma unroll
-        for (int u = 0; u < K; u++) {
-            const int i = lane + 32 * u;
-            a[u] = (i < n && c0 < n) ? Xg[(size_t)c0 * n + i] : 0.f;
-            b[u] = (i < n && c1 < n) ? Xg[(size_t)c1 * n + i] : 0.f;
-            c[u] = (i < n && c0 < n) ? Vg[(size_t)c0 * n + i] : 0.f;
-            d[u] = (i < n && c1 < n) ? Vg[(size_t)c1 * n + i] : 0.f;
-        }
-#pragma unroll
-        for (int u = 0; u < K; u++) {
-            const int i = lane + 32 * u;
-            if (i < n) {
-                Xl[(size_t)warp * n + i] = a[u];
-                Xl[(size_t)(warp + kBJ) * n + i] = b[u];
-                Vl[(size_t)warp * n + i] = c[u];
-                Vl[(size_t)(warp + kBJ) * n + i] = d[u];
-            }
-        }
-    }
+    // global column of local column c
+    auto gcol = [&](int c) { return c < kBJ ? bp * kBJ + c : bq * kBJ + c - kBJ; };
+    // X block (zero-padded to NP rows), then -- in flight during the inner
+    // rounds -- the V block (or its first chunk); J = I
+    stage_block_async(Xl, NP, Xg, n, 0, NP, gcol);
+    cp_async_commit();
+    stage_block_async(Vb, VLD, Vg, n, 0, VR, gcol);
+    cp_async_commit();
+    for (int e = threadIdx.x; e < kBCols * kBCols; e += kBThreads)
+        Jt[e / kBCols][e % kBCols] = e / kBCols == e % kBCols ? 1.f : 0.f;
+    cp_async_wait<1>();
     __syncthreads();
     const float tn = tiny[s];
     float wmax = 0.f;
-    for (int ir = 0; ir < kBCols - 1; ir++) {
-        int p, q;
-        round_robin(kBCols, ir, warp, p, q);
-        float *xp = Xl + (size_t)p * n, *xq = Xl + (size_t)q * n;
-        float x[K], y[K];
+    // J <- J G on columns p, q (row `lane` of each)
+    auto j_rotate = [&](int p, int q, float c, float sn) {
+        const float a = Jt[p][lane], b = Jt[q][lane];
+        Jt[p][lane] = c * a - sn * b;
+        Jt[q][lane] = sn * a + c * b;
+    };
+    float4 x[K4], y[K4];
+    if (intra) {
+        // pairs within each block: warps 0..7 block bp, 8..15 block bq
+        const int half = warp / (kBJ / 2);
+        for (int ir = 0; ir < kBJ - 1; ir++) {
+            int p, q;
+            round_robin(kBJ, ir, warp % (kBJ / 2), p, q);
+            p += half * kBJ;
+            q += half * kBJ;
+            float4 *xp = reinterpret_cast<float4 *>(Xl + (size_t)p * NP);
+            float4 *xq = reinterpret_cast<float4 *>(Xl + (size_t)q * NP);
 #pragma unroll
-        for (int u = 0; u < K; u++) {
-            const int i = lane + 32 * u;
-            x[u] = i < n ? xp[i] : 0.f;
-            y[u] = i < n ? xq[i] : 0.f;
-        }
-        float al = 0.f, be = 0.f, ga = 0.f;
-#pragma unroll
-        for (int u = 0; u < K; u++) {
-            al = fmaf(x[u], x[u], al);
-            be = fmaf(y[u], y[u], be);
-            ga = fmaf(x[u], y[u], ga);
-        }
-        al = warp_sum(al);
-        be = warp_sum(be);
-        ga = warp_sum(ga);
-        // cos of the pair = |ga| / (|x_p| |x_q|); rotation parameters from
-        // the (2-ulp) hardware reciprocal square root: the rotation only has
-        // to be orthogonal (c^2 + s^2 = 1 to float precision), not exact
-        const float cosv = fabsf(ga) * (rsqrtf(al) * rsqrtf(be));
-        // a null direction (or an empty slot past n), or already orthogonal
-        if (al > tn && be > tn && ga != 0.f && cosv > kJacTol) {
-            wmax = fmaxf(wmax, cosv);
-            const float zeta = __fdividef(be - al, 2.f * ga);
-            const float az = fabsf(zeta);
-            float t;
-            if (az < 1e15f) {
-                const float z2 = fmaf(zeta, zeta, 1.f);
-                t = __fdividef(1.f, az + z2 * rsqrtf(z2));
-            } else {
-                t = __fdividef(0.5f, az);
+            for (int u = 0; u < K4; u++) {
+                x[u] = xp[lane + 32 * u];
+                y[u] = xq[lane + 32 * u];
             }
-            t = zeta >= 0.f ? t : -t;
-            const float c = rsqrtf(fmaf(t, t, 1.f)), sn = c * t;
-            float *vp = Vl + (size_t)p * n, *vq = Vl + (size_t)q * n;
+            float c, sn;
+            const float cosv = jacobi_pair<K4>(x, y, tn, c, sn);
+            if (cosv > 0.f) {
+                wmax = fmaxf(wmax, cosv);
 #pragma unroll
-            for (int u = 0; u < K; u++) {
-                const int i = lane + 32 * u;
-                if (i < n) {
-                    const float a = vp[i], b = vq[i];
-                    xp[i] = c * x[u] - sn * y[u];
-                    xq[i] = sn * x[u] + c * y[u];
-                    vp[i] = c * a - sn * b;
-                    vq[i] = sn * a + c * b;
+                for (int u = 0; u < K4; u++) {
+                    xp[lane + 32 * u] = x[u];
+                    xq[lane + 32 * u] = y[u];
                 }
+                j_rotate(p, q, c, sn);
             }
+            __syncthreads();
+        }
+    }
+    // pairs across the blocks: in inner round r warp w pairs column w of bp
+    // (kept in registers throughout) with column (w + r) % kBJ of bq
+    float4 *xw = reinterpret_cast<float4 *>(Xl + (size_t)warp * NP);
+#pragma unroll
+    for (int u = 0; u < K4; u++)
+        x[u] = xw[lane + 32 * u];
+    for (int r = 0; r < kBJ; r++) {
+        const int q = kBJ + (warp + r) % kBJ;
+        float4 *xq = reinterpret_cast<float4 *>(Xl + (size_t)q * NP);
+#pragma unroll
+        for (int u = 0; u < K4; u++)
+            y[u] = xq[lane + 32 * u];
+        float c, sn;
+        const float cosv = jacobi_pair<K4>(x, y, tn, c, sn);
+        if (cosv > 0.f) {
+            wmax = fmaxf(wmax, cosv);
+#pragma unroll
+            for (int u = 0; u < K4; u++)
+                xq[lane + 32 * u] = y[u];
+            j_rotate(warp, q, c, sn);
         }
         __syncthreads();
     }
+#pragma unroll
+    for (int u = 0; u < K4; u++)
+        xw[lane + 32 * u] = x[u];
+    __syncthreads();
     if (lane == 0 && wmax > 0.f)
         atomicMax(off_bits + s, __float_as_uint(wmax));
+    // X block back (coalesced: thread t takes elements t, t + kBThreads, ...)
+    for (int e = threadIdx.x; e < kBCols * NP; e += kBThreads) {
+        const int c = e / NP, r = e % NP, gc = gcol(c);
+        if (r < n && gc < n)
+            Xg[(size_t)gc * n + r] = Xl[e];
+    }
+    for (int e = threadIdx.x; e < kBCols * kBCols; e += kBThreads)
+        Jr[e / kBCols][e % kBCols] = Jt[e % kBCols][e / kBCols];
+
+    // V block <- V block J, kVRows rows per pass: thread t computes rows
+    // 4 (t / 8) .. + 3 and columns 4 (t % 8) .. + 3 of each pass
+    const int cg = (threadIdx.x % 8) * 4, rg = (threadIdx.x / 8) * 4;
+    auto vj_tile = [&](const float *vb, int ld, float (&acc)[4][4]) {
 #pragma unroll
-    for (int u = 0; u < K; u++) {
-        const int i = lane + 32 * u;
-        if (i < n) {
-            if (c0 < n) {
-                Xg[(size_t)c0 * n + i] = Xl[(size_t)warp * n + i];
-                Vg[(size_t)c0 * n + i] = Vl[(size_t)warp * n + i];
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int v = 0; v < 4; v++)
+                acc[u][v] = 0.f;
+#pragma unroll 8
+        for (int i = 0; i < kBCols; i++) {
+            const float4 vin = *reinterpret_cast<const float4 *>(vb + (size_t)i * ld + rg);
+            const float4 jr = *reinterpret_cast<const float4 *>(&Jr[i][cg]);
+            const float vi[4] = {vin.x, vin.y, vin.z, vin.w}, ji[4] = {jr.x, jr.y, jr.z, jr.w};
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++)
+                    acc[u][v] = fmaf(vi[u], ji[v], acc[u][v]);
+        }
+    };
+    auto put_tile = [&](float *vb, int ld, const float (&acc)[4][4]) {
+#pragma unroll
+        for (int v = 0; v < 4; v++)
+            *reinterpret_cast<float4 *>(vb + (size_t)(cg + v) * ld + rg) =
+                make_float4(acc[0][v], acc[1][v], acc[2][v], acc[3][v]);
+    };
+    if constexpr (kWholeV) {
+        constexpr int kPasses = (NP + kVRows - 1) / kVRows; // 1 or 2
+        cp_async_wait<0>();
+        __syncthreads(); // V block and Jr in place
+        float acc[kPasses][4][4];
+#pragma unroll
+        for (int ps = 0; ps < kPasses; ps++)
+            if (ps * kVRows + rg < NP)
+                vj_tile(Vb + ps * kVRows, VLD, acc[ps]);
+        __syncthreads(); // every thread has read Vb
+#pragma unroll
+        for (int ps = 0; ps < kPasses; ps++)
+            if (ps * kVRows + rg < NP)
+                put_tile(Vb + ps * kVRows, VLD, acc[ps]);
+        __syncthreads();
+        for (int e = threadIdx.x; e < kBCols * NP; e += kBThreads) {
+            const int c = e / NP, r = e % NP, gc = gcol(c);
+            if (r < n && gc < n)
+                Vg[(size_t)gc * n + r] = Vb[(size_t)c * VLD + r];
+        }
+    } else {
+        for (int r0 = 0; r0 < n; r0 += kVRows) {
+            if (r0 > 0) {
+                __syncthreads(); // the previous chunk is written out
+                stage_block_async(Vb, VLD, Vg, n, r0, kVRows, gcol);
+                cp_async_commit();
             }
-            if (c1 < n) {
-                Xg[(size_t)c1 * n + i] = Xl[(size_t)(warp + kBJ) * n + i];
-                Vg[(size_t)c1 * n + i] = Vl[(size_t)(warp + kBJ) * n + i];
+            cp_async_wait<0>();
+            __syncthreads(); // chunk and Jr in place
+            float acc[4][4];
+            vj_tile(Vb, VLD, acc);
+            __syncthreads(); // every thread has read the chunk
+            put_tile(Vb, VLD, acc);
+            __syncthreads();
+            for (int e = threadIdx.x; e < kBCols * kVRows; e += kBThreads) {
+                const int c = e / kVRows, r = r0 + e % kVRows, gc = gcol(c);
+                if (r < n && gc < n)
+                    Vg[(size_t)gc * n + r] = Vb[(size_t)c * VLD + e % kVRows];
             }
         }
     }
@@ -611,8 +866,9 @@ constexpr int kQThreads = 256, kQCols = 4; // columns of Y per CTA
 // grid (ceil(n / kQCols), n_sino).
 __global__ void __launch_bounds__(kQThreads)
 nos_apply_q_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc,
-                   const double *__restrict__ tau, const int *__restrict__ perm,
-                   const float *__restrict__ P, int n, float *__restrict__ out) {
+                   const double *__restrict__ tau, const double *__restrict__ scale,
+                   const int *__restrict__ perm, const float *__restrict__ P, int n,
+                   float *__restrict__ out) {
     extern __shared__ __align__(16) unsigned char smraw[];
     float *y = reinterpret_cast<float *>(smraw);
     __shared__ float red[kQThreads / 32][kQCols];
@@ -625,19 +881,22 @@ nos_apply_q_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ des
         for (int i = threadIdx.x; i < m; i += kQThreads)
             y[c * m + i] = (c < nc && i < n) ? P[s * nn + i + (size_t)(j0 + c) * n] : 0.f;
     const float2 *As = A + d.a_off;
-    const double *ts = tau + (size_t)s * n;
+    const double *ts = tau + (size_t)s * n, *sc = scale + (size_t)s * n;
+    const int *pm = perm + (size_t)s * n;
     for (int k = n - 1; k >= 0; k--) {
         const float t = (float)ts[k];
         if (t == 0.f)
             continue; // uniform
-        const float2 *v = As + (size_t)k * m;
+        // reflector k: v = (1, x[k+1:] scale[k]), x the stored pivot column
+        const float2 *v = As + (size_t)pm[k] * m;
+        const float vs = (float)sc[k];
         __syncthreads();
         float w[kQCols];
 #pragma unroll
         for (int c = 0; c < kQCols; c++)
             w[c] = 0.f;
         for (int i = k + 1 + threadIdx.x; i < m; i += kQThreads) {
-            const float vi = (v[i].x + v[i].y);
+            const float vi = (v[i].x + v[i].y) * vs;
 #pragma unroll
             for (int c = 0; c < kQCols; c++)
                 w[c] = fmaf(vi, y[c * m + i], w[c]);
@@ -658,7 +917,7 @@ nos_apply_q_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ des
         }
         __syncthreads(); // everyone has read y[.., k] and red
         for (int i = k + 1 + threadIdx.x; i < m; i += kQThreads) {
-            const float vi = (v[i].x + v[i].y);
+            const float vi = (v[i].x + v[i].y) * vs;
 #pragma unroll
             for (int c = 0; c < kQCols; c++)
                 y[c * m + i] = fmaf(-w[c], vi, y[c * m + i]);
@@ -667,7 +926,6 @@ nos_apply_q_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ des
             y[threadIdx.x * m + k] -= w[threadIdx.x];
     }
     __syncthreads();
-    const int *pm = perm + (size_t)s * n;
     for (int c = 0; c < nc; c++) {
         float *o = out + d.out_off + (size_t)pm[j0 + c] * m;
         for (int i = threadIdx.x; i < m; i += kQThreads)
@@ -700,12 +958,17 @@ cudaError_t launch_nos_align(const float *sino, int rows, int cols, int n_sino,
 template <int K>
 static void qr_steps(float2 *A, const NosDesc *desc, int n, int n_sino, const NosWork &w,
                      cudaStream_t st) {
+    // CTAs per sinogram: one wave over all sinograms, at most kQrMaxCols
+    // positions per CTA
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_step_kernel<K>, kQrThreads, 0);
+    const int wave = std::max(1, sms * std::max(per_sm, 1) / std::max(n_sino, 1));
     for (int k = 0; k < n; k++) {
-        qr_pivot_kernel<K><<<n_sino, kQrThreads, 0, st>>>(A, desc, n, k, w.norms, w.orig, w.perm,
-                                                          w.tau);
-        if (k + 1 < n)
-            qr_update_kernel<K><<<dim3(n - k - 1, n_sino), kQrThreads, 0, st>>>(
-                A, desc, n, k, w.norms, w.orig, w.tau);
+        const int left = n - k;
+        const int g = std::min(left, std::max(wave, (left + kQrMaxCols - 1) / kQrMaxCols));
+        qr_step_kernel<K><<<dim3(g, n_sino), kQrThreads, 0, st>>>(A, desc, n, n_sino, k, w);
     }
 }
 
@@ -715,7 +978,7 @@ cudaError_t launch_nos_factor(float2 *A, const NosDesc *desc, int n, int n_sino,
                               const NosWork &w, cudaStream_t st) {
     if (max_m > nos_max_rows())
         return cudaErrorInvalidValue;
-    qr_init_kernel<<<dim3(n, n_sino), kQrThreads, 0, st>>>(A, desc, n, w.norms, w.orig, w.perm);
+    qr_init_kernel<<<dim3(n, n_sino), kQrThreads, 0, st>>>(A, desc, n, w);
     if (max_m <= 8 * kQrThreads)
         qr_steps<8>(A, desc, n, n_sino, w, st);
     else if (max_m <= 16 * kQrThreads)
@@ -723,29 +986,30 @@ cudaError_t launch_nos_factor(float2 *A, const NosDesc *desc, int n, int n_sino,
     else
         qr_steps<32>(A, desc, n, n_sino, w, st);
     const long long nn = (long long)n * n;
-    nos_rt_kernel<<<dim3((unsigned)((nn + 255) / 256), n_sino), 256, 0, st>>>(A, desc, n, w.X,
-                                                                              w.V, w.tiny);
+    nos_rt_kernel<<<dim3((unsigned)((nn + 255) / 256), n_sino), 256, 0, st>>>(A, desc, n, w);
     return cudaGetLastError();
 }
 
-template <int K> static cudaError_t block_rounds(int n, int n_sino, const NosWork &w,
-                                                 cudaStream_t st) {
+template <int K4>
+static cudaError_t block_rounds(int n, int n_sino, const NosWork &w, cudaStream_t st) {
     const int nb = (n + kBJ - 1) / kBJ, nbp = nb + (nb & 1);
-    const size_t smem = sizeof(float) * 2 * kBCols * (size_t)n;
+    const size_t smem = sizeof(float) * block_round_smem_floats(K4);
+    if (128 * K4 < n)
+        return cudaErrorInvalidValue;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(rt_block_round_kernel<K>,
+        cudaError_t e = cudaFuncSetAttribute(rt_block_round_kernel<K4>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)dynamic_smem_limit(
-                                                 (const void *)rt_block_round_kernel<K>));
+                                                 (const void *)rt_block_round_kernel<K4>));
         if (e != cudaSuccess)
             return e;
         attr = true;
     }
-    if (smem > dynamic_smem_limit((const void *)rt_block_round_kernel<K>))
+    if (smem > dynamic_smem_limit((const void *)rt_block_round_kernel<K4>))
         return cudaErrorInvalidValue;
     for (int r = 0; r < nbp - 1; r++)
-        rt_block_round_kernel<K><<<dim3(nbp / 2, n_sino), kBThreads, smem, st>>>(
+        rt_block_round_kernel<K4><<<dim3(nbp / 2, n_sino), kBThreads, smem, st>>>(
             w.X, w.V, n, nbp, r, w.off_bits, w.tiny);
     return cudaGetLastError();
 }
@@ -754,16 +1018,18 @@ cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, cudaStream_t s
     cudaError_t e = cudaMemsetAsync(w.off_bits, 0, sizeof(unsigned) * n_sino, st);
     if (e != cudaSuccess)
         return e;
+    if (n <= 128)
+        return block_rounds<1>(n, n_sino, w, st);
     if (n <= 256)
-        return block_rounds<8>(n, n_sino, w, st);
+        return block_rounds<2>(n, n_sino, w, st);
     if (n <= 384)
-        return block_rounds<12>(n, n_sino, w, st);
+        return block_rounds<3>(n, n_sino, w, st);
     if (n <= 512)
-        return block_rounds<16>(n, n_sino, w, st);
+        return block_rounds<4>(n, n_sino, w, st);
     if (n <= 768)
-        return block_rounds<24>(n, n_sino, w, st);
+        return block_rounds<6>(n, n_sino, w, st);
     if (n <= 1024)
-        return block_rounds<32>(n, n_sino, w, st);
+        return block_rounds<8>(n, n_sino, w, st);
     return cudaErrorInvalidValue; // more than 1024 angles
 }
 
@@ -797,7 +1063,7 @@ cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int
     if (smem > limit)
         return cudaErrorInvalidValue;
     nos_apply_q_kernel<<<dim3((n + kQCols - 1) / kQCols, n_sino), kQThreads, smem, st>>>(
-        A, desc, w.tau, w.perm, w.V, n, out);
+        A, desc, w.tau, w.scale, w.perm, w.V, n, out);
     return cudaGetLastError();
 }
 
