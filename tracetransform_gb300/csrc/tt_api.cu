@@ -640,20 +640,21 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
                     tt::nos_max_rows());
     if (cols > 1024)
         return fail(TT_ERR_UNSUPPORTED, "orthonormal circus of %d angles exceeds 1024", cols);
-    // scratch: 6 double + 3 int vectors of n, 3 float n x n matrices, 1 float vector
+    // scratch: 5 double-float + 3 int vectors of n, 3 float n x n matrices,
+    // 2 float vectors
     const size_t nv = ncol, nm = (size_t)cols * cols * n_sino;
-    TT_CHECK(p->ensure(p->nos_work, sizeof(double) * 6 * nv + sizeof(int) * 3 * nv +
-                                        sizeof(float) * (3 * nm + nv) + sizeof(unsigned) * n_sino +
-                                        sizeof(float) * n_sino + 64));
+    TT_CHECK(p->ensure(p->nos_work, sizeof(float2) * 5 * nv + sizeof(int) * 3 * nv +
+                                        sizeof(float) * (3 * nm + 2 * nv) +
+                                        sizeof(unsigned) * n_sino + sizeof(float) * n_sino + 64));
     tt::NosWork w;
     {
         char *q = (char *)p->nos_work.p;
-        w.norms = (double *)q;
-        w.orig = w.norms + 2 * nv;
-        w.tau = w.orig + nv;
+        w.norms = (float2 *)q;
+        w.tau = w.norms + 2 * nv;
         w.beta = w.tau + nv;
         w.scale = w.beta + nv;
-        w.X = (float *)(w.scale + nv);
+        w.orig = (float *)(w.scale + nv);
+        w.X = w.orig + nv;
         w.V = w.X + nm;
         w.P = w.V + nm;
         w.inv = w.P + nm;

@@ -104,8 +104,9 @@ struct NosDesc {
 };
 // Per-call scratch of the nearest orthonormal sinogram (n = angles).
 struct NosWork {
-    double *norms;              // 2 x n_sino x n: QR partial norms by stored column, by step parity
-    double *orig, *tau, *beta, *scale; // n_sino x n each (norms at the last recompute, reflectors)
+    float2 *norms;              // 2 x n_sino x n: QR partial norms by position, by step parity
+    float *orig;                // n_sino x n: norm at the last recompute, by stored column
+    float2 *tau, *beta, *scale; // n_sino x n each: the reflectors (double-float)
     int *cmap;                  // 2 x n_sino x n: position -> stored column, by step parity
     int *perm;                  // n_sino x n: stored column that ends at each position
     float *X, *V, *P;           // n_sino x n x n each (R^T, Jacobi V, polar(R))

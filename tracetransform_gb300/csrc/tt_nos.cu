@@ -66,8 +66,10 @@ __global__ void nos_offsets_kernel(const float *__restrict__ sino, int rows, int
 // floats (~48 significant bits).  The QR's O(m n) work -- dot products and
 // trailing updates -- runs on these pairs with error-free float transforms
 // (Knuth's two-sum, the FMA two-product, Dekker's renormalisation), i.e. on
-// the FP32 pipes, which GB300 runs far faster than FP64.  Scalars (norms,
-// reflector coefficients) stay in double.
+// the FP32 pipes, which GB300 runs far faster than FP64; so do the scalars
+// (norms, reflector coefficients, with double-float division and square
+// root): a handful of FP64 operations per column step, each waiting on the
+// narrow FP64 pipe, cost more than the step's O(m n) double-float work.
 
 __device__ __forceinline__ float2 df_quick(float a, float b) { // |a| >= |b|
     const float s = a + b;
@@ -85,11 +87,32 @@ __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
     e = fmaf(a.y, b.x, e);
     return df_quick(p, e);
 }
+// acc + a b with the product's rounding error carried into the low word
+// instead of renormalising the product first
+__device__ __forceinline__ float2 df_fma(float2 a, float2 b, float2 acc) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    const float s = acc.x + p, bb = s - acc.x;
+    const float err = (acc.x - (s - bb)) + (p - bb);
+    return df_quick(s, err + e + acc.y);
+}
 __device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ double df_to_d(float2 a) { return (double)a.x + (double)a.y; }
-__device__ __forceinline__ float2 d_to_df(double d) {
-    const float hi = __double2float_rn(d);
-    return make_float2(hi, __double2float_rn(d - (double)hi));
+__device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, df_neg(b)); }
+// a / b: float quotient, corrected once by the double-float remainder
+__device__ __forceinline__ float2 df_div(float2 a, float2 b) {
+    const float q1 = a.x / b.x;
+    const float2 r = df_sub(a, df_mul(make_float2(q1, 0.f), b));
+    return df_quick(q1, r.x / b.x);
+}
+// sqrt(a), a >= 0: float root, corrected once by the double-float residual
+__device__ __forceinline__ float2 df_sqrt(float2 a) {
+    if (!(a.x > 0.f))
+        return make_float2(0.f, 0.f);
+    const float r0 = sqrtf(a.x);
+    const float2 res = df_sub(a, df_mul(make_float2(r0, 0.f), make_float2(r0, 0.f)));
+    return df_quick(r0, res.x / (2.f * r0));
 }
 __device__ __forceinline__ float2 df_shfl_xor(float2 v, int o) {
     return make_float2(__shfl_xor_sync(TT_FULL_MASK, v.x, o),
@@ -146,24 +169,22 @@ template <int kThreads> __device__ __forceinline__ float2 block_sum_df(float2 v,
 constexpr int kQrThreads = 256;
 
 // Squared column norms (partial, by position, in the step-0 half of the
-// double buffer; and the reference copy, by stored column, double) and the
-// identity position map.  grid (n, n_sino).
+// double buffer, double-float; and the reference copy, by stored column,
+// float) and the identity position map.  grid (n, n_sino).
 __global__ void __launch_bounds__(kQrThreads)
 qr_init_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n,
                NosWork w) {
-    __shared__ double red[kQrThreads / 32];
+    __shared__ float2 red[kQrThreads / 32];
     const int j = blockIdx.x, s = blockIdx.y;
     const NosDesc d = desc[s];
     const float2 *a = A + d.a_off + (size_t)j * d.m;
-    double v = 0;
-    for (int i = threadIdx.x; i < d.m; i += kQrThreads) {
-        const double x = df_to_d(a[i]);
-        v += x * x;
-    }
-    v = block_sum<double, kQrThreads>(v, red);
+    float2 v = make_float2(0.f, 0.f);
+    for (int i = threadIdx.x; i < d.m; i += kQrThreads)
+        v = df_fma(a[i], a[i], v);
+    v = block_sum_df<kQrThreads>(v, red);
     if (threadIdx.x == 0) {
         w.norms[(size_t)s * n + j] = v;
-        w.orig[(size_t)s * n + j] = v;
+        w.orig[(size_t)s * n + j] = v.x;
         w.cmap[(size_t)s * n + j] = j;
     }
 }
@@ -171,9 +192,9 @@ qr_init_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc, i
 // Most positions one CTA of the column step handles.
 constexpr int kQrMaxCols = 64;
 
-// Warp-then-block double-float sum through red[kQrThreads / 32]; one barrier.
+// Warp-then-block double-float sum through red[T / 32]; one barrier.
 // Consecutive calls must alternate between two red buffers.
-__device__ __forceinline__ float2 qr_block_sum(float2 v, float2 *red) {
+template <int T> __device__ __forceinline__ float2 qr_block_sum(float2 v, float2 *red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
@@ -183,7 +204,7 @@ __device__ __forceinline__ float2 qr_block_sum(float2 v, float2 *red) {
     __syncthreads();
     v = red[0];
 #pragma unroll
-    for (int u = 1; u < kQrThreads / 32; u++)
+    for (int u = 1; u < T / 32; u++)
         v = df_add(v, red[u]);
     return v;
 }
@@ -209,33 +230,43 @@ __device__ __forceinline__ float2 qr_block_sum(float2 v, float2 *red) {
 // position) and cmap are double-buffered by step parity.  perm[k] receives
 // the stored column that ends at position k.
 //
-// Element slots: thread t holds rows t + kQrThreads u (u < K, K kQrThreads >=
+// Element slots: thread t holds rows k + 1 + t + kQrThreads u (u < K, K kQrThreads >=
 // m) of a column in registers, so each column is read once with all loads in
-// flight and written once.  The O(m) sums and updates are double-float; the
-// few scalars double, computed by one lane per warp (FP64 is a slow pipe).
-template <int K>
-__global__ void __launch_bounds__(kQrThreads)
+// flight and written once.  Sums, updates and scalars are all double-float;
+// the scalars are computed by one lane per warp.
+template <int K, int T>
+__global__ void __launch_bounds__(T)
 qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, int n_sino,
                int k, NosWork w) {
-    constexpr int kW = kQrThreads / 32;
+    constexpr int kW = T / 32;
     constexpr bool kPrefetch = K <= 16; // registers for a second column
-    __shared__ long long s_bv[kW];
+    __shared__ int s_bv[kW];
     __shared__ int s_bi[kW];
     __shared__ float2 s_red[2][kW];
     __shared__ float2 s_red2[kW];
     __shared__ int s_col[kQrMaxCols];
+    __shared__ float2 s_nr[kQrMaxCols];
+    __shared__ float s_og[kQrMaxCols];
     const int s = blockIdx.y, G = gridDim.x, b = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const NosDesc d = desc[s];
     const int m = d.m;
+    // slot (t, u) of a column holds row k + 1 + t + T u; keff slots
+    // cover the rows below the diagonal
+    const int keff = (m - k - 1 + T - 1) / T;
     float2 *As = A + d.a_off;
     const size_t cur = (size_t)(k & 1) * n_sino + s, nxt = (size_t)((k + 1) & 1) * n_sino + s;
-    const double *nr = w.norms + cur * n;
+    const float2 *nr = w.norms + cur * n;
     const int *cm = w.cmap + cur * n;
     const int j0 = k + b;
     const int cnt = min((n - j0 + G - 1) / G, kQrMaxCols);
-    for (int t = threadIdx.x; t < cnt; t += kQrThreads)
-        s_col[t] = cm[j0 + t * G];
+    // per own column: stored column, partial norm and recompute threshold
+    for (int t = threadIdx.x; t < cnt; t += T) {
+        const int c = cm[j0 + t * G];
+        s_col[t] = c;
+        s_nr[t] = nr[j0 + t * G];
+        s_og[t] = w.orig[(size_t)s * n + c];
+    }
 
     // first own column, loaded while the pivot is chosen
     const int c0 = cm[j0];
@@ -244,20 +275,20 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
         const float2 *c = As + (size_t)c0 * m;
 #pragma unroll
         for (int u = 0; u < K; u++) {
-            const int i = threadIdx.x + kQrThreads * u;
-            cv[u] = i > k && i < m ? c[i] : make_float2(0.f, 0.f);
+            const int i = k + 1 + threadIdx.x + T * u;
+            cv[u] = u < keff && i < m ? c[i] : make_float2(0.f, 0.f);
         }
     }
     float2 ck = As[(size_t)c0 * m + k];
 
     // pivot: argmax of the partial norms over positions k..n-1, compared as
-    // the bit patterns of the (non-negative) doubles on the integer pipe; a
-    // NaN or negative norm counts as 0
-    long long best = -1;
+    // the bit patterns of their (non-negative) high words on the integer
+    // pipe; a NaN or negative norm counts as 0
+    int best = -1;
     int bidx = n;
-    for (int jj = k + threadIdx.x; jj < n; jj += kQrThreads) {
-        long long v = __double_as_longlong(nr[jj]);
-        if (v < 0 || v > 0x7FF0000000000000LL)
+    for (int jj = k + threadIdx.x; jj < n; jj += T) {
+        int v = __float_as_int(nr[jj].x);
+        if (v < 0 || v > 0x7F800000)
             v = 0;
         if (v > best) { // positions rise per thread: the first maximum stays
             best = v;
@@ -266,7 +297,7 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const long long ov = __shfl_xor_sync(TT_FULL_MASK, best, o);
+        const int ov = __shfl_xor_sync(TT_FULL_MASK, best, o);
         const int oi = __shfl_xor_sync(TT_FULL_MASK, bidx, o);
         if (ov > best || (ov == best && oi < bidx)) {
             best = ov;
@@ -292,18 +323,19 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
     float2 xv[K];
 #pragma unroll
     for (int u = 0; u < K; u++) {
-        const int i = threadIdx.x + kQrThreads * u;
-        xv[u] = i > k && i < m ? x[i] : make_float2(0.f, 0.f);
+        const int i = k + 1 + threadIdx.x + T * u;
+        xv[u] = u < keff && i < m ? x[i] : make_float2(0.f, 0.f);
     }
     const float2 xk = x[k];
 
     // |x[k+1:]|^2 and, for the first own column, x[k+1:] . a[k+1:]
     float2 xn = make_float2(0.f, 0.f), xa = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int u = 0; u < K; u++) {
-        xn = df_add(xn, df_mul(xv[u], xv[u]));
-        xa = df_add(xa, df_mul(xv[u], cv[u]));
-    }
+    for (int u = 0; u < K; u++)
+        if (u < keff) {
+            xn = df_fma(xv[u], xv[u], xn);
+            xa = df_fma(xv[u], cv[u], xa);
+        }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         xn = df_add(xn, df_shfl_xor(xn, o));
@@ -324,28 +356,30 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
     int rb = 1; // s_red[rb] is the next free reduction buffer
     const bool zero = xn.x == 0.f; // uniform: H = I, x stays as it is
 
-    // reflector scalars in double by lane 0 of each warp, broadcast by shuffle
+    // reflector scalars (double-float, no FP64: GB300's FP64 pipe would
+    // serialise them) by lane 0 of each warp, broadcast by shuffle
     float2 scale_df = make_float2(0.f, 0.f), tau_df = make_float2(0.f, 0.f);
     if (lane == 0) {
-        const double alpha = df_to_d(xk), x2 = df_to_d(xn);
-        const double beta = zero ? alpha : -copysign(sqrt(alpha * alpha + x2), alpha);
-        const double scale = zero ? 0.0 : 1 / (alpha - beta);
-        const double tau = zero ? 0.0 : (beta - alpha) / beta;
+        float2 beta = xk;
+        if (!zero) {
+            const float2 root = df_sqrt(df_fma(xk, xk, xn));
+            beta = xk.x >= 0.f ? df_neg(root) : root;
+            scale_df = df_div(make_float2(1.f, 0.f), df_sub(xk, beta));
+            tau_df = df_div(df_sub(beta, xk), beta);
+        }
         if (warp == 0 && (p - k) % G == b) {
             const size_t o = (size_t)s * n + k;
             w.beta[o] = beta;
-            w.scale[o] = scale;
-            w.tau[o] = tau;
+            w.scale[o] = scale_df;
+            w.tau[o] = tau_df;
             w.perm[o] = cp;
         }
-        scale_df = d_to_df(scale);
-        tau_df = d_to_df(tau);
     }
     scale_df = make_float2(__shfl_sync(TT_FULL_MASK, scale_df.x, 0),
                            __shfl_sync(TT_FULL_MASK, scale_df.y, 0));
     tau_df = make_float2(__shfl_sync(TT_FULL_MASK, tau_df.x, 0),
                          __shfl_sync(TT_FULL_MASK, tau_df.y, 0));
-    double *og = w.orig + (size_t)s * n;
+    float *og = w.orig + (size_t)s * n;
 
     for (int t = 0; t < cnt; t++) {
         const int j = j0 + t * G, cj = s_col[t];
@@ -355,8 +389,8 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
             const float2 *c = As + (size_t)s_col[t + 1] * m;
 #pragma unroll
             for (int u = 0; u < (kPrefetch ? K : 1); u++) {
-                const int i = threadIdx.x + kQrThreads * u;
-                cn[u] = i > k && i < m ? c[i] : make_float2(0.f, 0.f);
+                const int i = k + 1 + threadIdx.x + T * u;
+                cn[u] = u < keff && i < m ? c[i] : make_float2(0.f, 0.f);
             }
             ckn = c[k];
         }
@@ -366,8 +400,9 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
                 float2 v = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int u = 0; u < K; u++)
-                    v = df_add(v, df_mul(xv[u], cv[u]));
-                xa = qr_block_sum(v, s_red[rb]);
+                    if (u < keff)
+                        v = df_fma(xv[u], cv[u], v);
+                xa = qr_block_sum<T>(v, s_red[rb]);
                 rb ^= 1;
             }
             if (!zero) {
@@ -377,9 +412,10 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
                 const float2 ntws = df_mul(ntw, scale_df);
 #pragma unroll
                 for (int u = 0; u < K; u++) {
-                    const int i = threadIdx.x + kQrThreads * u;
-                    cv[u] = df_add(cv[u], df_mul(ntws, xv[u]));
-                    if (i > k && i < m)
+                    const int i = k + 1 + threadIdx.x + T * u;
+                    if (u < keff)
+                        cv[u] = df_fma(ntws, xv[u], cv[u]);
+                    if (u < keff && i < m)
                         c[i] = cv[u];
                 }
                 ck = df_add(ck, ntw);
@@ -387,23 +423,23 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
                     c[k] = ck;
             }
             // partial norm for step k + 1, decided by lane 0 of each warp
-            double n2 = 0;
+            float2 n2 = make_float2(0.f, 0.f);
             int recompute = 0;
             if (lane == 0) {
-                const double ckd = df_to_d(ck);
-                n2 = nr[j] - ckd * ckd;
-                recompute = n2 <= 1.5e-8 * og[cj];
+                n2 = df_sub(s_nr[t], df_mul(ck, ck));
+                recompute = n2.x <= 1.5e-8f * s_og[t];
             }
             if (__shfl_sync(TT_FULL_MASK, recompute, 0)) { // uniform
                 float2 r = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int u = 0; u < K; u++)
-                    r = df_add(r, df_mul(cv[u], cv[u]));
-                r = qr_block_sum(r, s_red[rb]);
+                    if (u < keff)
+                        r = df_fma(cv[u], cv[u], r);
+                r = qr_block_sum<T>(r, s_red[rb]);
                 rb ^= 1;
-                n2 = df_to_d(r);
+                n2 = r;
                 if (threadIdx.x == 0)
-                    og[cj] = n2;
+                    og[cj] = n2.x;
             }
             if (threadIdx.x == 0) {
                 const int dest = j == k ? p : j;
@@ -421,8 +457,8 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
                 const float2 *c = As + (size_t)s_col[t + 1] * m;
 #pragma unroll
                 for (int u = 0; u < K; u++) {
-                    const int i = threadIdx.x + kQrThreads * u;
-                    cv[u] = i > k && i < m ? c[i] : make_float2(0.f, 0.f);
+                    const int i = k + 1 + threadIdx.x + T * u;
+                    cv[u] = u < keff && i < m ? c[i] : make_float2(0.f, 0.f);
                 }
                 ck = c[k];
             }
@@ -436,7 +472,7 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
 // largest column norm of the aligned matrix) are below the double precision
 // of the input: they take no rotations and no part in U, as the oracle
 // treats exactly-zero directions.
-constexpr double kNullRel = 1e-15;
+constexpr float kNullRel = 1e-15f;
 
 // X[i + j n] = R[j, i] (upper triangle of the QR result), V = I, and the
 // null-direction bound tiny[s] = (kNullRel R[0, 0])^2.
@@ -449,17 +485,19 @@ __global__ void nos_rt_kernel(const float2 *__restrict__ A, const NosDesc *__res
         return;
     const int s = blockIdx.y, i = (int)(e % n), j = (int)(e / n);
     const NosDesc d = desc[s];
-    const double *beta = w.beta + (size_t)s * n;
+    const float2 *beta = w.beta + (size_t)s * n;
     if (e == 0) {
-        const double r = kNullRel * beta[0];
-        w.tiny[s] = (float)(r * r);
+        const float r = kNullRel * (beta[0].x + beta[0].y);
+        w.tiny[s] = r * r;
     }
     // R[j, i]: the diagonal from beta, above it the stored column of position i
     float r = 0.f;
     if (j == i)
-        r = (float)beta[i];
-    else if (j < i)
-        r = (float)df_to_d(A[d.a_off + j + (size_t)w.perm[(size_t)s * n + i] * d.m]);
+        r = beta[i].x + beta[i].y;
+    else if (j < i) {
+        const float2 a = A[d.a_off + j + (size_t)w.perm[(size_t)s * n + i] * d.m];
+        r = a.x + a.y;
+    }
     w.X[s * nn + e] = r;
     w.V[s * nn + e] = i == j ? 1.f : 0.f;
 }
@@ -866,7 +904,7 @@ constexpr int kQThreads = 256, kQCols = 4; // columns of Y per CTA
 // grid (ceil(n / kQCols), n_sino).
 __global__ void __launch_bounds__(kQThreads)
 nos_apply_q_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc,
-                   const double *__restrict__ tau, const double *__restrict__ scale,
+                   const float2 *__restrict__ tau, const float2 *__restrict__ scale,
                    const int *__restrict__ perm, const float *__restrict__ P, int n,
                    float *__restrict__ out) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -881,15 +919,15 @@ nos_apply_q_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ des
         for (int i = threadIdx.x; i < m; i += kQThreads)
             y[c * m + i] = (c < nc && i < n) ? P[s * nn + i + (size_t)(j0 + c) * n] : 0.f;
     const float2 *As = A + d.a_off;
-    const double *ts = tau + (size_t)s * n, *sc = scale + (size_t)s * n;
+    const float2 *ts = tau + (size_t)s * n, *sc = scale + (size_t)s * n;
     const int *pm = perm + (size_t)s * n;
     for (int k = n - 1; k >= 0; k--) {
-        const float t = (float)ts[k];
+        const float t = ts[k].x + ts[k].y;
         if (t == 0.f)
             continue; // uniform
         // reflector k: v = (1, x[k+1:] scale[k]), x the stored pivot column
         const float2 *v = As + (size_t)pm[k] * m;
-        const float vs = (float)sc[k];
+        const float vs = sc[k].x + sc[k].y;
         __syncthreads();
         float w[kQCols];
 #pragma unroll
@@ -955,7 +993,7 @@ cudaError_t launch_nos_align(const float *sino, int rows, int cols, int n_sino,
     return cudaGetLastError();
 }
 
-template <int K>
+template <int K, int T>
 static void qr_steps(float2 *A, const NosDesc *desc, int n, int n_sino, const NosWork &w,
                      cudaStream_t st) {
     // CTAs per sinogram: one wave over all sinograms, at most kQrMaxCols
@@ -963,12 +1001,12 @@ static void qr_steps(float2 *A, const NosDesc *desc, int n, int n_sino, const No
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_step_kernel<K>, kQrThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_step_kernel<K, T>, T, 0);
     const int wave = std::max(1, sms * std::max(per_sm, 1) / std::max(n_sino, 1));
     for (int k = 0; k < n; k++) {
         const int left = n - k;
         const int g = std::min(left, std::max(wave, (left + kQrMaxCols - 1) / kQrMaxCols));
-        qr_step_kernel<K><<<dim3(g, n_sino), kQrThreads, 0, st>>>(A, desc, n, n_sino, k, w);
+        qr_step_kernel<K, T><<<dim3(g, n_sino), T, 0, st>>>(A, desc, n, n_sino, k, w);
     }
 }
 
@@ -979,12 +1017,16 @@ cudaError_t launch_nos_factor(float2 *A, const NosDesc *desc, int n, int n_sino,
     if (max_m > nos_max_rows())
         return cudaErrorInvalidValue;
     qr_init_kernel<<<dim3(n, n_sino), kQrThreads, 0, st>>>(A, desc, n, w);
-    if (max_m <= 8 * kQrThreads)
-        qr_steps<8>(A, desc, n, n_sino, w, st);
+    // 128-thread CTAs up to 2048 rows (more CTAs, and so more column chains,
+    // in flight per SM), 256 above
+    if (max_m <= 12 * 128)
+        qr_steps<12, 128>(A, desc, n, n_sino, w, st);
+    else if (max_m <= 16 * 128)
+        qr_steps<16, 128>(A, desc, n, n_sino, w, st);
     else if (max_m <= 16 * kQrThreads)
-        qr_steps<16>(A, desc, n, n_sino, w, st);
+        qr_steps<16, kQrThreads>(A, desc, n, n_sino, w, st);
     else
-        qr_steps<32>(A, desc, n, n_sino, w, st);
+        qr_steps<32, kQrThreads>(A, desc, n, n_sino, w, st);
     const long long nn = (long long)n * n;
     nos_rt_kernel<<<dim3((unsigned)((nn + 255) / 256), n_sino), 256, 0, st>>>(A, desc, n, w);
     return cudaGetLastError();
