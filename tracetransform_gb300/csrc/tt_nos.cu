@@ -577,18 +577,68 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Columns c of the 2 kBJ block (global column gcol(c), nothing past n) into
-// rows [r0, r0 + rows) of a shared column-major block with leading dimension
-// ld, zero-filled past n, as 4-byte asynchronous copies (coalesced: thread t
-// takes elements t, t + kBThreads, ...).
+// 16-byte asynchronous copy of src_bytes (0 or 16) bytes, zero-filling the rest.
+__device__ __forceinline__ void cp_async16(float *dst, const float *src, int src_bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src),
+                 "r"(src_bytes)
+                 : "memory");
+}
+
+// Rows [r0, r0 + rows) of the 2 kBJ columns of the block (global column
+// gcol(c), none past n) into a shared column-major block with leading
+// dimension ld, zero-filled past n, as asynchronous copies: warp w takes
+// local columns w and w + kBJ, its lanes consecutive rows -- 16 bytes at a
+// time when n is a multiple of 4 (every column then starts 16-byte
+// aligned, given a 16-byte aligned matrix), else 4.  rows and r0 are
+// multiples of 4.
 template <typename G>
-__device__ __forceinline__ void stage_block_async(float *dst, int ld, const float *src, int n,
-                                                  int r0, int rows, G gcol) {
-    for (int e = threadIdx.x; e < kBCols * rows; e += kBThreads) {
-        const int c = e / rows, r = r0 + e % rows, gc = gcol(c);
-        const bool ok = r < n && gc < n;
-        cp_async4(dst + (size_t)c * ld + (e % rows), ok ? src + (size_t)gc * n + r : src,
-                  ok ? 4 : 0);
+__device__ __forceinline__ void stage_cols_async(float *dst, int ld, const float *src, int n,
+                                                 int r0, int rows, G gcol) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool vec = (n & 3) == 0 && ((uintptr_t)src & 15) == 0;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int c = warp + kBJ * h, gc = gcol(c);
+        float *d = dst + (size_t)c * ld;
+        const float *g = src + (size_t)(gc < n ? gc : 0) * n;
+        if (vec) {
+            for (int q = lane; q < rows / 4; q += 32) {
+                const int r = r0 + 4 * q;
+                const bool ok = gc < n && r < n;
+                cp_async16(d + 4 * q, ok ? g + r : src, ok ? 16 : 0);
+            }
+        } else {
+            for (int q = lane; q < rows; q += 32) {
+                const int r = r0 + q;
+                const bool ok = gc < n && r < n;
+                cp_async4(d + q, ok ? g + r : src, ok ? 4 : 0);
+            }
+        }
+    }
+}
+
+// The inverse of stage_cols_async (plain stores, none past n).
+template <typename G>
+__device__ __forceinline__ void store_cols(float *dst, const float *sm, int ld, int n, int r0,
+                                           int rows, G gcol) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool vec = (n & 3) == 0 && ((uintptr_t)dst & 15) == 0;
+    const int lim = min(rows, n - r0); // rows of the block inside the matrix
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int c = warp + kBJ * h, gc = gcol(c);
+        if (gc >= n)
+            continue;
+        const float *l = sm + (size_t)c * ld;
+        float *g = dst + (size_t)gc * n + r0;
+        if (vec) {
+            for (int q = lane; 4 * q < lim; q += 32)
+                *reinterpret_cast<float4 *>(g + 4 * q) = *reinterpret_cast<const float4 *>(l + 4 * q);
+        } else {
+            for (int q = lane; q < lim; q += 32)
+                g[q] = l[q];
+        }
     }
 }
 
@@ -674,9 +724,9 @@ rt_block_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int n
     auto gcol = [&](int c) { return c < kBJ ? bp * kBJ + c : bq * kBJ + c - kBJ; };
     // X block (zero-padded to NP rows), then -- in flight during the inner
     // rounds -- the V block (or its first chunk); J = I
-    stage_block_async(Xl, NP, Xg, n, 0, NP, gcol);
+    stage_cols_async(Xl, NP, Xg, n, 0, NP, gcol);
     cp_async_commit();
-    stage_block_async(Vb, VLD, Vg, n, 0, VR, gcol);
+    stage_cols_async(Vb, VLD, Vg, n, 0, VR, gcol);
     cp_async_commit();
     for (int e = threadIdx.x; e < kBCols * kBCols; e += kBThreads)
         Jt[e / kBCols][e % kBCols] = e / kBCols == e % kBCols ? 1.f : 0.f;
@@ -749,12 +799,8 @@ rt_block_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int n
     __syncthreads();
     if (lane == 0 && wmax > 0.f)
         atomicMax(off_bits + s, __float_as_uint(wmax));
-    // X block back (coalesced: thread t takes elements t, t + kBThreads, ...)
-    for (int e = threadIdx.x; e < kBCols * NP; e += kBThreads) {
-        const int c = e / NP, r = e % NP, gc = gcol(c);
-        if (r < n && gc < n)
-            Xg[(size_t)gc * n + r] = Xl[e];
-    }
+    // X block back
+    store_cols(Xg, Xl, NP, n, 0, NP, gcol);
     for (int e = threadIdx.x; e < kBCols * kBCols; e += kBThreads)
         Jr[e / kBCols][e % kBCols] = Jt[e % kBCols][e / kBCols];
 
@@ -800,16 +846,12 @@ rt_block_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int n
             if (ps * kVRows + rg < NP)
                 put_tile(Vb + ps * kVRows, VLD, acc[ps]);
         __syncthreads();
-        for (int e = threadIdx.x; e < kBCols * NP; e += kBThreads) {
-            const int c = e / NP, r = e % NP, gc = gcol(c);
-            if (r < n && gc < n)
-                Vg[(size_t)gc * n + r] = Vb[(size_t)c * VLD + r];
-        }
+        store_cols(Vg, Vb, VLD, n, 0, NP, gcol);
     } else {
         for (int r0 = 0; r0 < n; r0 += kVRows) {
             if (r0 > 0) {
                 __syncthreads(); // the previous chunk is written out
-                stage_block_async(Vb, VLD, Vg, n, r0, kVRows, gcol);
+                stage_cols_async(Vb, VLD, Vg, n, r0, kVRows, gcol);
                 cp_async_commit();
             }
             cp_async_wait<0>();
@@ -819,11 +861,7 @@ rt_block_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int n
             __syncthreads(); // every thread has read the chunk
             put_tile(Vb, VLD, acc);
             __syncthreads();
-            for (int e = threadIdx.x; e < kBCols * kVRows; e += kBThreads) {
-                const int c = e / kVRows, r = r0 + e % kVRows, gc = gcol(c);
-                if (r < n && gc < n)
-                    Vg[(size_t)gc * n + r] = Vb[(size_t)c * VLD + e % kVRows];
-            }
+            store_cols(Vg, Vb, VLD, n, r0, kVRows, gcol);
         }
     }
 }
