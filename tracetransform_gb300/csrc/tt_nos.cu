@@ -936,6 +936,7 @@ rt_gemm_kernel(const float *__restrict__ A, int ai, int ak, const float *__restr
 }
 
 constexpr int kQThreads = 256, kQCols = 4; // columns of Y per CTA
+constexpr int kNosMaxCols = 1024;              // angles the orthonormal circus takes
 
 // Y = Q [P; 0] = H_0 H_1 ... H_{n-1} [P; 0] for kQCols columns of P per CTA
 // (shared memory: kQCols x m floats), then out[:, perm[j]] = Y[:, j].
@@ -1006,6 +1007,111 @@ nos_apply_q_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ des
         float *o = out + d.out_off + (size_t)pm[j0 + c] * m;
         for (int i = threadIdx.x; i < m; i += kQThreads)
             o[i] = y[c * m + i];
+    }
+}
+
+// The same product with Y held in registers, for m <= K kQThreads: thread t
+// owns rows t + kQThreads u (u < K) of the kQCols columns, so applying a
+// reflector needs one block reduction (double-buffered: one barrier) and no
+// other exchange; the next reflector's column is loaded while the current
+// one is applied, and the reflector scalars sit in shared memory.  Slot
+// (t, u) of reflector k holds v_i for i = t + kQThreads u: 1 at i = k, the
+// scaled pivot column below it, 0 above.
+template <int K>
+__global__ void __launch_bounds__(kQThreads)
+nos_apply_q_reg_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc,
+                       const float2 *__restrict__ tau, const float2 *__restrict__ scale,
+                       const int *__restrict__ perm, const float *__restrict__ P, int n,
+                       float *__restrict__ out) {
+    __shared__ float s_t[kNosMaxCols], s_vs[kNosMaxCols];
+    __shared__ int s_pm[kNosMaxCols];
+    __shared__ float red[2][kQThreads / 32][kQCols];
+    const int s = blockIdx.y, j0 = blockIdx.x * kQCols;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const NosDesc d = desc[s];
+    const int m = d.m, nc = min(kQCols, n - j0);
+    const size_t nn = (size_t)n * n;
+    for (int k = threadIdx.x; k < n; k += kQThreads) {
+        const float2 t = tau[(size_t)s * n + k], v = scale[(size_t)s * n + k];
+        s_t[k] = t.x + t.y;
+        s_vs[k] = v.x + v.y;
+        s_pm[k] = perm[(size_t)s * n + k];
+    }
+    float y[kQCols][K];
+#pragma unroll
+    for (int u = 0; u < K; u++) {
+        const int i = threadIdx.x + kQThreads * u;
+#pragma unroll
+        for (int c = 0; c < kQCols; c++)
+            y[c][u] = (c < nc && i < n) ? P[s * nn + i + (size_t)(j0 + c) * n] : 0.f;
+    }
+    __syncthreads(); // scalars in place
+    const float2 *As = A + d.a_off;
+    auto load_v = [&](int k, float(&v)[K]) {
+        const float2 *x = As + (size_t)s_pm[k] * m;
+        const float vs = s_vs[k];
+#pragma unroll
+        for (int u = 0; u < K; u++) {
+            const int i = threadIdx.x + kQThreads * u;
+            float vi = 0.f;
+            if (i > k && i < m) {
+                const float2 xi = x[i];
+                vi = (xi.x + xi.y) * vs;
+            } else if (i == k) {
+                vi = 1.f;
+            }
+            v[u] = vi;
+        }
+    };
+    float v[K], vn[K];
+    load_v(n - 1, v);
+    int rb = 0;
+    for (int k = n - 1; k >= 0; k--) {
+        if (k > 0)
+            load_v(k - 1, vn);
+        const float t = s_t[k];
+        if (t != 0.f) { // uniform
+            float w[kQCols];
+#pragma unroll
+            for (int c = 0; c < kQCols; c++) {
+                w[c] = 0.f;
+#pragma unroll
+                for (int u = 0; u < K; u++)
+                    w[c] = fmaf(v[u], y[c][u], w[c]);
+                w[c] = warp_sum(w[c]);
+            }
+            if (lane == 0)
+#pragma unroll
+                for (int c = 0; c < kQCols; c++)
+                    red[rb][warp][c] = w[c];
+            __syncthreads();
+#pragma unroll
+            for (int c = 0; c < kQCols; c++) {
+                float tot = 0.f;
+#pragma unroll
+                for (int q = 0; q < kQThreads / 32; q++)
+                    tot += red[rb][q][c];
+                w[c] = t * tot;
+            }
+            rb ^= 1;
+#pragma unroll
+            for (int u = 0; u < K; u++)
+#pragma unroll
+                for (int c = 0; c < kQCols; c++)
+                    y[c][u] = fmaf(-w[c], v[u], y[c][u]);
+        }
+#pragma unroll
+        for (int u = 0; u < K; u++)
+            v[u] = vn[u];
+    }
+    for (int c = 0; c < nc; c++) {
+        float *o = out + d.out_off + (size_t)s_pm[j0 + c] * m;
+#pragma unroll
+        for (int u = 0; u < K; u++) {
+            const int i = threadIdx.x + kQThreads * u;
+            if (i < m)
+                o[i] = y[c][u];
+        }
     }
 }
 
@@ -1130,6 +1236,17 @@ cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int
     rt_gemm_kernel<<<gt, 256, 0, st>>>(w.V, 1, n, w.X, n, 1, nullptr, 1.f, 0.f, n, w.P);
     rt_gemm_kernel<<<gt, 256, 0, st>>>(w.P, n, 1, w.P, 1, n, nullptr, 1.f, 0.f, n, w.X);
     rt_gemm_kernel<<<gt, 256, 0, st>>>(w.P, 1, n, w.X, 1, n, w.P, -0.5f, 1.5f, n, w.V);
+    const dim3 gq((n + kQCols - 1) / kQCols, n_sino);
+    if (n <= kNosMaxCols && max_m <= 8 * kQThreads) {
+        nos_apply_q_reg_kernel<8><<<gq, kQThreads, 0, st>>>(A, desc, w.tau, w.scale, w.perm,
+                                                             w.V, n, out);
+        return cudaGetLastError();
+    }
+    if (n <= kNosMaxCols && max_m <= 16 * kQThreads) {
+        nos_apply_q_reg_kernel<16><<<gq, kQThreads, 0, st>>>(A, desc, w.tau, w.scale, w.perm,
+                                                              w.V, n, out);
+        return cudaGetLastError();
+    }
     static size_t limit = 0;
     if (limit == 0) {
         limit = dynamic_smem_limit((const void *)nos_apply_q_kernel);
