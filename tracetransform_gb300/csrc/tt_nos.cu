@@ -65,7 +65,9 @@ __global__ void nos_offsets_kernel(const float *__restrict__ sino, int rows, int
 // The aligned matrices hold each element as an unevaluated sum hi + lo of two
 // floats (~48 significant bits).  The QR's O(m n) work -- dot products and
 // trailing updates -- runs on these pairs with error-free float transforms
-// (Knuth's two-sum, the FMA two-product, Dekker's renormalisation), i.e. on
+// (Knuth's two-sum, the FMA two-product, Dekker's renormalisation; the
+// products that feed a two-sum are __fmul_rn, which the compiler never
+// contracts into a fused multiply-add), i.e. on
 // the FP32 pipes, which GB300 runs far faster than FP64; so do the scalars
 // (norms, reflector coefficients, with double-float division and square
 // root): a handful of FP64 operations per column step, each waiting on the
@@ -81,7 +83,7 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
     return df_quick(s, e + a.y + b.y);
 }
 __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
-    const float p = a.x * b.x;
+    const float p = __fmul_rn(a.x, b.x); // never contracted into a later add
     float e = fmaf(a.x, b.x, -p);
     e = fmaf(a.x, b.y, e);
     e = fmaf(a.y, b.x, e);
@@ -90,7 +92,7 @@ __device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
 // acc + a b with the product's rounding error carried into the low word
 // instead of renormalising the product first
 __device__ __forceinline__ float2 df_fma(float2 a, float2 b, float2 acc) {
-    const float p = a.x * b.x;
+    const float p = __fmul_rn(a.x, b.x); // never contracted into a later add
     float e = fmaf(a.x, b.x, -p);
     e = fmaf(a.x, b.y, e);
     e = fmaf(a.y, b.x, e);
@@ -98,6 +100,23 @@ __device__ __forceinline__ float2 df_fma(float2 a, float2 b, float2 acc) {
     const float err = (acc.x - (s - bb)) + (p - bb);
     return df_quick(s, err + e + acc.y);
 }
+// Compensated dot product of double-float vectors (Ogita, Rump and Oishi's
+// Dot2, extended by the low-word cross terms): the high words' products go
+// into s with Knuth's two-sum, whose errors, the products' FMA rounding
+// errors and the cross terms collect in e; only s + p is on the dependent
+// path per element.  df_dot_end renormalises.
+struct DfDot {
+    float s = 0.f, e = 0.f;
+};
+__device__ __forceinline__ void df_dot_add(DfDot &d, float2 a, float2 b) {
+    const float p = __fmul_rn(a.x, b.x); // never contracted into a later add
+    const float pe = fmaf(a.x, b.x, -p);
+    const float t = d.s + p, bb = t - d.s;
+    const float err = (d.s - (t - bb)) + (p - bb);
+    d.e += (err + pe) + fmaf(a.x, b.y, a.y * b.x);
+    d.s = t;
+}
+__device__ __forceinline__ float2 df_dot_end(DfDot d) { return df_quick(d.s, d.e); }
 __device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, df_neg(b)); }
 // a / b: float quotient, corrected once by the double-float remainder
@@ -329,13 +348,18 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
     const float2 xk = x[k];
 
     // |x[k+1:]|^2 and, for the first own column, x[k+1:] . a[k+1:]
-    float2 xn = make_float2(0.f, 0.f), xa = make_float2(0.f, 0.f);
+    float2 xn, xa;
+    {
+        DfDot dn[2], da[2];
 #pragma unroll
-    for (int u = 0; u < K; u++)
-        if (u < keff) {
-            xn = df_fma(xv[u], xv[u], xn);
-            xa = df_fma(xv[u], cv[u], xa);
-        }
+        for (int u = 0; u < K; u++)
+            if (u < keff) {
+                df_dot_add(dn[u & 1], xv[u], xv[u]);
+                df_dot_add(da[u & 1], xv[u], cv[u]);
+            }
+        xn = df_add(df_dot_end(dn[0]), df_dot_end(dn[1]));
+        xa = df_add(df_dot_end(da[0]), df_dot_end(da[1]));
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         xn = df_add(xn, df_shfl_xor(xn, o));
@@ -397,12 +421,12 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
         if (j != p) { // uniform
             float2 *c = As + (size_t)cj * m;
             if (t > 0) {
-                float2 v = make_float2(0.f, 0.f);
+                DfDot dv[2];
 #pragma unroll
                 for (int u = 0; u < K; u++)
                     if (u < keff)
-                        v = df_fma(xv[u], cv[u], v);
-                xa = qr_block_sum<T>(v, s_red[rb]);
+                        df_dot_add(dv[u & 1], xv[u], cv[u]);
+                xa = qr_block_sum<T>(df_add(df_dot_end(dv[0]), df_dot_end(dv[1])), s_red[rb]);
                 rb ^= 1;
             }
             if (!zero) {
@@ -430,12 +454,12 @@ qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, 
                 recompute = n2.x <= 1.5e-8f * s_og[t];
             }
             if (__shfl_sync(TT_FULL_MASK, recompute, 0)) { // uniform
-                float2 r = make_float2(0.f, 0.f);
+                DfDot dr[2];
 #pragma unroll
                 for (int u = 0; u < K; u++)
                     if (u < keff)
-                        r = df_fma(cv[u], cv[u], r);
-                r = qr_block_sum<T>(r, s_red[rb]);
+                        df_dot_add(dr[u & 1], cv[u], cv[u]);
+                const float2 r = qr_block_sum<T>(df_add(df_dot_end(dr[0]), df_dot_end(dr[1])), s_red[rb]);
                 rb ^= 1;
                 n2 = r;
                 if (threadIdx.x == 0)
