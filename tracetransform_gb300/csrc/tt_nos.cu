@@ -5,7 +5,9 @@
 // (m = N + padding) and replaces it by the polar factor U V^T of its SVD,
 // computed by Eigen's float JacobiSVD with a column-pivoting Householder QR
 // preconditioner.  Here, for n_sino sinograms at once, the same structure
-// with the precision split that GB300's rates call for (FP64 ~1/64 of FP32):
+// with the precision split that GB300's rates call for: no FP64 at all
+// (its pipe is narrow enough that a few scalar FP64 operations per step
+// dominate), double-float pairs on the FP32 pipes where float is too short:
 //
 //   nos_offsets   per column: weighted median row - center, with the
 //                 reference's sequential float sums (one thread per column)
@@ -16,18 +18,19 @@
 //                 singular directions that a float factorisation would lose;
 //                 the O(m A) work per step runs on the FP32 pipes); one
 //                 launch per column step, in which every CTA picks the pivot
-//                 itself and applies the reflector to its own column,
+//                 itself and applies the reflector to its own columns,
 //                 LAPACK-style otherwise (tau, partial column norms downdated
 //                 and recomputed when cancellation sets in)
 //   Jacobi        one-sided Jacobi on X = R^T in float (R^T of a pivoted QR is
-//                 graded, so float rotations keep relative accuracy), two-
-//                 level: round-robin rounds of column-block pairs, each pair
-//                 swept in one CTA's shared memory, V accumulated;
+//                 graded, so float rotations keep relative accuracy), block-
+//                 cyclic: round-robin rounds of 16-column block pairs, each
+//                 pair rotated in one CTA's shared memory with V updated once
+//                 per round through the accumulated rotation;
 //                 X V = U_X S, so polar(R) = V U_X^T
 //   assemble      P = V U_X^T (float) with one Newton-Schulz step to clean
 //                 its orthogonality, then polar(A P) = Q [P; 0] applied
-//                 reflector by reflector per group of columns in shared
-//                 memory, and the column permutation undone
+//                 reflector by reflector to groups of columns held in
+//                 registers, and the column permutation undone
 //
 // Against the oracle's double one-sided Jacobi on the aligned matrix the
 // result agrees to ~3e-5 absolute (entries up to ~0.7) for condition numbers
