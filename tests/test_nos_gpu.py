@@ -99,3 +99,30 @@ def test_orthonormal_circus_rejects():
     wide = torch.rand((1, 1030, 1100), device="cuda")  # more angles than the Jacobi holds
     with pytest.raises(TTError):
         eng.circus_orthonormal(wide, [1])
+
+
+def _bump_sinogram(rows, cols, seed):
+    """Positive synthetic sinogram: a Gaussian ridge whose centre moves with
+    the angle (as a point's trace does), plus uniform noise."""
+    rng = np.random.default_rng(seed)
+    r = np.arange(rows, dtype=np.float64)[:, None]
+    a = np.arange(cols, dtype=np.float64)[None, :]
+    centre = rows / 2 + rows / 6 * np.sin(2 * np.pi * a / cols)
+    ridge = np.exp(-((r - centre) ** 2) / (2 * (rows / 10) ** 2))
+    return np.asfortranarray((ridge + 0.05 * rng.random((rows, cols))).astype(np.float32))
+
+
+# (rows, angles): the aligned rows m select the QR and Q [P; 0] kernels
+# (m <= 1536, <= 2048, <= 4096, above), the angle count the Jacobi round's
+# slots per lane (<= 128, 256, 384, 512, 768) and its 16- or 4-byte staging
+# (angle count a multiple of 4 or not)
+@pytest.mark.parametrize("rows,cols", [(1300, 150), (1700, 150), (2300, 200), (4300, 96),
+                                       (600, 500), (760, 718)])
+def test_nos_kernel_variants_vs_oracle(oracle_lib, rows, cols):
+    sino = _bump_sinogram(rows, cols, seed=rows + cols)
+    got, c = tt.nearest_orthonormal_sinogram(sino)
+    want, wc = oracle_lib.nos(sino)
+    assert got.shape == want.shape and c == wc
+    g = got.astype(np.float64)
+    assert np.abs(g.T @ g - np.eye(cols)).max() < 1e-4
+    assert np.abs(got - want).max() < 1e-4
