@@ -307,19 +307,14 @@ __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long
                 im5 = fmaf(w.y, v, im5);
             }
         }
-        // hypot of the two float integrals in double, as C's hypot does
-        if (w3) {
-            const double re = warp_sum(re3), im = warp_sum(im3);
-            r345[0] = (float)sqrt(re * re + im * im);
-        }
-        if (w4) {
-            const double re = warp_sum(re4), im = warp_sum(im4);
-            r345[1] = (float)sqrt(re * re + im * im);
-        }
-        if (w5) {
-            const double re = warp_sum(re5), im = warp_sum(im5);
-            r345[2] = (float)sqrt(re * re + im * im);
-        }
+        // hypot of the two float integrals (CUDA's hypotf: no FP64, whose
+        // narrow pipe every lane of every line would otherwise queue on)
+        if (w3)
+            r345[0] = hypotf(warp_sum(re3), warp_sum(im3));
+        if (w4)
+            r345[1] = hypotf(warp_sum(re4), warp_sum(im4));
+        if (w5)
+            r345[2] = hypotf(warp_sum(re5), warp_sum(im5));
     }
 
     float r6v = 0.f, r7v = 0.f;
