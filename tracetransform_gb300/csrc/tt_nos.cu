@@ -154,22 +154,6 @@ __global__ void nos_align_kernel(const float *__restrict__ sino, int rows, int c
         dst[r] = make_float2(src[r], 0.f);
 }
 
-template <typename T, int kThreads> __device__ __forceinline__ T block_sum(T v, T *red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_xor_sync(TT_FULL_MASK, v, o);
-    if (lane == 0)
-        red[warp] = v;
-    __syncthreads();
-    T t = 0;
-#pragma unroll
-    for (int w = 0; w < kThreads / 32; w++)
-        t += red[w];
-    __syncthreads();
-    return t;
-}
-
 template <int kThreads> __device__ __forceinline__ float2 block_sum_df(float2 v, float2 *red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
