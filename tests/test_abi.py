@@ -85,3 +85,5 @@ def test_compute_without_gpu_raises(lib):
         pytest.skip("a GPU is present")
     with pytest.raises(_native.TTError):
         tt.getSinograms(np.zeros((5, 5), np.float32), 1, ["0"])
+    with pytest.raises(_native.TTError):
+        tt.resize(np.zeros((5, 5), np.float32), 3, 3)
