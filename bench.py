@@ -398,12 +398,12 @@ def run_engine(args, world, rank, local_rank):
     kern_s = (sum(kern_ms) / len(kern_ms)) / 1e3
     achieved = alg_bytes / kern_s / 1e9
     line = {
-        "metric": METRIC, "value": world * len(tfs) / (ms / 1e3), "unit": "sinograms/s",
+        "metric": METRIC, "value": job_rate(len(tfs), world, ms), "unit": "sinograms/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded blob+noise, the reference ships no images)",
         "config": config_dict(args.workload, n, angles, tfs, pfs, world),
-        "e2e": {"value": world * len(tfs) / e2e_s, "unit": "sinograms/s",
+        "e2e": {"value": job_rate(len(tfs), world, e2e_s * 1e3), "unit": "sinograms/s",
                 "h2d_bytes_per_step": int(rows * cols * 4),
                 "d2h_bytes_per_step": int(2 * (n_out + h_herm.numel()) * 4)},
         "gpu_launches": launches,
@@ -585,12 +585,12 @@ def run_batch(args, world, rank, local_rank):
         out_floats += len(BATCH_T) * len(BATCH_P) * a
     achieved = alg / (ms / 1e3) / 1e9
     line = {
-        "metric": METRIC, "value": world * n_sino / (ms / 1e3), "unit": "sinograms/s",
+        "metric": METRIC, "value": job_rate(n_sino, world, ms), "unit": "sinograms/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded blob+noise, the reference ships no images)",
         "config": batch_config(imgs, steps, world),
-        "e2e": {"value": world * n_sino / e2e_s, "unit": "sinograms/s",
+        "e2e": {"value": job_rate(n_sino, world, e2e_s * 1e3), "unit": "sinograms/s",
                 "h2d_bytes_per_step": int(flat_h.nbytes),
                 "d2h_bytes_per_step": int(2 * 4 * out_floats)},
         "plain_per_image": {"value": n_sino / (plain_ms / 1e3), "unit": "sinograms/s",
@@ -600,7 +600,7 @@ def run_batch(args, world, rank, local_rank):
                                     "tt_circus_device + tt_zscore_device per image; e2e: one "
                                     "tt_transform (host buffers) per image"},
         "batched_over_plain": plain_ms / ms,
-        "images_per_s": world * len(imgs) / (ms / 1e3),
+        "images_per_s": job_rate(len(imgs), world, ms),
         "gpu_launches": 3 * args.steps,
         "roofline": {"bound": "hbm", "kernel": "batch graph (sino + circus + zscore)",
                      "achieved": achieved, "peak": peak, "peak_source": peak_kind,
@@ -771,15 +771,15 @@ def run_grad(args, world, rank, local_rank):
     # per image: one sinogram launch; per batch: circus, circus adjoint, line
     # parameters, rotation adjoint
     line = {
-        "metric": METRIC, "value": world * n_sino / (ms / 1e3), "unit": "sinograms/s",
+        "metric": METRIC, "value": job_rate(n_sino, world, ms), "unit": "sinograms/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded blob+noise, the reference ships no images)",
         "config": grad_config(world),
         "forward_ms": statistics.mean(fwd), "backward_ms": statistics.mean(bwd),
         "backward_over_forward": statistics.mean(bwd) / statistics.mean(fwd),
-        "images_per_s": world * GRAD_IMAGES / (ms / 1e3),
-        "e2e": {"value": world * n_sino / e2e_s, "unit": "sinograms/s",
+        "images_per_s": job_rate(GRAD_IMAGES, world, ms),
+        "e2e": {"value": job_rate(n_sino, world, e2e_s * 1e3), "unit": "sinograms/s",
                 "h2d_bytes_per_step": int(h_imgs.numel() * 4),
                 "d2h_bytes_per_step": int(h_grad.numel() * 4 + 4), "loss": lv},
         "gpu_launches": (GRAD_IMAGES + 4) * args.steps,
@@ -797,6 +797,12 @@ def run_grad(args, world, rank, local_rank):
                                 "sample": desc + "; forward only (the reference has no "
                                                  "gradient)"}
     print(json.dumps(line), flush=True)
+
+
+def job_rate(units_per_rank, world, ms):
+    """Whole-job throughput of a weak-scaling run: every rank processes
+    units_per_rank per step and ms is the slowest rank's step time."""
+    return world * units_per_rank / (ms / 1e3)
 
 
 def barrier(world):
