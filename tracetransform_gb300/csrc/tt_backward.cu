@@ -420,15 +420,9 @@ cudaError_t launch_circus_backward(const T *sino, int rows, int cols, int n_sino
         return cudaSuccess;
     const size_t base = sizeof(T) * ((size_t)rows + 3 * (size_t)(rows / 2 + 1));
     const size_t with_tab = base + sizeof(T) * 2 * (size_t)rows;
-    static size_t limit = 0;
-    if (limit == 0) {
-        limit = dynamic_smem_limit((const void *)circus_backward_kernel<T>);
-        cudaError_t e = cudaFuncSetAttribute(circus_backward_kernel<T>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)limit);
-        if (e != cudaSuccess)
-            return e;
-    }
+    const size_t limit = opt_in_smem((const void *)circus_backward_kernel<T>);
+    if (limit == 0)
+        return cudaErrorInvalidValue;
     const bool tab = with_tab <= limit;
     const size_t smem = tab ? with_tab : base;
     if (smem > limit)

@@ -279,15 +279,9 @@ size_t circus_smem_bytes(const CircusArgs &a) {
 }
 
 cudaError_t launch_circus(const CircusArgs &a, cudaStream_t stream) {
-    static size_t limit = 0;
-    if (limit == 0) {
-        limit = dynamic_smem_limit((const void *)circus_kernel);
-        cudaError_t e = cudaFuncSetAttribute(circus_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)limit);
-        if (e != cudaSuccess)
-            return e;
-    }
+    const size_t limit = opt_in_smem((const void *)circus_kernel);
+    if (limit == 0)
+        return cudaErrorInvalidValue;
     const size_t smem = circus_smem_bytes(a);
     if (smem > limit)
         return cudaErrorInvalidValue;
@@ -305,15 +299,9 @@ cudaError_t launch_zscore(const float *in, int n_vec, int len, float *out,
 }
 
 cudaError_t prepare_circus_batch(size_t smem) {
-    static size_t limit = 0;
-    if (limit == 0) {
-        limit = dynamic_smem_limit((const void *)circus_batch_kernel);
-        cudaError_t e = cudaFuncSetAttribute(circus_batch_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)limit);
-        if (e != cudaSuccess)
-            return e;
-    }
+    const size_t limit = opt_in_smem((const void *)circus_batch_kernel);
+    if (limit == 0)
+        return cudaErrorInvalidValue;
     return smem > limit ? cudaErrorInvalidValue : cudaSuccess;
 }
 

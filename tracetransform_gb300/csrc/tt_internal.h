@@ -135,6 +135,10 @@ int record_error(int status, const char *message);
 
 // Opt-in shared memory per block minus the kernel's static shared memory.
 size_t dynamic_smem_limit(const void *kernel);
+// Raises the kernel's dynamic shared memory cap to dynamic_smem_limit on the
+// current device (once per device and kernel, thread-safe); returns the cap,
+// 0 on failure.
+size_t opt_in_smem(const void *kernel);
 
 // Batched P-stage: one image's sinogram stack and tables.
 struct BatchCircusImage {

@@ -1196,17 +1196,7 @@ static cudaError_t block_rounds(int n, int n_sino, const NosWork &w, cudaStream_
     const size_t smem = sizeof(float) * block_round_smem_floats(K4);
     if (128 * K4 < n)
         return cudaErrorInvalidValue;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(rt_block_round_kernel<K4>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)dynamic_smem_limit(
-                                                 (const void *)rt_block_round_kernel<K4>));
-        if (e != cudaSuccess)
-            return e;
-        attr = true;
-    }
-    if (smem > dynamic_smem_limit((const void *)rt_block_round_kernel<K4>))
+    if (smem > opt_in_smem((const void *)rt_block_round_kernel<K4>))
         return cudaErrorInvalidValue;
     for (int r = 0; r < nbp - 1; r++)
         rt_block_round_kernel<K4><<<dim3(nbp / 2, n_sino), kBThreads, smem, st>>>(
@@ -1261,15 +1251,9 @@ cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int
                                                               w.V, n, out);
         return cudaGetLastError();
     }
-    static size_t limit = 0;
-    if (limit == 0) {
-        limit = dynamic_smem_limit((const void *)nos_apply_q_kernel);
-        cudaError_t e = cudaFuncSetAttribute(nos_apply_q_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)limit);
-        if (e != cudaSuccess)
-            return e;
-    }
+    const size_t limit = opt_in_smem((const void *)nos_apply_q_kernel);
+    if (limit == 0)
+        return cudaErrorInvalidValue;
     const size_t smem = nos_apply_smem(max_m);
     if (smem > limit)
         return cudaErrorInvalidValue;

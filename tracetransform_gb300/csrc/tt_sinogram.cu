@@ -25,6 +25,9 @@
 // T6 and T7 need no sort: their weighted medians come from a histogram
 // selection with exact fixed-point weights (tt_select.cuh).
 #include <climits>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "tt_common.cuh"
 #include "tt_internal.h"
@@ -556,15 +559,9 @@ __global__ void bbox_finish(int *r) {
 
 template <int L, bool kSel>
 cudaError_t launch_one(const SinoArgs &a, size_t smem, cudaStream_t stream) {
-    static size_t limit = 0;
-    if (limit == 0) {
-        limit = dynamic_smem_limit((const void *)sino_kernel<L, kSel>);
-        cudaError_t e = cudaFuncSetAttribute(sino_kernel<L, kSel>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)limit);
-        if (e != cudaSuccess)
-            return e;
-    }
+    const size_t limit = opt_in_smem((const void *)sino_kernel<L, kSel>);
+    if (limit == 0)
+        return cudaErrorInvalidValue;
     if (smem > limit)
         return cudaErrorInvalidValue;
     dim3 grid((a.n + L - 1) / L, a.n_angles);
@@ -581,6 +578,25 @@ size_t dynamic_smem_limit(const void *kernel) {
     cudaFuncAttributes fa{};
     cudaFuncGetAttributes(&fa, kernel);
     return optin > (int)fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
+}
+
+size_t opt_in_smem(const void *kernel) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> done; // (device, kernel) -> limit
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return 0;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_pair(dev, kernel);
+    const auto it = done.find(key);
+    if (it != done.end())
+        return it->second;
+    const size_t limit = dynamic_smem_limit(kernel);
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit) !=
+        cudaSuccess)
+        return 0;
+    done.emplace(key, limit);
+    return limit;
 }
 
 int sino_lines_per_block(int n, unsigned need) {
@@ -611,15 +627,9 @@ cudaError_t launch_sinograms(const SinoArgs &a, int lines, cudaStream_t stream) 
 
 namespace {
 template <int L, bool kSel> cudaError_t set_batch_attr(size_t smem) {
-    static size_t limit = 0;
-    if (limit == 0) {
-        limit = dynamic_smem_limit((const void *)sino_batch_kernel<L, kSel>);
-        cudaError_t e = cudaFuncSetAttribute(sino_batch_kernel<L, kSel>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)limit);
-        if (e != cudaSuccess)
-            return e;
-    }
+    const size_t limit = opt_in_smem((const void *)sino_batch_kernel<L, kSel>);
+    if (limit == 0)
+        return cudaErrorInvalidValue;
     return smem > limit ? cudaErrorInvalidValue : cudaSuccess;
 }
 
