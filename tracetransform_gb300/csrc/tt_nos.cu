@@ -241,7 +241,7 @@ template <int T> __device__ __forceinline__ float2 qr_block_sum(float2 v, float2
 // flight and written once.  Sums, updates and scalars are all double-float;
 // the scalars are computed by one lane per warp.
 template <int K, int T>
-__global__ void __launch_bounds__(T)
+__global__ void __launch_bounds__(T, K == 32 ? 1 : 512 / T) // no spills at 128 registers below K = 32
 qr_step_kernel(float2 *__restrict__ A, const NosDesc *__restrict__ desc, int n, int n_sino,
                int k, NosWork w) {
     constexpr int kW = T / 32;
@@ -1032,7 +1032,7 @@ nos_apply_q_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ des
 // (t, u) of reflector k holds v_i for i = t + kQThreads u: 1 at i = k, the
 // scaled pivot column below it, 0 above.
 template <int K>
-__global__ void __launch_bounds__(kQThreads)
+__global__ void __launch_bounds__(kQThreads, K == 8 ? 3 : 1) // 3 CTAs per SM fit K = 8 unspilled
 nos_apply_q_reg_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc,
                        const float2 *__restrict__ tau, const float2 *__restrict__ scale,
                        const int *__restrict__ perm, const float *__restrict__ P, int n,
