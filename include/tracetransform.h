@@ -175,8 +175,8 @@ tt_status tt_circus_device(tt_plan *plan, const float *d_sino, int rows, int col
 /* Orthonormal (Hermite) circus functions of n_sino stacked rows x cols
  * sinograms (as tt_sinograms_device wrote them): each sinogram's nearest
  * orthonormal sinogram (c++/src/circus.cpp:68-102; here a column-pivoting
- * QR in double, a one-sided Jacobi SVD of R^T in float and Q applied on the
- * device), then the Hermite P-functionals with the center it yields
+ * QR in double-float, a one-sided Jacobi SVD of R^T in float and Q applied on
+ * the device), then the Hermite P-functionals with the center it yields
  * (c++/src/transform.cpp:75-85).  pfuncs must all be TT_P_HERMITE (their
  * centers are ignored).  d_out: n_sino x n_p x cols; centers (host, may be
  * NULL): the n_sino centers used.  The reference runs this only on images

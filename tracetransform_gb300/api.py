@@ -241,7 +241,8 @@ def getCircusFunctions(sinogram, pfunctionals: Sequence,
 def nearest_orthonormal_sinogram(sinogram, plan: Optional[Plan] = None):
     """(nos, new_center) of c++/src/circus.cpp:68-102 for one N x A sinogram:
     the columns aligned on their weighted medians and replaced by the polar
-    factor U V^T (device Jacobi SVD in double)."""
+    factor U V^T (on the device: pivoted QR in double-float, one-sided
+    Jacobi on R^T in float)."""
     sinogram = np.asarray(sinogram, dtype=np.float32)
     rows, cols = sinogram.shape
     out = np.zeros(2 * rows * cols, np.float32)
