@@ -276,6 +276,23 @@ Matrix<T, Dynamic, Dynamic> operator*(const Block<T> &a,
     return Matrix<T, Dynamic, Dynamic>::product(am, b);
 }
 
+// Map over external column-major storage.  The stand-in copies on
+// construction (Eigen's Map aliases the storage); enough for code that reads
+// through a Map or converts it to a Matrix, as the engine's reference-side
+// bindings do.
+template <typename MatrixType> class Map : public MatrixType {
+  public:
+    typedef typename MatrixType::Scalar Scalar;
+    Map(const Scalar *p, Index rows, Index cols) : MatrixType(rows, cols) {
+        for (Index i = 0; i < rows * cols; i++)
+            this->data()[i] = p[i];
+    }
+    Map(const Scalar *p, Index n) : MatrixType(n) {
+        for (Index i = 0; i < n; i++)
+            this->data()[i] = p[i];
+    }
+};
+
 typedef Matrix<float, Dynamic, Dynamic> MatrixXf;
 typedef Matrix<int, Dynamic, Dynamic> MatrixXi;
 typedef Matrix<double, Dynamic, Dynamic> MatrixXd;
