@@ -129,3 +129,15 @@ def test_device_resize_bit_exact(i):
 def test_device_resize_rejects_bad_sizes():
     with pytest.raises(Exception):
         api.resize(np.ones((4, 4), np.float32), 0, 4)
+
+
+def test_workload_pgm_round_trip(tmp_path):
+    """The synthetic workloads are also written as ASCII PGM (the reference's
+    demo input); readnetpbm + gray2mat give back the very floats the bench
+    feeds both paths."""
+    from tracetransform_gb300 import synthetic
+    (path, step), = synthetic.write_pgm("single256", str(tmp_path))
+    (pix,) = api.readnetpbm(path)
+    (img, step2), = synthetic.workload("single256")
+    assert step == step2
+    assert np.array_equal(api.gray2mat(pix).view(np.uint32), img.view(np.uint32))

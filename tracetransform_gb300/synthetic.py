@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["blob_image", "blob_image_u8", "workload"]
+__all__ = ["blob_image", "blob_image_u8", "workload", "workload_u8", "write_pgm"]
 
 
 def blob_image_u8(rows: int, cols: int, n_blobs: int, sigma: tuple[float, float],
@@ -34,6 +34,10 @@ def blob_image_u8(rows: int, cols: int, n_blobs: int, sigma: tuple[float, float]
     return np.rint(np.clip(img, 0.0, 255.0)).astype(np.uint8)
 
 
+def _u8(rows, cols, n_blobs, sigma, amplitude, seed):
+    return blob_image_u8(rows, cols, n_blobs, sigma, amplitude, np.random.default_rng(seed))
+
+
 def blob_image(rows: int, cols: int, n_blobs: int, sigma=(8.0, 40.0),
                amplitude=(40.0, 200.0), seed: int = 1) -> np.ndarray:
     """float32 (rows, cols) Fortran-order image in [0, 1], as gray2mat gives."""
@@ -43,7 +47,29 @@ def blob_image(rows: int, cols: int, n_blobs: int, sigma=(8.0, 40.0),
 
 
 def workload(name: str):
-    """The named benchmark workloads.
+    """The named workloads as gray2mat floats: [(image, angle_step), ...]
+    (the pixels of workload_u8 / 255 in double, stored as float32)."""
+    return [(np.asfortranarray((u8.astype(np.float64) / 255.0).astype(np.float32)), step)
+            for u8, step in workload_u8(name)]
+
+
+def write_pgm(name: str, directory: str):
+    """Writes the named workload's images as ASCII PGM (P2) files
+    <name>_<i>.pgm -- the input format of the reference's demo
+    (c++/src/demo.cpp:190-194, readnetpbm) -- and returns their paths with
+    the angle steps."""
+    import os
+    from .api import writepgm
+    out = []
+    for i, (u8, step) in enumerate(workload_u8(name)):
+        path = os.path.join(directory, f"{name}_{i}.pgm")
+        writepgm(path, u8.astype(np.int32))
+        out.append((path, step))
+    return out
+
+
+def workload_u8(name: str):
+    """The named benchmark workloads, as uint8 pixels.
 
     ``single256``  256x256, 8 blobs (sigma 8-40, amplitude 40-200), seed 1
     ``single1024`` 1024x1024, 32 blobs (sigma 16-160), seed 2
@@ -54,17 +80,17 @@ def workload(name: str):
     Returns a list of (image, angle_step_degrees) pairs.
     """
     if name == "single256":
-        return [(blob_image(256, 256, 8, (8, 40), (40, 200), 1), 1.0)]
+        return [(_u8(256, 256, 8, (8, 40), (40, 200), 1), 1.0)]
     if name == "single1024":
-        return [(blob_image(1024, 1024, 32, (16, 160), (40, 200), 2), 1.0)]
+        return [(_u8(1024, 1024, 32, (16, 160), (40, 200), 2), 1.0)]
     if name == "single4096":
-        return [(blob_image(4096, 4096, 256, (32, 640), (40, 200), 6), 0.5)]
+        return [(_u8(4096, 4096, 256, (32, 640), (40, 200), 6), 0.5)]
     if name == "batch512":
         rng = np.random.default_rng(3)
         rows = rng.integers(64, 513, 512)
         cols = rng.integers(64, 513, 512)
         nb = rng.integers(4, 17, 512)
         steps = np.where(rng.random(512) < 0.5, 1.0, 2.0)
-        return [(blob_image(int(rows[i]), int(cols[i]), int(nb[i]), (8, 40), (40, 200),
-                            3000 + i), float(steps[i])) for i in range(512)]
+        return [(_u8(int(rows[i]), int(cols[i]), int(nb[i]), (8, 40), (40, 200), 3000 + i),
+                 float(steps[i])) for i in range(512)]
     raise ValueError(f"unknown workload {name!r}")
