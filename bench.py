@@ -412,6 +412,7 @@ def run_engine(args, world, rank, local_rank):
                      "frac": achieved / peak,
                      "traffic": committed_traffic("sino_kernel", args.workload),
                      "algorithmic_bytes_per_launch": alg_bytes,
+                     "padded_sweep_bytes_per_launch": 4.0 * A * n * n,
                      "kernel_ms": kern_s * 1e3},
         "clocks": clk,
     }
