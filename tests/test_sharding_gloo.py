@@ -67,6 +67,14 @@ class OracleCompute:
         return np.stack(out)
 
 
+    def transform_images(self, images, steps, tfs, pfs):
+        out = []
+        for im, st in zip(images, steps):
+            r = O.transform(im, int(st), list(tfs), [(k, o) for k, o, _ in pfs])
+            out.append((r["circus"], np.ascontiguousarray(r["sig"])))
+        return out
+
+
 rank, world = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"])
 dist.init_process_group("gloo")
 O.build()
@@ -81,6 +89,17 @@ for name, step, tfs, pfs in [("regular", 4, [0, 1, 5, 6, 7], [(1, 0, -1), (2, 0,
         np.save(os.path.join(os.environ["TT_OUT"], name + "_sig.npy"), r[1])
     else:
         assert r is None
+imgs = [blob_image(r, c, 3, (2, 6), (40, 200), 50 + i)
+        for i, (r, c) in enumerate([(20, 14), (33, 30), (12, 25), (28, 28), (16, 16)])]
+steps = [6, 4, 8, 6, 5]
+res = sharding.transform_images_sharded(imgs, steps, [0, 2, 7], [(1, 0, -1), (3, 0, -1)],
+                                        rank, world, compute=OracleCompute())
+if rank == 0:
+    for i, (c, z) in enumerate(res):
+        np.save(os.path.join(os.environ["TT_OUT"], "batch%d_circus.npy" % i), c)
+        np.save(os.path.join(os.environ["TT_OUT"], "batch%d_sig.npy" % i), z)
+else:
+    assert res is None
 dist.destroy_process_group()
 print(json.dumps({"rank": rank, "ok": True}))
 """
@@ -126,3 +145,11 @@ def test_angle_sharded_transform_two_gloo_ranks(oracle_lib, tmp_path):
     z = np.stack([O.zscore(v) for v in herm.reshape(-1, herm.shape[2])])
     assert np.array_equal(np.load(tmp_path / "hermite_sig.npy").view(np.uint32),
                           np.ascontiguousarray(z.T).view(np.uint32))
+    # a batch over the two ranks: every image's result back on rank 0, in order
+    for i, ((r, c), st) in enumerate(zip([(20, 14), (33, 30), (12, 25), (28, 28), (16, 16)],
+                                         [6, 4, 8, 6, 5])):
+        im = blob_image(r, c, 3, (2, 6), (40, 200), 50 + i)
+        w = O.transform(im, st, [0, 2, 7], [(O.P1, 0), (O.P3, 0)])
+        assert np.array_equal(np.load(tmp_path / ("batch%d_circus.npy" % i)), w["circus"])
+        assert np.array_equal(np.load(tmp_path / ("batch%d_sig.npy" % i)), np.asarray(w["sig"]))
+

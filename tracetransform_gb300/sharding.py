@@ -7,9 +7,10 @@ circus entry depends only on its own angle's sinogram column
 and the nearest orthonormal sinogram (c++/src/circus.cpp:68-102) need all
 the angles of a sinogram.  Hence two partitionings:
 
-* ``assign_images``: the images of a batch to ranks, largest cost
-  (4 A H W) first onto the least-loaded rank.  No exchange at all; every
-  rank runs its images through the batched engine.
+* ``assign_images`` + ``transform_images_sharded``: the images of a batch
+  to ranks, largest cost (4 A H W) first onto the least-loaded rank.  Every
+  rank runs its images through the batched engine with no exchange; rank 0
+  then gathers the finished per-image results.
 * ``angle_ranges`` + ``transform_angle_sharded``: the angles of one large
   image in contiguous ranges, one per rank.  Each rank computes its sinogram
   columns and their raw circus entries; rank 0 gathers the raw circus
@@ -28,7 +29,7 @@ from typing import List, Optional, Sequence, Tuple
 import numpy as np
 
 __all__ = ["angle_ranges", "assign_images", "image_cost", "EngineCompute",
-           "transform_angle_sharded"]
+           "transform_angle_sharded", "transform_images_sharded"]
 
 
 def image_cost(rows: int, cols: int, n_angles: int) -> float:
@@ -94,6 +95,27 @@ class EngineCompute:
         dev = torch.from_numpy(np.ascontiguousarray(vectors, dtype=np.float32)).to(self.engine.device)
         return self.engine.zscore(dev).cpu().numpy()
 
+    def transform_images(self, images, angle_steps, tfuncs, pfuncs):
+        """The batched engine (regular P-functionals) on this rank's images:
+        [(circus nT x nP x A_i, signatures A_i x (nT nP))] in input order."""
+        torch = self._torch
+        bufs = [np.ascontiguousarray(np.asarray(im, np.float32).ravel(order="F")) for im in images]
+        offsets = np.zeros(len(bufs), np.int64)
+        offsets[1:] = np.cumsum([b.size for b in bufs])[:-1]
+        flat = torch.from_numpy(np.concatenate(bufs)).to(self.engine.device)
+        circ, sig = self.engine.transform_batch(
+            flat, offsets, [im.shape[0] for im in images], [im.shape[1] for im in images],
+            [int(x) for x in angle_steps], tfuncs, list(pfuncs))
+        circ, sig = circ.cpu().numpy(), sig.cpu().numpy()
+        out, at = [], 0
+        n_tp = len(tfuncs) * len(pfuncs)
+        for x in angle_steps:
+            a = 360 // int(x)
+            out.append((circ[at:at + n_tp * a].reshape(len(tfuncs), len(pfuncs), a).copy(),
+                        np.ascontiguousarray(sig[at:at + n_tp * a].reshape(n_tp, a).T)))
+            at += n_tp * a
+        return out
+
     def orthonormal(self, sino: np.ndarray, orders: Sequence[int]) -> np.ndarray:
         torch = self._torch
         dev = torch.from_numpy(np.ascontiguousarray(sino.transpose(0, 2, 1))).to(self.engine.device)
@@ -146,3 +168,29 @@ def transform_angle_sharded(image, angle_stepsize: int, tfuncs: Sequence[int],
     n_t, n_p = circus.shape[0], circus.shape[1]
     z = compute.zscore(circus.reshape(n_t * n_p, n_a))
     return circus, np.ascontiguousarray(z.reshape(n_t * n_p, n_a).T)
+
+
+def transform_images_sharded(images, angle_steps, tfuncs: Sequence[int],
+                             pfuncs: Sequence[Tuple[int, int, int]], rank: int, world: int,
+                             group=None, compute=None):
+    """A batch of independent images over `world` ranks (call it on every
+    rank): each rank transforms its assign_images share (cost 4 A H W) in one
+    batched call, and rank 0 gathers the per-image results.  Returns, on rank
+    0, [(circus nT x nP x A_i, signatures A_i x (nT nP))] in input order, and
+    None on every other rank."""
+    compute = compute if compute is not None else EngineCompute()
+    costs = [image_cost(im.shape[0], im.shape[1], 360 // int(st))
+             for im, st in zip(images, angle_steps)]
+    mine = assign_images(costs, world)[rank]
+    results = (compute.transform_images([images[i] for i in mine],
+                                        [angle_steps[i] for i in mine], tfuncs, pfuncs)
+               if mine else [])
+    local = list(zip(mine, results))
+    parts = _gather(local, group) if world > 1 else [local]
+    if rank != 0:
+        return None
+    out = [None] * len(images)
+    for part in parts:
+        for i, r in part:
+            out[i] = r
+    return out
