@@ -87,3 +87,19 @@ def test_compute_without_gpu_raises(lib):
         tt.getSinograms(np.zeros((5, 5), np.float32), 1, ["0"])
     with pytest.raises(_native.TTError):
         tt.resize(np.zeros((5, 5), np.float32), 3, 3)
+
+
+def test_transformer_validation_before_compute():
+    """Transformer checks its arguments on the host, as the reference's
+    constructor and demo do (c++/src/transform.cpp:28-47,
+    c++/src/demo.cpp:153-169), so these fail the same way without a GPU."""
+    img = np.zeros((8, 8), np.float32)
+    with pytest.raises(ValidationError):
+        tt.Transformer(img, "x", 0, False)
+    tr = tt.Transformer(img, "x", 4, False)
+    with pytest.raises(ValidationError, match="Cannot mix"):
+        tr.getTransform(["0"], ["1", "H2"], write_data=False)
+    with pytest.raises(ValidationError, match="orthonormal"):
+        tr.getTransform(["0"], ["H2"], write_data=False)
+    with pytest.raises(ValidationError):
+        tr.getTransform(["9"], ["1"], write_data=False)
