@@ -49,10 +49,16 @@ def _run_ranks(script, world, extra_env=None, args=()):
         procs.append(subprocess.Popen([sys.executable, "-c", script, *args], env=env,
                                       stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True))
     outs = []
-    for p in procs:
-        out, err = p.communicate(timeout=120)
-        assert p.returncode == 0, err
-        outs.append(out)
+    try:
+        for p in procs:
+            out, err = p.communicate(timeout=120)
+            assert p.returncode == 0, err
+            outs.append(out)
+    finally:
+        for p in procs:  # a rank that failed or hung must not outlive the test
+            if p.poll() is None:
+                p.kill()
+                p.wait()
     return outs
 
 

@@ -120,10 +120,16 @@ def test_angle_sharded_transform_two_gloo_ranks(oracle_lib, tmp_path):
                    RANK=str(rank), LOCAL_RANK=str(rank), TT_ROOT=ROOT, TT_OUT=str(tmp_path))
         procs.append(subprocess.Popen([sys.executable, "-c", _RANK_SCRIPT], env=env,
                                       stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True))
-    for p in procs:
-        out, err = p.communicate(timeout=300)
-        assert p.returncode == 0, err
-        assert json.loads(out.strip().splitlines()[-1])["ok"]
+    try:
+        for p in procs:
+            out, err = p.communicate(timeout=300)
+            assert p.returncode == 0, err
+            assert json.loads(out.strip().splitlines()[-1])["ok"]
+    finally:
+        for p in procs:  # a rank that failed or hung must not outlive the test
+            if p.poll() is None:
+                p.kill()
+                p.wait()
     from tracetransform_gb300.synthetic import blob_image
     img = blob_image(40, 32, 5, (3, 10), (40, 200), 7)
     # regular mode: the oracle's unsharded Transformer
