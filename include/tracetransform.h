@@ -151,6 +151,25 @@ tt_status tt_transform(tt_plan *plan, const float *image, int rows, int cols,
                        const tt_pfunctional *pfuncs, int n_p, float *circus,
                        float *signatures);
 
+/* Transformer's two modes over the same sinograms in one call, from host
+ * buffers.  The reference computes P1-P3 (regular mode) and the Hermite
+ * circus (orthonormal mode) in separate Transformer runs, the latter on the
+ * image stretched to tt_ortho_size (c++/src/transform.cpp:28-112,
+ * demo.cpp:153-169 rejects mixing them); this call computes, for the
+ * unstretched image and an explicit angle list (degrees, any values),
+ * every T-functional's sinogram once, the regular circus functions of pfuncs
+ * (P1-P3 only) and the Hermite circus of hermite_orders on each sinogram's
+ * nearest orthonormal sinogram (c++/src/circus.cpp:68-102, centers as
+ * transform.cpp:75-85 sets them).  circus / signatures (may be NULL):
+ * n_t x n_p x n_angles as tt_transform; hermite_circus / hermite_signatures
+ * (may be NULL): n_t x n_h x n_angles; centers (may be NULL): n_t. */
+tt_status tt_transform_extended(tt_plan *plan, const float *image, int rows, int cols,
+                                const float *angles_deg, int n_angles, const int32_t *tfuncs,
+                                int n_t, const tt_pfunctional *pfuncs, int n_p,
+                                const int32_t *hermite_orders, int n_h, float *circus,
+                                float *signatures, float *hermite_circus,
+                                float *hermite_signatures, int32_t *centers);
+
 /* ---- device entry points (stream ordered) ----------------------------- */
 /* Fused rotate + T-functional sweep over an explicit angle list (degrees;
  * the integer-step list of the reference is tt_angles_from_step).
@@ -278,6 +297,22 @@ tt_status tt_transform_batch_device(tt_plan *plan, const float *d_images, const 
                                     const int32_t *angle_steps, int n_images,
                                     const int32_t *tfuncs, int n_t, const tt_pfunctional *pfuncs,
                                     int n_p, float *d_circus, float *d_signatures, void *stream);
+
+/* The sinograms behind the plan's last tt_transform_batch[_device] call,
+ * image after image in input order, each n_t x A_i x N_i as
+ * tt_sinograms_device writes them (N_i from tt_pad_geometry): the per-image
+ * sinograms the reference writes in its debug output
+ * (Transformer::getTransform with write_data, c++/src/transform.cpp:61-72).
+ * *count (may be NULL) receives the float count, 0 before the first batch;
+ * d_out may be NULL to query it, else it must hold capacity >= *count floats.
+ * Ordered on stream (NULL: the plan's stream) after the last batch. */
+tt_status tt_transform_batch_sinograms_device(tt_plan *plan, float *d_out, int64_t capacity,
+                                              int64_t *count, void *stream);
+
+/* Device time, in milliseconds, of the three kernels of the plan's last
+ * batched call (ms[0] sinograms, ms[1] P-functionals, ms[2] z-scores), from
+ * CUDA events recorded inside the captured graph; waits for that call. */
+tt_status tt_transform_batch_stage_ms(tt_plan *plan, float *ms);
 
 /* ---- allocation-free entry point ---------------------------------------- */
 /* No counterpart in the reference.  P1 / P2 / P3 circus functions of n_sino

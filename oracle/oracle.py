@@ -64,6 +64,8 @@ def lib():
         l.tto_t345_prepare.argtypes = [ctypes.c_int, ctypes.c_int, _F, _F]
         l.tto_t345.argtypes = [_F, ctypes.c_int, _F, _F]
         l.tto_t345.restype = ctypes.c_float
+        l.tto_t_at.argtypes = [ctypes.c_int, _F, ctypes.c_int, ctypes.c_int]
+        l.tto_t_at.restype = ctypes.c_float
         l.tto_hermite_function.argtypes = [ctypes.c_uint, ctypes.c_float]
         l.tto_hermite_function.restype = ctypes.c_float
         l.tto_p_hermite.argtypes = [_F, ctypes.c_int, ctypes.c_uint, ctypes.c_int]
@@ -117,6 +119,19 @@ def rotate(image: np.ndarray, angle_deg: float) -> np.ndarray:
     l = lib()
     l.tto_rotate(_fp(_f32(image)), rows, cols, l.tto_deg2rad(ctypes.c_float(angle_deg)), _fp(out))
     return out.reshape((rows, cols), order="F")
+
+
+def t_at(f: int, x: np.ndarray, median: int) -> float:
+    """T-functional f of column x with the weighted median held at row
+    `median` (the reference's arithmetic, c++/src/functionals.cpp:95-276)."""
+    x = np.ascontiguousarray(x, np.float32)
+    return float(lib().tto_t_at(int(f), _fp(x), x.size, int(median)))
+
+
+def weighted_median(x: np.ndarray) -> int:
+    """findWeightedMedian (c++/src/functionals.cpp:21-30)."""
+    x = np.ascontiguousarray(x, np.float32)
+    return int(lib().tto_find_weighted_median(_fp(x), x.size))
 
 
 def angles_for_step(step) -> np.ndarray:

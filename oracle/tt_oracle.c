@@ -340,6 +340,35 @@ float tto_t7(const float *x, int n) {
     return t7_at(x, n, tto_find_weighted_median(x, n));
 }
 
+/* T-functional f of column x with its weighted median held at row median
+ * (the *_at bodies above; T0 ignores median).  Test infrastructure: the
+ * parity checker evaluates the reference's arithmetic at the row the engine
+ * chose when the reference's own crossing is a rounding tie. */
+float tto_t_at(int f, const float *x, int n, int median) {
+    if (f == TTO_RADON)
+        return tto_t_radon(x, n);
+    if (median < 0 || median >= n)
+        return NAN;
+    switch (f) {
+    case TTO_T1: return t1_at(x, n, median);
+    case TTO_T2: return t2_at(x, n, median);
+    case TTO_T3:
+    case TTO_T4:
+    case TTO_T5: {
+        float *re = (float *)malloc(sizeof(float) * (size_t)n);
+        float *im = (float *)malloc(sizeof(float) * (size_t)n);
+        tto_t345_prepare(f, n, re, im);
+        float r = t345_at(x, n, median, re, im);
+        free(re);
+        free(im);
+        return r;
+    }
+    case TTO_T6: return t6_at(x, n, median);
+    case TTO_T7: return t7_at(x, n, median);
+    default: return NAN;
+    }
+}
+
 /* c++/src/functionals.cpp:287-296; fabs there is C's double fabs. */
 float tto_p1(const float *x, int n) {
     float sum = 0;

@@ -48,6 +48,7 @@ void tto_t345_prepare(int which, int rows, float *re, float *im); /* :136-198 */
 float tto_t345(const float *x, int n, const float *re, const float *im); /* :200-213 */
 float tto_t6(const float *x, int n);                            /* :226-255 */
 float tto_t7(const float *x, int n);                            /* :262-276 */
+float tto_t_at(int f, const float *x, int n, int median);      /* *_at above */
 float tto_p1(const float *x, int n);                            /* :287-296 */
 float tto_p2(const float *x, int n);                            /* :303-311 */
 float tto_p3(const float *x, int n);                            /* :332-360 */

@@ -60,8 +60,8 @@ def test_orthonormal_circus_device(oracle_lib):
         nos, c = O.nos(ref[t])
         assert centers[t] == c
         want = O.circus(nos, [(0, o, c) for o in (1, 2, 3, 4, 5)])
-        scale = np.abs(want).max(axis=1, keepdims=True)
-        assert np.abs(got[t] - want).max() <= 1e-3 * scale.max()
+        from parity import rel_err
+        assert rel_err(got[t], want).max() <= HERMITE_RTOL
 
 
 def test_nos_zero_and_rank_one(oracle_lib):
@@ -126,3 +126,68 @@ def test_nos_kernel_variants_vs_oracle(oracle_lib, rows, cols):
     g = got.astype(np.float64)
     assert np.abs(g.T @ g - np.eye(cols)).max() < 1e-4
     assert np.abs(got - want).max() < 1e-4
+
+
+# Orthonormal (Hermite) circus against the oracle.  The nearest orthonormal
+# sinogram is the orthogonal polar factor U V^T of the aligned sinogram; its
+# directions of small singular values are ill-conditioned (their error grows
+# as eps / sigma_min), so the engine (double-float QR, float Jacobi) and the
+# oracle (double one-sided Jacobi) agree entry by entry only to the bound
+# HERMITE_RTOL, stated from the measured error at the 1024^2 workload's
+# 1449 x 360 shape; the measured figures are recorded with TT_PARITY_REPORT.
+HERMITE_RTOL = 1e-3
+
+
+def _hermite_report(got, want):
+    from parity import rel_err
+    e = rel_err(got, want)
+    return {"max_rel": float(e.max()), "p99": float(np.quantile(e, 0.99)),
+            "p50": float(np.median(e)), "over_1e-4": int((e > 1e-4).sum()),
+            "entries": int(e.size)}
+
+
+def test_orthonormal_mode_golden(oracle_lib):
+    """Transformer in orthonormal mode on the reference's own outputs
+    (stretch, NOS, Hermite circus, signatures)."""
+    from parity import record
+    import os
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden",
+                                  "blob48_ortho_step4.npz")))
+    tfs = [str(int(t)) for t in g["tfuncs"]]
+    pfs = ["H%d" % int(o) for o in g["porders"]]
+    tr = tt.Transformer(g["image"], "ortho", int(g["step"]), True)
+    tr.getTransform(tfs, pfs, write_data=False)
+    rep = _hermite_report(tr.circus, g["circus"])
+    record("golden_orthonormal", rep)
+    assert rep["max_rel"] <= HERMITE_RTOL, rep
+
+
+def test_orthonormal_circus_single1024_shape(oracle_lib):
+    """The 1024^2 workload's Hermite circus: T0, T1, T3 sinograms of
+    1449 x 360 from the engine, their nearest orthonormal sinograms and
+    Hermite orders 1-5, against the oracle's on the same sinograms."""
+    import torch
+    from parity import engine_sinograms, record
+    from tracetransform_gb300.device import Engine
+    from tracetransform_gb300.synthetic import workload
+    O = oracle_lib
+    img, _ = workload("single1024")[0]
+    tfs = [0, 1, 3]
+    eng = Engine(0)
+    sino, _ = engine_sinograms(eng, img, O.angles_for_step(1), tfs)
+    dev = torch.from_numpy(np.ascontiguousarray(sino.transpose(0, 2, 1))).cuda()
+    got, centers = eng.circus_orthonormal(dev, [1, 2, 3, 4, 5])
+    got = got.cpu().numpy()
+    want = np.zeros_like(got)
+    nos_err = 0.0
+    for t in range(len(tfs)):
+        nos, c = O.nos(sino[t])
+        assert centers[t] == c
+        want[t] = O.circus(nos, [(0, o, c) for o in (1, 2, 3, 4, 5)])
+        mine, _ = tt.nearest_orthonormal_sinogram(sino[t])
+        nos_err = max(nos_err, float(np.abs(mine - nos).max()))
+    rep = _hermite_report(got, want)
+    rep["nos_max_abs"] = nos_err
+    record("orthonormal_1449x360", rep)
+    assert nos_err < 1e-4, rep
+    assert rep["max_rel"] <= HERMITE_RTOL, rep

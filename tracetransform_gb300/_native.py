@@ -25,7 +25,8 @@ EXPORTS = (
     "tt_circus_zscore_noalloc", "tt_transform_batch", "tt_transform_batch_device",
     "tt_circus_backward_device", "tt_sinograms_backward_device", "tt_sinograms_f64_device",
     "tt_circus_f64_device", "tt_circus_backward_f64_device", "tt_sinograms_backward_f64_device",
-    "tt_circus_orthonormal_device", "tt_nos",
+    "tt_circus_orthonormal_device", "tt_nos", "tt_transform_batch_sinograms_device",
+    "tt_transform_batch_stage_ms", "tt_transform_extended",
 )
 
 
@@ -102,6 +103,11 @@ def lib():
         "tt_circus_orthonormal_device": [_P, _P, _int, _int, _int, ctypes.POINTER(PFunctionalC),
                                          _int, _P, _I32, _I32, _P],
         "tt_nos": [_P, _F, _int, _int, _F, _I32, _I32],
+        "tt_transform_batch_sinograms_device": [_P, _P, ctypes.c_int64, _I64, _P],
+        "tt_transform_batch_stage_ms": [_P, _F],
+        "tt_transform_extended": [_P, _F, _int, _int, _F, _int, _I32, _int,
+                                  ctypes.POINTER(PFunctionalC), _int, _I32, _int, _F, _F, _F,
+                                  _F, _I32],
     }
     for name, args in sig.items():
         fn = getattr(l, name)

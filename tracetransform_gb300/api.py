@@ -40,6 +40,7 @@ __all__ = [
     "TFunctional", "PFunctional", "TFunctionalWrapper", "PFunctionalWrapper", "ValidationError",
     "pad", "pad_geometry", "ortho_size", "angles_from_step", "getSinograms", "getCircusFunctions",
     "zscore", "Transformer", "writecsv", "Plan", "transform_batch", "rotate",
+    "transform_extended",
 ]
 
 
@@ -489,6 +490,33 @@ def transform_batch(images: Sequence, angle_stepsizes: Sequence[int], tfunctiona
         s = sig[at:at + k].reshape(len(ids) * len(pfs), a).T
         out.append((c, s))
         at += k
+    return out
+
+
+def transform_extended(image, angles_deg, tfunctionals: Sequence, pfunctionals: Sequence,
+                       hermite_orders: Sequence[int], plan: Optional[Plan] = None) -> dict:
+    """tt_transform_extended: the regular circus functions (P1-P3) and the
+    orthonormal Hermite circus of the same (unstretched) sinograms in one
+    call, over an explicit angle list.  Returns circus / signatures of shape
+    (nT, nP, A), hermite_circus / hermite_signatures (nT, nH, A) and the
+    nT Hermite centers."""
+    tfs = _as_tfunctionals(tfunctionals)
+    pfs = _as_pfunctionals(pfunctionals)
+    img = _colmajor(np.asarray(image, dtype=np.float32))
+    rows, cols = np.shape(image)
+    ang = np.ascontiguousarray(np.asarray(angles_deg, np.float32))
+    ids = np.array([int(t.functional) for t in tfs], np.int32)
+    orders = np.ascontiguousarray(np.asarray(hermite_orders, np.int32))
+    nt, npf, nh, a = len(ids), len(pfs), len(orders), len(ang)
+    out = {k: np.zeros((nt, m, a), np.float32) for k, m in
+           (("circus", npf), ("signatures", npf), ("hermite_circus", nh),
+            ("hermite_signatures", nh))}
+    centers = np.zeros(max(nt, 1), np.int32)
+    check(lib().tt_transform_extended(
+        _handle(plan), fptr(img), rows, cols, fptr(ang), a, iptr(ids), nt, _pf_array(pfs), npf,
+        iptr(orders), nh, fptr(out["circus"]), fptr(out["signatures"]),
+        fptr(out["hermite_circus"]), fptr(out["hermite_signatures"]), iptr(centers)))
+    out["centers"] = centers[:nt]
     return out
 
 

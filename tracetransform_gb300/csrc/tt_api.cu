@@ -844,6 +844,111 @@ tt_status tt_transform_batch(tt_plan *plan, const float *images, const int64_t *
     return TT_OK;
 }
 
+tt_status tt_transform_extended(tt_plan *plan, const float *image, int rows, int cols,
+                                const float *angles_deg, int n_angles, const int32_t *tfuncs,
+                                int n_t, const tt_pfunctional *pfuncs, int n_p,
+                                const int32_t *hermite_orders, int n_h, float *circus,
+                                float *signatures, float *hermite_circus,
+                                float *hermite_signatures, int32_t *centers) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    if (rows <= 0 || cols <= 0 || !image)
+        return fail(TT_ERR_INVALID_ARG, "empty image");
+    if (n_angles < 0 || (n_angles > 0 && !angles_deg))
+        return fail(TT_ERR_INVALID_ARG, "bad angle list");
+    if (n_h < 0 || n_h > TT_MAX_PFUNCTIONALS || (n_h > 0 && !hermite_orders))
+        return fail(TT_ERR_INVALID_ARG, "bad Hermite order list");
+    unsigned tneed, pneed;
+    TT_CHECK(check_tfuncs(tfuncs, n_t, &tneed));
+    TT_CHECK(check_pfuncs(pfuncs, n_p, false, &pneed));
+    for (int i = 0; i < n_p; i++)
+        if (pfuncs[i].kind == TT_P_HERMITE)
+            return fail(TT_ERR_INVALID_ARG, "pfuncs are the regular P-functionals; Hermite orders "
+                                            "go in hermite_orders");
+    std::vector<tt_pfunctional> hpf(n_h);
+    for (int i = 0; i < n_h; i++)
+        hpf[i] = tt_pfunctional{TT_P_HERMITE, hermite_orders[i], -1};
+    unsigned hneed = 0;
+    TT_CHECK(check_pfuncs(hpf.data(), n_h, false, &hneed));
+    int n, ro, co;
+    pad_geometry(rows, cols, &n, &ro, &co);
+    const int A = n_angles;
+    const size_t sino_elems = (size_t)n_t * n * A, circ_elems = (size_t)n_t * n_p * A,
+                 herm_elems = (size_t)n_t * n_h * A;
+    cudaStream_t st = p->stream;
+    TT_CHECK(p->ensure(p->in, sizeof(float) * (size_t)rows * cols));
+    TT_CHECK(p->ensure(p->sino, sizeof(float) * std::max<size_t>(sino_elems, 1)));
+    TT_CHECK(p->ensure(p->circ, sizeof(float) * std::max<size_t>(circ_elems + herm_elems, 1)));
+    TT_CHECK(p->ensure(p->sig, sizeof(float) * std::max<size_t>(circ_elems + herm_elems, 1)));
+    TT_CUDA(cudaMemcpyAsync(p->in.p, image, sizeof(float) * (size_t)rows * cols,
+                            cudaMemcpyHostToDevice, st));
+    TT_CHECK(run_sinograms(p, (const float *)p->in.p, rows, cols, rows, n, ro, co, nullptr,
+                           angles_deg, A, tfuncs, n_t, tneed, (float *)p->sino.p, nullptr, st));
+    float *d_circ = (float *)p->circ.p, *d_herm = d_circ + circ_elems;
+    float *d_sig = (float *)p->sig.p, *d_hsig = d_sig + circ_elems;
+    if (A > 0 && n_t > 0) {
+        TT_CHECK(run_circus(p, (const float *)p->sino.p, n, A, n_t, pfuncs, n_p, nullptr, pneed,
+                            d_circ, st));
+        if (n_h > 0) {
+            std::vector<NosDesc> desc;
+            std::vector<int> c;
+            TT_CHECK(run_nos(p, (const float *)p->sino.p, n, A, n_t, st, desc, c));
+            for (int t = 0; t < n_t; t++) {
+                const int32_t c32 = c[t];
+                TT_CHECK(run_circus(p, (const float *)p->nos.p + desc[t].out_off, desc[t].m, A,
+                                    1, hpf.data(), n_h, &c32, hneed,
+                                    d_herm + (size_t)t * n_h * A, st));
+                if (centers)
+                    centers[t] = c32;
+            }
+        }
+        if (circ_elems + herm_elems > 0)
+            TT_CUDA(tt::launch_zscore(d_circ, n_t * (n_p + n_h), A, d_sig, st));
+    }
+    if (circus && circ_elems)
+        TT_CUDA(cudaMemcpyAsync(circus, d_circ, sizeof(float) * circ_elems,
+                                cudaMemcpyDeviceToHost, st));
+    if (signatures && circ_elems)
+        TT_CUDA(cudaMemcpyAsync(signatures, d_sig, sizeof(float) * circ_elems,
+                                cudaMemcpyDeviceToHost, st));
+    if (hermite_circus && herm_elems)
+        TT_CUDA(cudaMemcpyAsync(hermite_circus, d_herm, sizeof(float) * herm_elems,
+                                cudaMemcpyDeviceToHost, st));
+    if (hermite_signatures && herm_elems)
+        TT_CUDA(cudaMemcpyAsync(hermite_signatures, d_hsig, sizeof(float) * herm_elems,
+                                cudaMemcpyDeviceToHost, st));
+    TT_CUDA(cudaStreamSynchronize(st));
+    return TT_OK;
+}
+
+tt_status tt_transform_batch_sinograms_device(tt_plan *plan, float *d_out, int64_t capacity,
+                                              int64_t *count, void *stream) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    if (capacity < 0)
+        return fail(TT_ERR_INVALID_ARG, "negative capacity");
+    size_t n = 0;
+    if (p->batch) {
+        const int st = tt::batch_sinograms(p->batch, d_out, (size_t)capacity, &n,
+                                           pick_stream(p, stream));
+        if (st != TT_OK)
+            return (tt_status)st;
+    }
+    if (count)
+        *count = (int64_t)n;
+    return TT_OK;
+}
+
+tt_status tt_transform_batch_stage_ms(tt_plan *plan, float *ms) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    if (!ms)
+        return fail(TT_ERR_INVALID_ARG, "NULL output");
+    if (!p->batch)
+        return fail(TT_ERR_INVALID_ARG, "no batch has run on this plan");
+    return (tt_status)tt::batch_stage_ms(p->batch, ms);
+}
+
 // ---- backward ------------------------------------------------------------
 
 static tt_status check_grad_funcs(const int32_t *tfuncs, int n_t, const tt_pfunctional *pf,

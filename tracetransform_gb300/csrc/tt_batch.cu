@@ -163,6 +163,9 @@ class BatchEngine {
             cudaEventDestroy(ev_in_);
         if (ev_out_)
             cudaEventDestroy(ev_out_);
+        for (cudaEvent_t e : stage_ev_)
+            if (e)
+                cudaEventDestroy(e);
         if (own_)
             cudaStreamDestroy(own_);
     }
@@ -170,6 +173,8 @@ class BatchEngine {
     int run(const float *d_images, const long long *offsets, const int *rows, const int *cols,
             const int *steps, int n_img, const int32_t *tfuncs, int n_t,
             const tt_pfunctional *pf, int n_p, float *d_circus, float *d_sig, cudaStream_t st);
+    int sinograms(float *d_out, size_t capacity, size_t *count, cudaStream_t st);
+    int stage_ms(float ms[3]);
 
   private:
     int build(cudaStream_t st);
@@ -196,7 +201,7 @@ class BatchEngine {
     BatchCircusArgs cargs_{};
     size_t circ_smem_ = 0;
     int circ_blocks_ = 0, n_vec_ = 0, n_max_ = 0;
-    size_t out_floats_ = 0;
+    size_t out_floats_ = 0, sino_floats_ = 0;
     std::vector<int> trig_off_, tab_off_;
     Tune tune_;
     size_t sino_smem_ = 0;
@@ -206,6 +211,9 @@ class BatchEngine {
     // before the caller's stream by events
     cudaStream_t own_ = nullptr;
     cudaEvent_t ev_in_ = nullptr, ev_out_ = nullptr;
+    // recorded inside the graph around its three kernels (per-stage timing)
+    cudaEvent_t stage_ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool replayed_ = false;
 };
 
 void BatchEngine::release() {
@@ -282,6 +290,7 @@ int BatchEngine::build(cudaStream_t st) {
         out_total += (long long)n_t * n_p * na_[i];
     }
     out_floats_ = (size_t)out_total;
+    sino_floats_ = (size_t)sino_total;
     // textures (texel (u, v) = image row u, column v; border reads 0)
     tex_.resize(n_img);
     for (int i = 0; i < n_img; i++) {
@@ -520,11 +529,19 @@ int BatchEngine::capture(cudaStream_t st) {
                                      sizeof(float) * shape_.rows[i], shape_.cols[i],
                                      cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess)
+        e = cudaEventRecordWithFlags(stage_ev_[0], st, cudaEventRecordExternal);
+    if (e == cudaSuccess)
         e = launch_sino_batch(sargs_, tune_.lines, tune_.ctas_per_sm * dev_sms, sino_smem_, st);
+    if (e == cudaSuccess)
+        e = cudaEventRecordWithFlags(stage_ev_[1], st, cudaEventRecordExternal);
     if (e == cudaSuccess)
         e = launch_circus_batch(cargs_, circ_blocks_, circ_smem_, st);
     if (e == cudaSuccess)
+        e = cudaEventRecordWithFlags(stage_ev_[2], st, cudaEventRecordExternal);
+    if (e == cudaSuccess)
         e = launch_zscore_batch(circ_.p, voff_.p, vlen_.p, n_vec_, sig_.p, st);
+    if (e == cudaSuccess)
+        e = cudaEventRecordWithFlags(stage_ev_[3], st, cudaEventRecordExternal);
     const cudaError_t e_end = cudaStreamEndCapture(st, &graph);
     if (e != cudaSuccess) {
         if (graph)
@@ -556,6 +573,8 @@ int BatchEngine::run(const float *d_images, const long long *offsets, const int 
         B_CUDA(cudaStreamCreateWithFlags(&own_, cudaStreamNonBlocking));
         B_CUDA(cudaEventCreateWithFlags(&ev_in_, cudaEventDisableTiming));
         B_CUDA(cudaEventCreateWithFlags(&ev_out_, cudaEventDisableTiming));
+        for (cudaEvent_t &ev : stage_ev_)
+            B_CUDA(cudaEventCreate(&ev));
     }
     // the engine's stream starts after the caller's pending work (the images)
     B_CUDA(cudaEventRecord(ev_in_, st));
@@ -569,6 +588,7 @@ int BatchEngine::run(const float *d_images, const long long *offsets, const int 
         B_CHECK(capture(own_));
     }
     B_CUDA(cudaGraphLaunch(exec_, own_));
+    replayed_ = true;
     if (d_circus)
         B_CUDA(cudaMemcpyAsync(d_circus, circ_.p, sizeof(float) * out_floats_,
                                cudaMemcpyDeviceToDevice, own_));
@@ -578,6 +598,34 @@ int BatchEngine::run(const float *d_images, const long long *offsets, const int 
     // and the caller's stream continues after the results
     B_CUDA(cudaEventRecord(ev_out_, own_));
     B_CUDA(cudaStreamWaitEvent(st, ev_out_, 0));
+    return TT_OK;
+}
+
+// The last batch's sinograms, image after image in input order (each
+// n_t x n_angles x n), ordered after the last replay on the caller's stream.
+int BatchEngine::sinograms(float *d_out, size_t capacity, size_t *count, cudaStream_t st) {
+    *count = built_ ? sino_floats_ : 0;
+    if (!d_out || !built_ || sino_floats_ == 0)
+        return TT_OK;
+    if (capacity < sino_floats_)
+        return berr(TT_ERR_INVALID_ARG, "sinogram buffer smaller than the last batch's sinograms");
+    B_CUDA(cudaEventRecord(ev_in_, st));
+    B_CUDA(cudaStreamWaitEvent(own_, ev_in_, 0));
+    B_CUDA(cudaMemcpyAsync(d_out, sino_.p, sizeof(float) * sino_floats_, cudaMemcpyDeviceToDevice,
+                           own_));
+    B_CUDA(cudaEventRecord(ev_out_, own_));
+    B_CUDA(cudaStreamWaitEvent(st, ev_out_, 0));
+    return TT_OK;
+}
+
+// Device time of the last replay's sinogram, P-functional and z-score
+// kernels (events recorded inside the graph); waits for that replay.
+int BatchEngine::stage_ms(float ms[3]) {
+    if (!replayed_)
+        return berr(TT_ERR_INVALID_ARG, "no batch has run on this plan");
+    B_CUDA(cudaEventSynchronize(stage_ev_[3]));
+    for (int k = 0; k < 3; k++)
+        B_CUDA(cudaEventElapsedTime(&ms[k], stage_ev_[k], stage_ev_[k + 1]));
     return TT_OK;
 }
 
@@ -592,5 +640,12 @@ int batch_run(BatchEngine *b, const float *d_images, const long long *offsets, c
     return b->run(d_images, offsets, rows, cols, steps, n_img, tfuncs, n_t, pf, n_p, d_circus,
                   d_sig, st);
 }
+
+int batch_sinograms(BatchEngine *b, float *d_out, size_t capacity, size_t *count,
+                    cudaStream_t st) {
+    return b->sinograms(d_out, capacity, count, st);
+}
+
+int batch_stage_ms(BatchEngine *b, float ms[3]) { return b->stage_ms(ms); }
 
 } // namespace tt

@@ -73,6 +73,13 @@ int batch_run(BatchEngine *b, const float *d_images, const long long *offsets, c
               const int *cols, const int *steps, int n_img, const int32_t *tfuncs, int n_t,
               const tt_pfunctional *pf, int n_p, float *d_circus, float *d_sig,
               cudaStream_t st);
+// Copies the last batch's sinograms (input order, each n_t x A_i x N_i);
+// *count receives their float count (0 before the first batch).
+int batch_sinograms(BatchEngine *b, float *d_out, size_t capacity, size_t *count,
+                    cudaStream_t st);
+// Device milliseconds of the last replay's three kernels (sinograms,
+// P-functionals, z-scores), from events recorded inside the graph.
+int batch_stage_ms(BatchEngine *b, float ms[3]);
 
 // Backward pass (tt_backward.cu), T = float or double.  cs: (cos, sin) per
 // angle as the forward used them; cosv / sinv: cos, sin(2 pi j / rows);

@@ -211,6 +211,24 @@ class Engine:
             _ptr(signatures), _stream(flat)))
         return circus, signatures
 
+    def batch_sinograms(self, like: torch.Tensor) -> torch.Tensor:
+        """The sinograms behind the last transform_batch call, flat: image
+        after image in input order, each (nT, A_i, N_i)."""
+        count = ctypes.c_int64(0)
+        check(lib().tt_transform_batch_sinograms_device(self.plan.handle, None, 0,
+                                                        ctypes.byref(count), _stream(like)))
+        out = torch.empty(max(count.value, 1), dtype=torch.float32, device=like.device)
+        check(lib().tt_transform_batch_sinograms_device(self.plan.handle, _ptr(out), out.numel(),
+                                                        ctypes.byref(count), _stream(like)))
+        return out[:count.value]
+
+    def batch_stage_ms(self):
+        """Device ms of the last transform_batch call's sinogram, P-functional
+        and z-score kernels (waits for it)."""
+        ms = (ctypes.c_float * 3)()
+        check(lib().tt_transform_batch_stage_ms(self.plan.handle, ms))
+        return [float(v) for v in ms]
+
     def transform(self, image_cm: torch.Tensor, rows: int, cols: int, angles_deg, tfuncs,
                   pfuncs, out_sino=None):
         """Regular (non-orthonormal) transform on the device: returns
