@@ -96,6 +96,9 @@ def parse_args():
     ap.add_argument("--profile-steps", type=int, default=0, metavar="STEPS",
                     help="for profiler launch lists: run the workload's full device step "
                          "STEPS times and exit")
+    ap.add_argument("--images", type=int, default=0,
+                    help="with --profile-steps on batch512: only the first IMAGES images (a "
+                         "small case for profiler captures)")
     ap.add_argument("--tfuncs", default=None,
                     help="comma-separated T-functional ids overriding the workload's")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
@@ -964,6 +967,8 @@ def run_profile_steps(args):
     from tracetransform_gb300.device import Engine, to_colmajor
     if args.workload == "batch512":
         imgs, steps = make_batch()
+        if args.images:
+            imgs, steps = imgs[:args.images], steps[:args.images]
         bufs = [np.ascontiguousarray(im.ravel(order="F")) for im in imgs]
         offsets = np.zeros(len(bufs), np.int64)
         offsets[1:] = np.cumsum([b.size for b in bufs])[:-1]

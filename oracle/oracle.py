@@ -128,6 +128,14 @@ def t_at(f: int, x: np.ndarray, median: int) -> float:
     return float(lib().tto_t_at(int(f), _fp(x), x.size, int(median)))
 
 
+def t345_tables(which: int, n: int):
+    """T3/T4/T5 kernels re, im (n floats each) as the reference rounds them
+    (c++/src/functionals.cpp:136-198)."""
+    re, im = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    lib().tto_t345_prepare(int(which), int(n), _fp(re), _fp(im))
+    return re, im
+
+
 def weighted_median(x: np.ndarray) -> int:
     """findWeightedMedian (c++/src/functionals.cpp:21-30)."""
     x = np.ascontiguousarray(x, np.float32)

@@ -86,3 +86,40 @@ def test_zscore_mismatches(oracle_lib):
     assert zscore_mismatches(c, z) == 0
     z[1, 1, 7] = np.nextafter(z[1, 1, 7], np.float32(1e9))
     assert zscore_mismatches(c, z) == 1
+
+
+def test_conditioning_needs_the_engine_at_least_as_accurate(oracle_lib):
+    """A T3 entry off the reference's float value is excused only when the
+    exact value shows the engine no worse than the reference."""
+    from oracle.parity import t_exact
+    padded, ang, tfs, ref, med = _case(oracle_lib, (3,))
+    a = 4
+    line = int(np.argmax(ref[0, :, a]))
+    x = oracle_lib.rotate(padded, float(ang[a]))[:, line]
+    exact = t_exact(3, x, int(med[0, line, a]))
+    r = float(ref[0, line, a])
+    assert abs(r - exact) <= 1e-4 * abs(exact)
+    got = ref.copy()
+    got[0, line, a] = np.float32(exact * (1 + 5e-5))  # off the reference by up to ~1e-4
+    rep = account_sinograms(padded, ang, tfs, got, ref, med.copy(), med)
+    assert rep["unexplained"] == 0
+    got[0, line, a] = np.float32(exact * (1 + 3e-4))  # far from the exact value
+    rep = account_sinograms(padded, ang, tfs, got, ref, med.copy(), med)
+    assert rep["unexplained"] == 1
+
+
+def test_exact_values_follow_the_formulas(oracle_lib):
+    from oracle.parity import p_exact, t_exact
+    x = np.random.default_rng(2).random(41).astype(np.float32)
+    m = oracle_lib.weighted_median(x)
+    for f in (0, 1, 2):
+        want = float(oracle_lib.t_at(f, x, m))
+        assert abs(t_exact(f, x, m) - want) <= 1e-5 * abs(want)
+    sq = oracle_lib.weighted_median(np.sqrt(x))
+    for f in (3, 4, 5):
+        want = float(oracle_lib.t_at(f, x, sq))
+        assert abs(t_exact(f, x, sq) - want) <= 1e-4 * abs(want)
+    col = x.reshape(-1, 1)
+    for k in (1, 3):
+        want = float(oracle_lib.circus(col, [(k, 0, 0)])[0, 0])
+        assert abs(p_exact(k, x) - want) <= 1e-5 * abs(want)

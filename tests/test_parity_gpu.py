@@ -97,12 +97,14 @@ def test_golden_sinograms(oracle_lib, engine, name):
     dev = torch.from_numpy(np.ascontiguousarray(padded.T)).cuda()
     out, med = engine.sinograms(dev, n, n, ang, tfs, padded=True, medians=True)
     got, got_med = out.cpu().numpy().transpose(0, 2, 1), med.cpu().numpy().transpose(0, 2, 1)
-    # the host drop-in entry point is the same computation
-    host = np.stack(tt.getSinograms(padded, int(g["step"]), [str(t) for t in tfs]))
-    assert np.array_equal(host, got, equal_nan=True)
     rep = account_sinograms(padded, ang, tfs, got, g["sino"], got_med, None)
     record("golden:" + name, rep)
     assert_accounted(rep, name)
+    # the host drop-in entry point (which samples only the frame's non-zero
+    # box, so its sums are chunked differently) is accounted the same way
+    host = np.stack(tt.getSinograms(padded, int(g["step"]), [str(t) for t in tfs]))
+    rep = account_sinograms(padded, ang, tfs, host, g["sino"])
+    assert_accounted(rep, name + " (getSinograms)")
 
 
 @pytest.mark.parametrize("name", [n for n in GOLDEN if "ortho" not in n])

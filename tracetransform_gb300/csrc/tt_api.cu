@@ -27,6 +27,8 @@
 #endif
 
 using tt::CircusArgs;
+using tt::CircusStack;
+using tt::CircusStackArgs;
 using tt::NosDesc;
 using tt::SinoArgs;
 
@@ -153,6 +155,10 @@ struct tt_plan {
     std::map<std::vector<float>, float2 *> trig;        // angle list -> (c, s)
     std::map<std::vector<long>, const float **> herm_ptrs;
     DevBuf in, stretch, sino, circ, sig, region, nos, batch_in, batch_out, params;
+    // P-stage scratch: P3 partial sums, the exact-sort list of P2 (count + entries)
+    DevBuf cpart, cfb;
+    std::map<int, std::pair<float2 *, float *>> p3dft; // n -> twiddles, trapz weights
+    int sms = 0;
     // nearest orthonormal sinogram scratch (double matrices, V, norms, ...)
     DevBuf nos_a, nos_work, nos_desc, nos_off;
     // the QR and one Jacobi sweep as graphs, for the buffers and sizes they
@@ -249,7 +255,7 @@ struct tt_plan {
         for (void *p : owned)
             cudaFree(p);
         for (DevBuf *b : {&in, &sino, &circ, &sig, &region, &nos, &batch_in, &batch_out, &params,
-                          &nos_a, &nos_work, &nos_desc, &nos_off})
+                          &nos_a, &nos_work, &nos_desc, &nos_off, &cpart, &cfb})
             cudaFree(b->p);
         for (Graph *g : {&nos_factor_graph, &nos_sweep_graph})
             if (g->exec)
@@ -404,6 +410,23 @@ struct tt_plan {
         return TT_OK;
     }
 
+    tt_status get_p3dft(int n, const float2 **tw, const float **ck) {
+        auto it = p3dft.find(n);
+        if (it == p3dft.end()) {
+            std::vector<float2> t(n);
+            std::vector<float> c(n / 2 + 1);
+            tt::p3_dft_tables(n, t.data(), c.data());
+            float2 *dt;
+            float *dc;
+            TT_CHECK(upload(&dt, t));
+            TT_CHECK(upload(&dc, c));
+            it = p3dft.emplace(n, std::make_pair(dt, dc)).first;
+        }
+        *tw = it->second.first;
+        *ck = it->second.second;
+        return TT_OK;
+    }
+
     tt_status get_herm(int n, int order, int center, const float **out) {
         auto key = std::make_tuple(n, order, center);
         auto it = herm.find(key);
@@ -534,6 +557,53 @@ tt_status run_sinograms(tt_plan *p, const float *d_src, int src_rows, int src_co
     return TT_OK;
 }
 
+// P1-P3 without Hermite: P3 as a DFT computed like a GEMM, P1 / P2 one warp
+// per column (launch_circus_stacks), the stack descriptor passed by value.
+tt_status run_circus_stacks(tt_plan *p, const float *d_sino, int rows, int cols, int n_sino,
+                            const tt_pfunctional *pf, int n_p, unsigned need, float *d_out,
+                            cudaStream_t st) {
+    if (tt::circus_warp_smem_bytes(rows) > 227 * 1024)
+        return fail(TT_ERR_UNSUPPORTED, "sinogram length %d exceeds the shared-memory column "
+                                        "buffers", rows);
+    CircusStackArgs a{};
+    CircusStack &S = a.one;
+    S.sino = d_sino;
+    S.out = d_out;
+    S.n = rows;
+    S.angles = cols;
+    S.cols = cols * n_sino;
+    S.mtiles = (need & (1u << 3)) ? tt::p3_freq_tiles(rows) : 0;
+    if (need & (1u << 3))
+        TT_CHECK(p->get_p3dft(rows, &S.tw, &S.ck));
+    const size_t part = (size_t)S.mtiles * S.cols;
+    TT_CHECK(p->ensure(p->cpart, sizeof(float) * std::max<size_t>(part, 1)));
+    TT_CHECK(p->ensure(p->cfb, sizeof(int2) * ((size_t)S.cols + 1)));
+    S.partial = (float *)p->cpart.p;
+    a.st = nullptr;
+    a.n_st = 1;
+    a.total_tiles = S.mtiles * ((S.cols + 127) / 128);
+    a.total_cols = S.cols;
+    a.n_p = n_p;
+    for (int i = 0; i < n_p; i++)
+        a.kind[i] = pf[i].kind;
+    a.need = need;
+    a.stride = tt::circus_warp_stride(rows);
+    a.fb_count = (unsigned *)p->cfb.p;
+    a.fb_list = (int2 *)p->cfb.p + 1;
+    a.fb_capacity = S.cols;
+    int sl = 1;
+    while (sl < rows)
+        sl <<= 1;
+    a.sort_len_max = sl;
+    if (!p->sms)
+        TT_CUDA(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device));
+    a.fb_grid = 2 * p->sms;
+    if (sizeof(float) * (size_t)sl > 227 * 1024)
+        return fail(TT_ERR_UNSUPPORTED, "sinogram length %d exceeds the sort buffer", rows);
+    TT_CUDA(tt::launch_circus_stacks(a, tt::circus_warp_smem_bytes(rows), st));
+    return TT_OK;
+}
+
 tt_status run_circus(tt_plan *p, const float *d_sino, int rows, int cols, int n_sino,
                      const tt_pfunctional *pf, int n_p, const int32_t *centers, unsigned need,
                      float *d_out, cudaStream_t st) {
@@ -541,6 +611,8 @@ tt_status run_circus(tt_plan *p, const float *d_sino, int rows, int cols, int n_
         return TT_OK;
     if (rows <= 0)
         return fail(TT_ERR_INVALID_ARG, "sinograms need at least one row");
+    if (!(need & 1u) && (size_t)cols * n_sino <= 0x7fffffff / 8)
+        return run_circus_stacks(p, d_sino, rows, cols, n_sino, pf, n_p, need, d_out, st);
     CircusArgs a{};
     a.sino = d_sino;
     a.rows = rows;

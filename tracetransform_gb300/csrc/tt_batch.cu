@@ -191,16 +191,17 @@ class BatchEngine {
     std::vector<int> n_, ro_, co_, na_, order_;
     std::vector<long long> sino_off_, out_off_;
     DevArray<BatchImage> img_;
-    DevArray<BatchCircusImage> cimg_;
-    DevArray<float2> trig_, tab_, tables_;
-    DevArray<float> lin_, sino_, circ_, sig_;
+    DevArray<CircusStack> stacks_;
+    DevArray<float2> trig_, tab_, p3tw_;
+    DevArray<float> p3ck_, sino_, circ_, sig_, part_;
+    DevArray<int2> fb_;
     DevArray<unsigned> counter_;
     DevArray<long long> voff_;
     DevArray<int> vlen_;
     BatchSinoArgs sargs_{};
-    BatchCircusArgs cargs_{};
+    CircusStackArgs cargs_{};
     size_t circ_smem_ = 0;
-    int circ_blocks_ = 0, n_vec_ = 0, n_max_ = 0;
+    int n_vec_ = 0, n_max_ = 0;
     size_t out_floats_ = 0, sino_floats_ = 0;
     std::vector<int> trig_off_, tab_off_;
     Tune tune_;
@@ -310,17 +311,17 @@ int BatchEngine::build(cudaStream_t st) {
         B_CUDA(cudaCreateTextureObject(&tex_[i].tex, &res, &td, nullptr));
     }
     // rotation tables per distinct step, T3-T5 and P3 tables per distinct size
-    std::vector<float2> trig, tab, tables;
-    std::vector<float> lin;
+    std::vector<float2> trig, tab, p3tw;
+    std::vector<float> p3ck;
     std::map<int, int> step_at, tab_at;
-    std::map<int, long long> chirp_at;
-    std::vector<BatchCircusImage> cimg(n_img);
-    int col_begin = 0;
-    size_t circ_smem = 0;
+    std::map<int, std::pair<long long, long long>> p3_at;
     const bool p3 = std::find(shape_.pk.begin(), shape_.pk.end(), (int)TT_P3) != shape_.pk.end();
     unsigned pneed = 0;
     for (int k : shape_.pk)
         pneed |= 1u << k;
+    std::vector<CircusStack> stacks(n_img);
+    int col_begin = 0, tile_begin = 0, sort_len = 1;
+    long long part_total = 0;
     for (int i = 0; i < n_img; i++) {
         const int step = shape_.steps[i], n = n_[i];
         if (!step_at.count(step)) {
@@ -335,58 +336,50 @@ int BatchEngine::build(cudaStream_t st) {
             t345_tables(n, tab.data() + tab_at[n]);
         }
         tab_off_[i] = tab_at[n];
-        BatchCircusImage &c = cimg[i];
-        c.rows = n;
-        c.cols = na_[i];
-        c.col_begin = col_begin;
-        col_begin += n_t * na_[i];
-        c.M = p3 ? p3_fft_length(n) : 2;
-        int sl = 1;
-        while (sl < n)
-            sl <<= 1;
-        c.sort_len = sl;
-        c.sino_off = sino_off_[i];
-        c.out_off = out_off_[i];
-        if (p3) {
-            if (!chirp_at.count(n)) {
-                const int M = c.M;
-                chirp_at[n] = (long long)tables.size();
-                const size_t base = tables.size();
-                tables.resize(base + n + M + M / 2);
-                const size_t lbase = lin.size();
-                lin.resize(lbase + n);
-                std::vector<std::complex<double>> work(M);
-                p3_tables(n, tables.data() + base, tables.data() + base + n,
-                          tables.data() + base + n + M, lin.data() + lbase, work.data());
-                tab_at[-n] = (int)lbase; // linspace offset, keyed by -n
-            }
-            c.chirp_off = chirp_at[n];
-            c.filt_off = c.chirp_off + n;
-            c.twid_off = c.filt_off + c.M;
-            c.lin_off = tab_at[-n];
-        } else {
-            c.chirp_off = c.filt_off = c.twid_off = c.lin_off = 0;
+        if (p3 && !p3_at.count(n)) {
+            p3_at[n] = std::make_pair((long long)p3tw.size(), (long long)p3ck.size());
+            p3tw.resize(p3tw.size() + n);
+            p3ck.resize(p3ck.size() + n / 2 + 1);
+            p3_dft_tables(n, p3tw.data() + p3_at[n].first, p3ck.data() + p3_at[n].second);
         }
-        CircusArgs probe{};
-        probe.rows = n;
-        probe.M = c.M;
-        probe.sort_len = sl;
-        probe.need = pneed;
-        circ_smem = std::max(circ_smem, circus_smem_bytes(probe));
+        while (sort_len < n)
+            sort_len <<= 1;
+        CircusStack &c = stacks[i];
+        c.n = n;
+        c.angles = na_[i];
+        c.cols = n_t * na_[i];
+        c.mtiles = p3 ? p3_freq_tiles(n) : 0;
+        c.col_begin = col_begin;
+        c.tile_begin = tile_begin;
+        col_begin += c.cols;
+        tile_begin += c.mtiles * ((c.cols + 127) / 128);
+        part_total += (long long)c.mtiles * c.cols;
     }
-    if (tables.empty())
-        tables.push_back(make_float2(0.f, 0.f));
-    if (lin.empty())
-        lin.push_back(0.f);
+    if (p3tw.empty()) {
+        p3tw.push_back(make_float2(0.f, 0.f));
+        p3ck.push_back(0.f);
+    }
     B_CHECK(trig_.upload(trig, st));
     B_CHECK(tab_.upload(tab, st));
-    B_CHECK(tables_.upload(tables, st));
-    B_CHECK(lin_.upload(lin, st));
-    B_CHECK(cimg_.upload(cimg, st));
+    B_CHECK(p3tw_.upload(p3tw, st));
+    B_CHECK(p3ck_.upload(p3ck, st));
     B_CHECK(sino_.resize((size_t)std::max<long long>(sino_total, 1)));
     B_CHECK(circ_.resize(std::max<size_t>(out_floats_, 1)));
     B_CHECK(sig_.resize(std::max<size_t>(out_floats_, 1)));
     B_CHECK(counter_.resize(1));
+    B_CHECK(part_.resize((size_t)std::max<long long>(part_total, 1)));
+    B_CHECK(fb_.resize((size_t)col_begin + 1));
+    long long part_at = 0;
+    for (int i = 0; i < n_img; i++) {
+        CircusStack &c = stacks[i];
+        c.sino = sino_.p + sino_off_[i];
+        c.out = circ_.p + out_off_[i];
+        c.partial = part_.p + part_at;
+        part_at += (long long)c.mtiles * c.cols;
+        c.tw = p3 ? p3tw_.p + p3_at[n_[i]].first : nullptr;
+        c.ck = p3 ? p3ck_.p + p3_at[n_[i]].second : nullptr;
+    }
+    B_CHECK(stacks_.upload(stacks, st));
     // z-score vectors: n_t x n_p per image, length = its angle count
     std::vector<long long> voff;
     std::vector<int> vlen;
@@ -425,21 +418,26 @@ int BatchEngine::build(cudaStream_t st) {
     sargs_.tf_code = code;
     sargs_.n_t = n_t;
     sargs_.need = tneed;
-    cargs_ = BatchCircusArgs{};
-    cargs_.img = cimg_.p;
-    cargs_.n_img = n_img;
-    cargs_.n_sino = n_t;
+    cargs_ = CircusStackArgs{};
+    cargs_.st = stacks_.p;
+    cargs_.n_st = n_img;
+    cargs_.total_tiles = tile_begin;
+    cargs_.total_cols = col_begin;
     cargs_.n_p = n_p;
     for (int p = 0; p < n_p; p++)
         cargs_.kind[p] = shape_.pk[p];
     cargs_.need = pneed;
-    cargs_.sino = sino_.p;
-    cargs_.tables = tables_.p;
-    cargs_.lin = lin_.p;
-    cargs_.out = circ_.p;
-    circ_blocks_ = col_begin;
-    circ_smem_ = circ_smem;
-    B_CUDA(prepare_circus_batch(circ_smem_));
+    cargs_.stride = circus_warp_stride(n_max_);
+    cargs_.fb_count = reinterpret_cast<unsigned *>(fb_.p);
+    cargs_.fb_list = fb_.p + 1;
+    cargs_.fb_capacity = col_begin;
+    cargs_.sort_len_max = sort_len;
+    int sms = 0;
+    B_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+    cargs_.fb_grid = 2 * sms;
+    circ_smem_ = circus_warp_smem_bytes(n_max_);
+    if (circ_smem_ > 227 * 1024 || sizeof(float) * (size_t)sort_len > 227 * 1024)
+        return berr(TT_ERR_UNSUPPORTED, "batch image too large for the P-stage buffers");
     built_ = true;
     return TT_OK;
 }
@@ -535,7 +533,7 @@ int BatchEngine::capture(cudaStream_t st) {
     if (e == cudaSuccess)
         e = cudaEventRecordWithFlags(stage_ev_[1], st, cudaEventRecordExternal);
     if (e == cudaSuccess)
-        e = launch_circus_batch(cargs_, circ_blocks_, circ_smem_, st);
+        e = launch_circus_stacks(cargs_, circ_smem_, st);
     if (e == cudaSuccess)
         e = cudaEventRecordWithFlags(stage_ev_[2], st, cudaEventRecordExternal);
     if (e == cudaSuccess)

@@ -1,22 +1,28 @@
-// tt_circus.cu -- P-functional (circus) kernel and z-score kernel.
+// tt_circus.cu -- P-functional (circus) kernels and z-score kernel
+// (c++/src/circus.cpp:104-177 with c++/src/functionals.cpp:287-386).
 //
-// One CTA per sinogram column (one angle of one sinogram) computes every
-// requested P-functional of that column (c++/src/circus.cpp:104-177 with
-// c++/src/functionals.cpp:287-386):
-//   P1       sum |x[p] - x[p-1]|
-//   P2       bitonic sort in shared memory, weighted median of the sorted
-//            column weighted by itself
-//   P3       DFT of the real column by the chirp-z (Bluestein) identity on a
-//            power-of-two shared-memory FFT, then trapz(linspace(-1, 1),
-//            (|F_p| / N)^4) with the reference's mirror for p > N/2
-//   Hermite  projection on a host-built basis psi_order(z(p)) (the basis is
-//            evaluated on the host exactly as hermite_function does)
+// P1-P3 over stacks of sinogram columns (every call without Hermite, and
+// the batched engine), three launches:
+//   p3_dft_kernel      P3: the real DFT of every column as a GEMM-shaped
+//                      direct sum F = W^T X with |F_k / N|^4 and the trapz
+//                      weights folded into the epilogue (partial sums per
+//                      64-frequency tile, added in tile order: deterministic)
+//   circus_p12_kernel  one warp per column: P1 = sum |x[p] - x[p-1]|, P2 = the
+//                      weighted median of the column weighted by itself by
+//                      selection (tt_select.cuh, no sort), P3's tile sums
+//   p2_sort_kernel     P2 by an exact bitonic sort for the columns the
+//                      selection cannot take (negative or non-finite values)
+// circus_kernel (one CTA per column) serves calls with Hermite
+// P-functionals: P1, P2 by bitonic sort, P3 by the chirp-z (Bluestein)
+// identity on a power-of-two shared-memory FFT, and the Hermite projections
+// on a host-built basis psi_order(z(p)).
 // zscore_kernel follows c++/src/auxiliary.cpp:277-318 in the reference's own
 // order: a float mean, a double sum of squared float differences, n - 1.
 #include <climits>
 
 #include "tt_common.cuh"
 #include "tt_internal.h"
+#include "tt_select.cuh"
 
 namespace tt {
 namespace {
@@ -219,42 +225,6 @@ __global__ void __launch_bounds__(kThreads) circus_kernel(const CircusArgs a) {
     circus_column(a, blockIdx.y, blockIdx.x, smraw, red, redi);
 }
 
-// Batched P-stage: block b handles one column of one sinogram of one image;
-// images differ in sinogram length (rows), angle count (cols) and tables.
-__global__ void __launch_bounds__(kThreads) circus_batch_kernel(const BatchCircusArgs b) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ float red[kThreads / 32];
-    __shared__ int redi[kThreads / 32];
-    const int blk = blockIdx.x;
-    int lo = 0, hi = b.n_img - 1; // image whose column range holds blk
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (b.img[mid].col_begin <= blk)
-            lo = mid;
-        else
-            hi = mid - 1;
-    }
-    const BatchCircusImage im = b.img[lo];
-    const int k = blk - im.col_begin; // = sinogram * cols + column
-    CircusArgs a{};
-    a.sino = b.sino + im.sino_off;
-    a.rows = im.rows;
-    a.cols = im.cols;
-    a.n_sino = b.n_sino;
-    a.n_p = b.n_p;
-    for (int p = 0; p < b.n_p; p++)
-        a.kind[p] = b.kind[p];
-    a.chirp = b.tables + im.chirp_off;
-    a.filt = b.tables + im.filt_off;
-    a.twid = b.tables + im.twid_off;
-    a.lin = b.lin + im.lin_off;
-    a.M = im.M;
-    a.sort_len = im.sort_len;
-    a.need = b.need;
-    a.out = b.out + im.out_off;
-    circus_column(a, k / im.cols, k % im.cols, smraw, red, redi);
-}
-
 // z-score of vectors of varying length: vector v is in[off[v] .. off[v] + len[v]).
 __global__ void zscore_batch_kernel(const float *__restrict__ in, const long long *__restrict__ off,
                                     const int *__restrict__ len, float *__restrict__ out) {
@@ -265,6 +235,269 @@ __global__ void zscore_batch_kernel(const float *__restrict__ in, const long lon
 __global__ void zscore_kernel(const float *__restrict__ in, int len,
                               float *__restrict__ out) {
     zscore_vector(in + (size_t)blockIdx.x * len, len, out + (size_t)blockIdx.x * len);
+}
+
+// ---- P-stage over stacks --------------------------------------------------
+//
+// P3 as a direct DFT computed like a GEMM.  For a stack of columns X (n x
+// cols), F = W^T X with W[p][2k] = cos(2 pi k p / n), W[p][2k+1] =
+// -sin(2 pi k p / n), k <= n/2; the epilogue folds |F_k / n|^4 and the trapz
+// weights ck[k] into one partial sum per (64-frequency tile, column), which
+// the per-column kernel adds in tile order (deterministic).  A CTA computes a
+// 128 x 128 tile of F (64 frequencies as re/im rows x 128 columns) with an
+// 8 x 8 register tile per thread, samples staged 16 at a time through shared
+// memory (next step's global loads in flight during the current step's
+// FMAs); W is generated from the n-entry twiddle table with an incremental
+// (k p) mod n index.  The O(n^2) DFT replaces the Bluestein FFT's two
+// power-of-two transforms in shared memory: at these lengths the FMA pipe
+// runs it faster than the FFT's barrier-bound butterflies, and its float
+// error (accumulated over n terms) stays far inside the 1e-4 tolerance.
+constexpr int kDftBM = 128, kDftBN = 128, kDftBK = 16, kFreqTile = kDftBM / 2;
+
+__device__ __forceinline__ const CircusStack &stack_at(const CircusStackArgs &a, int i) {
+    return a.st ? a.st[i] : a.one;
+}
+
+__device__ __forceinline__ int stack_of(const CircusStack *st, int n_st, int v, bool by_tile) {
+    int lo = 0, hi = n_st - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const int b = by_tile ? __ldg(&st[mid].tile_begin) : __ldg(&st[mid].col_begin);
+        if (b <= v)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256, 2) p3_dft_kernel(const CircusStackArgs a) {
+    __shared__ __align__(16) float Ws[kDftBK][kDftBM];
+    __shared__ __align__(16) float Xs[kDftBK][kDftBN];
+    __shared__ float Red[16][kDftBN];
+    const int tile = blockIdx.x;
+    const CircusStack &S = stack_at(a, stack_of(a.st, a.n_st, tile, true));
+    const int n = S.n, cols = S.cols, K = n / 2 + 1;
+    const int local = tile - S.tile_begin;
+    const int mt = local % S.mtiles, ct = local / S.mtiles;
+    const int k0 = mt * kFreqTile, c0 = ct * kDftBN;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const float2 *tw = S.tw;
+    const float *x = S.sino;
+    // twiddles: frequency kk of the tile, samples pw .. pw + 3 of each step
+    const int kk = tid & 63, pw = (tid >> 6) * 4;
+    const int kg = k0 + kk;
+    const bool kval = kg < K;
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            acc[i][j] = 0.f;
+    float xr[8];
+    float2 wr[4];
+    auto load = [&](int p0) {
+        // (kg p) mod n for p = p0 + pw, then stepped by kg (kg < n, n < 46341)
+        unsigned idx = kval ? ((unsigned)kg * (unsigned)(p0 + pw)) % (unsigned)n : 0u;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int p = p0 + pw + j;
+            wr[j] = (kval && p < n) ? __ldg(tw + idx) : make_float2(0.f, 0.f);
+            idx += (unsigned)kg;
+            if (idx >= (unsigned)n)
+                idx -= (unsigned)n;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int e = tid + 256 * j;
+            const int col = e >> 4, p = p0 + (e & 15), gc = c0 + col;
+            xr[j] = (gc < cols && p < n) ? __ldg(x + (size_t)gc * n + p) : 0.f;
+        }
+    };
+    load(0);
+    for (int p0 = 0; p0 < n; p0 += kDftBK) {
+        __syncthreads(); // the previous step is done with Ws / Xs
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            Ws[pw + j][2 * kk] = wr[j].x;
+            Ws[pw + j][2 * kk + 1] = wr[j].y;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int e = tid + 256 * j;
+            Xs[e & 15][e >> 4] = xr[j];
+        }
+        __syncthreads();
+        if (p0 + kDftBK < n)
+            load(p0 + kDftBK);
+#pragma unroll
+        for (int q = 0; q < kDftBK; q++) {
+            const float4 a0 = *reinterpret_cast<const float4 *>(&Ws[q][ty * 4]);
+            const float4 a1 = *reinterpret_cast<const float4 *>(&Ws[q][64 + ty * 4]);
+            const float4 b0 = *reinterpret_cast<const float4 *>(&Xs[q][tx * 4]);
+            const float4 b1 = *reinterpret_cast<const float4 *>(&Xs[q][64 + tx * 4]);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+    }
+    // epilogue: rows (2f, 2f + 1) of the register tile are (re, im) of one
+    // frequency; ck |F / n|^4 summed over the thread's 4 frequencies
+    const float invn = 1.f / (float)n;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        float part = 0.f;
+#pragma unroll
+        for (int f = 0; f < 4; f++) {
+            const int freq = k0 + (f < 2 ? 0 : 32) + ty * 2 + (f & 1);
+            if (freq < K) {
+                const float re = acc[2 * f][j] * invn, im = acc[2 * f + 1][j] * invn;
+                const float s2 = re * re + im * im;
+                part = fmaf(__ldg(S.ck + freq), s2 * s2, part);
+            }
+        }
+        Red[ty][j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4)] = part;
+    }
+    __syncthreads();
+    if (tid < kDftBN) {
+        float sum = 0.f;
+#pragma unroll
+        for (int t = 0; t < 16; t++)
+            sum += Red[t][tid];
+        const int gc = c0 + tid;
+        if (gc < cols)
+            S.partial[(size_t)mt * cols + gc] = sum;
+    }
+}
+
+// P1, P2 and the P3 total of one column per warp (8 columns per CTA).  P2 is
+// the weighted selection of tt_select.cuh (no sort) for columns of finite,
+// non-negative values; any other column is listed for p2_sort_kernel.
+__global__ void __launch_bounds__(256) circus_p12_kernel(const CircusStackArgs a) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gcol = blockIdx.x * 8 + warp;
+    if (gcol >= a.total_cols)
+        return; // whole warps only: no CTA-wide barrier below
+    const int si = stack_of(a.st, a.n_st, gcol, false);
+    const CircusStack &S = stack_at(a, si);
+    const int c = gcol - S.col_begin, n = S.n;
+    const float *xg = S.sino + (size_t)c * n;
+    float *x = reinterpret_cast<float *>(smraw) + (size_t)warp * a.stride;
+    SelScratch *sc =
+        reinterpret_cast<SelScratch *>(reinterpret_cast<float *>(smraw) + 8 * (size_t)a.stride) +
+        warp;
+    float lsum = 0.f, lmax = 0.f;
+    bool bad = false;
+    for (int i = lane; i < n; i += 32) {
+        const float v = __ldg(xg + i);
+        x[i] = v;
+        lsum += v;
+        lmax = fmaxf(lmax, v);
+        bad |= !(v >= 0.f);
+    }
+    __syncwarp();
+    float v1 = 0.f, v2 = 0.f, v3 = 0.f;
+    if (a.need & (1u << 1)) {
+        float acc = 0.f;
+        for (int p = 1 + lane; p < n; p += 32)
+            acc += fabsf(x[p - 1] - x[p]);
+        v1 = warp_sum(acc);
+    }
+    if (a.need & (1u << 2)) {
+        const float xsum = warp_sum(lsum);
+        const float xmax = __int_as_float(warp_max(__float_as_int(lmax)));
+        if (__any_sync(TT_FULL_MASK, bad) || !(xsum < __int_as_float(0x7f800000))) {
+            if (lane == 0) {
+                const unsigned pos = atomicAdd(a.fb_count, 1u);
+                if (pos < (unsigned)a.fb_capacity)
+                    a.fb_list[pos] = make_int2(si, c);
+            }
+        } else {
+            v2 = select_p2(x, n, xmax, xsum, sc, lane);
+        }
+    }
+    if (lane == 0) {
+        if (a.need & (1u << 3)) {
+            float t = 0.f;
+            for (int m = 0; m < S.mtiles; m++)
+                t += S.partial[(size_t)m * S.cols + c];
+            v3 = n > 1 ? t * 0.5f : 0.f;
+        }
+        const int s = c / S.angles, ang = c - s * S.angles;
+        for (int p = 0; p < a.n_p; p++) {
+            const int k = a.kind[p];
+            if (k == 2 && bad)
+                continue; // written by p2_sort_kernel
+            S.out[((size_t)s * a.n_p + p) * S.angles + ang] = k == 1 ? v1 : k == 2 ? v2 : v3;
+        }
+    }
+}
+
+// PFunctional2 by an exact sort for the listed columns (values of any sign:
+// the reference sorts and walks the cumulative sum from the first element).
+__global__ void __launch_bounds__(kThreads) p2_sort_kernel(const CircusStackArgs a) {
+    extern __shared__ __align__(16) float srt[];
+    __shared__ float red[kThreads / 32];
+    __shared__ int redi[kThreads / 32];
+    const unsigned cnt = min(*a.fb_count, (unsigned)a.fb_capacity);
+    const int tid = threadIdx.x, bd = blockDim.x;
+    for (unsigned e = blockIdx.x; e < cnt; e += gridDim.x) {
+        const int2 it = a.fb_list[e];
+        const CircusStack &S = stack_at(a, it.x);
+        const int n = S.n, c = it.y;
+        int P = 1;
+        while (P < n)
+            P <<= 1;
+        const float *xg = S.sino + (size_t)c * n;
+        for (int i = tid; i < P; i += bd)
+            srt[i] = i < n ? xg[i] : __int_as_float(0x7f800000);
+        __syncthreads();
+        for (int k = 2; k <= P; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = tid; i < P; i += bd) {
+                    const int ixj = i ^ j;
+                    if (ixj > i) {
+                        const float u = srt[i], w = srt[ixj];
+                        const bool up = (i & k) == 0;
+                        if ((u > w) == up) {
+                            srt[i] = w;
+                            srt[ixj] = u;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        const int per = (n + bd - 1) / bd;
+        const int beg = min(tid * per, n), end = min(beg + per, n);
+        float loc = 0.f;
+        for (int i = beg; i < end; i++)
+            loc += srt[i];
+        float total;
+        float run = block_excl_scan(loc, red, &total);
+        int found = INT_MAX;
+        for (int i = beg; i < end; i++) {
+            run += srt[i];
+            if (2.f * run >= total) {
+                found = i;
+                break;
+            }
+        }
+        found = block_min(found, redi);
+        if (tid == 0) {
+            const float v = srt[found == INT_MAX ? n - 1 : found];
+            const int s = c / S.angles, ang = c - s * S.angles;
+            for (int p = 0; p < a.n_p; p++)
+                if (a.kind[p] == 2)
+                    S.out[((size_t)s * a.n_p + p) * S.angles + ang] = v;
+        }
+        __syncthreads();
+    }
 }
 
 } // namespace
@@ -290,26 +523,47 @@ cudaError_t launch_circus(const CircusArgs &a, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+int p3_freq_tiles(int n) { return (n / 2 + 1 + kFreqTile - 1) / kFreqTile; }
+
+int circus_warp_stride(int n_max) { return (n_max + 3) & ~3; }
+
+size_t circus_warp_smem_bytes(int n_max) {
+    return 8 * (sizeof(float) * (size_t)circus_warp_stride(n_max) + sizeof(SelScratch));
+}
+
+cudaError_t launch_circus_stacks(const CircusStackArgs &a, size_t smem, cudaStream_t st) {
+    if (a.total_cols <= 0 || a.n_p <= 0)
+        return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(a.fb_count, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess)
+        return e;
+    if ((a.need & (1u << 3)) && a.total_tiles > 0) {
+        p3_dft_kernel<<<a.total_tiles, 256, 0, st>>>(a);
+        if ((e = cudaGetLastError()) != cudaSuccess)
+            return e;
+    }
+    const size_t limit = opt_in_smem((const void *)circus_p12_kernel);
+    if (limit == 0 || smem > limit)
+        return cudaErrorInvalidValue;
+    circus_p12_kernel<<<(a.total_cols + 7) / 8, 256, smem, st>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess)
+        return e;
+    if (a.need & (1u << 2)) {
+        const size_t sm2 = sizeof(float) * (size_t)a.sort_len_max;
+        const size_t lim2 = opt_in_smem((const void *)p2_sort_kernel);
+        if (lim2 == 0 || sm2 > lim2)
+            return cudaErrorInvalidValue;
+        p2_sort_kernel<<<a.fb_grid, kThreads, sm2, st>>>(a);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
 cudaError_t launch_zscore(const float *in, int n_vec, int len, float *out,
                           cudaStream_t stream) {
     if (n_vec <= 0 || len <= 0)
         return cudaSuccess;
     zscore_kernel<<<n_vec, 128, 0, stream>>>(in, len, out);
-    return cudaGetLastError();
-}
-
-cudaError_t prepare_circus_batch(size_t smem) {
-    const size_t limit = opt_in_smem((const void *)circus_batch_kernel);
-    if (limit == 0)
-        return cudaErrorInvalidValue;
-    return smem > limit ? cudaErrorInvalidValue : cudaSuccess;
-}
-
-cudaError_t launch_circus_batch(const BatchCircusArgs &a, int blocks, size_t smem,
-                                cudaStream_t stream) {
-    if (blocks <= 0)
-        return cudaSuccess;
-    circus_batch_kernel<<<blocks, kThreads, smem, stream>>>(a);
     return cudaGetLastError();
 }
 

@@ -50,6 +50,46 @@ struct CircusArgs {
     float *out;           // n_sino x n_p x cols
 };
 
+// P-stage over stacks of columns (P1, P2, P3; no Hermite): P3 as a direct
+// DFT computed like a GEMM (F = W^T X per stack, |F|^4 and the trapz weights
+// folded into its epilogue), P1 and P2 one warp per column.
+struct CircusStack {
+    const float *sino;  // cols columns of n floats (n_sino sinograms x angles)
+    float *out;         // n_sino x n_p x angles
+    float *partial;     // P3: mtiles x cols partial sums of ck |F_k / n|^4
+    const float2 *tw;   // n twiddles (cos, -sin)(2 pi j / n)
+    const float *ck;    // n / 2 + 1 trapz weights
+    int n, angles, cols;
+    int mtiles;         // frequency tiles of 64 (P3)
+    int tile_begin;     // first P3 tile of this stack (flat over stacks)
+    int col_begin;      // first column (flat over stacks)
+};
+
+struct CircusStackArgs {
+    const CircusStack *st; // n_st descriptors in device memory, or NULL: `one`
+    CircusStack one;
+    int n_st;
+    int total_tiles, total_cols;
+    int n_p;
+    int kind[kMaxP];
+    unsigned need;      // bit k: P kind k requested
+    int stride;         // floats of shared memory per warp's column buffer
+    unsigned *fb_count; // P2 columns left to the exact sort (negative / non-finite)
+    int2 *fb_list;      // (stack, column) of those columns
+    int fb_capacity;
+    int sort_len_max;   // power of two >= the longest column (exact-sort fallback)
+    int fb_grid;        // CTAs of the exact-sort fallback
+};
+
+// Host tables of the direct-DFT P3 (tt_tables.cu): tw (n), ck (n / 2 + 1).
+void p3_dft_tables(int n, float2 *tw, float *ck);
+// P3 frequency tiles of a column length n.
+int p3_freq_tiles(int n);
+size_t circus_warp_smem_bytes(int n_max);
+int circus_warp_stride(int n_max);
+// The three launches of the P-stage over stacks (fb_count zeroed on stream).
+cudaError_t launch_circus_stacks(const CircusStackArgs &a, size_t smem, cudaStream_t st);
+
 // P3 tables (tt_tables.cu): FFT length M for a column of n samples, and the
 // chirp (n), filter (M), twiddles (M / 2) and linspace (n); work holds M.
 int p3_fft_length(int n);
@@ -147,28 +187,6 @@ size_t dynamic_smem_limit(const void *kernel);
 // 0 on failure.
 size_t opt_in_smem(const void *kernel);
 
-// Batched P-stage: one image's sinogram stack and tables.
-struct BatchCircusImage {
-    int rows, cols;        // sinogram length N and angle count A
-    int col_begin;         // first block index: blocks are n_sino * cols per image
-    int M, sort_len;       // P3 FFT length, power-of-two sort length
-    long long sino_off;    // into sino (n_sino x cols x rows floats)
-    long long out_off;     // into out (n_sino x n_p x cols floats)
-    long long chirp_off, filt_off, twid_off; // into tables (float2)
-    long long lin_off;     // into lin (float)
-};
-
-struct BatchCircusArgs {
-    const BatchCircusImage *img;
-    int n_img, n_sino, n_p;
-    int kind[kMaxP];
-    unsigned need;
-    const float *sino;
-    const float2 *tables;
-    const float *lin;
-    float *out;
-};
-
 // Batched sinograms: one image of a batch (device descriptor).
 struct BatchImage {
     cudaTextureObject_t tex; // the image, texel (u, v) = (row, col)
@@ -213,9 +231,6 @@ cudaError_t prepare_sino_batch(int lines, bool sel, size_t smem);
 int sino_batch_occupancy(int lines, bool sel, size_t smem);
 cudaError_t launch_sino_batch(const BatchSinoArgs &a, int lines, int grid, size_t smem,
                               cudaStream_t stream);
-cudaError_t prepare_circus_batch(size_t smem);
-cudaError_t launch_circus_batch(const BatchCircusArgs &a, int blocks, size_t smem,
-                                cudaStream_t stream);
 cudaError_t launch_zscore_batch(const float *in, const long long *off, const int *len,
                                 int n_vec, float *out, cudaStream_t stream);
 

@@ -157,7 +157,7 @@ __device__ __forceinline__ int sel_bin(float k, float klo, float bs) {
 // is refined in place: each round histograms [klo, khi], keeps the crossing
 // bin's keys (a strided sweep, so every write lands on an already-read slot)
 // until at most 64 remain or they are all equal.
-__device__ float sel_list_sqrt(float *keys, int count, float klo, float khi, float qs,
+inline __device__ float sel_list_sqrt(float *keys, int count, float klo, float khi, float qs,
                                unsigned long long below, unsigned long long total,
                                SelScratch *sc, int lane) {
     for (int level = 0; level < 16 && count > kSelList; level++) {
@@ -204,12 +204,29 @@ __device__ float sel_list_sqrt(float *keys, int count, float klo, float khi, flo
     return sel_finish(sc, count, below, total, khi, lane);
 }
 
+// Fixed-point weight of a sample v: sqrt(v) (T6, T7) or v itself (P2).
+struct SqrtWeight {
+    float qs;
+    __device__ __forceinline__ unsigned operator()(float v) const {
+        return __float2uint_rn(sqrt_nn(v) * qs);
+    }
+};
+struct LinearWeight {
+    float qs;
+    __device__ __forceinline__ unsigned operator()(float v) const {
+        return __float2uint_rn(v * qs);
+    }
+};
+
 // Interval refinement for a crossing bin that held more than 64 keys:
 // repeat histogram + compaction over [klo, khi] (the bin's key range).
-template <class KeyFn>
+template <class KeyFn, class WFn = SqrtWeight>
 __device__ float sel_refine(const float *x, int jlo, int j0, int j1, int per, KeyFn keyfn,
                             float qs, float klo, float khi, unsigned long long below,
-                            unsigned long long total, SelScratch *sc, int lane) {
+                            unsigned long long total, SelScratch *sc, int lane,
+                            WFn wfn = WFn{0.f}) {
+    if (wfn.qs == 0.f)
+        wfn.qs = qs;
     for (int level = 0; level < 8; level++) {
         if (!(khi > klo))
             return klo;
@@ -221,7 +238,7 @@ __device__ float sel_refine(const float *x, int jlo, int j0, int j1, int per, Ke
             const float v = x[j - jlo];
             const float k = keyfn(j, v);
             if (k >= klo && k <= khi)
-                atomicAdd(sc->hist + sel_bin(k, klo, bs), __float2uint_rn(sqrt_nn(v) * qs));
+                atomicAdd(sc->hist + sel_bin(k, klo, bs), wfn(v));
         }
         __syncwarp();
         const int d = sel_pick_bin(sc->hist, &below, total, lane);
@@ -238,7 +255,7 @@ __device__ float sel_refine(const float *x, int jlo, int j0, int j1, int per, Ke
                 k = keyfn(j, v);
                 if (k >= klo && k <= khi && sel_bin(k, klo, bs) == d) {
                     in = true;
-                    wq = __float2uint_rn(sqrt_nn(v) * qs);
+                    wq = wfn(v);
                     bmin = fminf(bmin, k);
                     bmax = fmaxf(bmax, k);
                 }
@@ -265,7 +282,7 @@ __device__ float sel_refine(const float *x, int jlo, int j0, int j1, int per, Ke
 // compacts its bin in place and refines on that list.  xmax and qtot (the
 // line's largest sample and sum of square roots) bound every key and weight
 // total, so no separate range pass is needed.
-__device__ void select_t67(float *x, int jlo, int jhi, int m1, int m2, bool want6,
+inline __device__ void select_t67(float *x, int jlo, int jhi, int m1, int m2, bool want6,
                            bool want7, float xmax, float qtot, SelScratch *s6, SelScratch *s7,
                            int lane, float *r6, float *r7) {
     *r6 = 0.f;
@@ -375,6 +392,66 @@ __device__ void select_t67(float *x, int jlo, int jhi, int m1, int m2, bool want
         mx = __int_as_float(warp_max(__float_as_int(mx)));
         *r7 = sel_list_sqrt(x, c, mn, mx, qs, below, W7, s7, lane);
     }
+}
+
+// PFunctional2 of one non-negative column (c++/src/functionals.cpp:303-311):
+// the column sorted, weighted by itself, its weighted median -- the smallest
+// value v with 2 * sum(x <= v) >= sum(x), found without sorting.  x: the
+// column in shared memory, n values, xmax their maximum, xsum their sum (a
+// bound for the fixed-point scale).  One warp.
+inline __device__ float select_p2(const float *x, int n, float xmax, float xsum, SelScratch *sc,
+                           int lane) {
+    if (n <= 0)
+        return 0.f;
+    if (!(xmax > 0.f) || !(xsum > 0.f))
+        return 0.f; // all zero: the first sorted value
+    const int per = ((n + 31) >> 5) | 1;
+    const int j0 = min(lane * per, n), j1 = min(j0 + per, n);
+    const float qb = xsum * 1.001f;
+    const int E = ((__float_as_int(qb) >> 23) & 0xff) - 126;
+    const float qs = __int_as_float((127 + 30 - E) << 23);
+    const LinearWeight wfn{qs};
+    const float bs = (float)kSelBins / xmax;
+    for (int i = lane; i < kSelBins; i += 32)
+        sc->hist[i] = 0u;
+    __syncwarp();
+    unsigned lw = 0;
+    for (int j = j0; j < j1; j++) {
+        const float v = x[j];
+        const unsigned wq = wfn(v);
+        lw += wq;
+        atomicAdd(sc->hist + sel_bin(v, 0.f, bs), wq);
+    }
+    const unsigned long long W = __reduce_add_sync(TT_FULL_MASK, lw);
+    __syncwarp();
+    unsigned long long below = 0;
+    const int d = sel_pick_bin(sc->hist, &below, W, lane);
+    __syncwarp();
+    int c = 0;
+    float mn = __int_as_float(0x7f800000), mx = 0.f;
+    for (int i = 0; i < per; i++) {
+        const int j = j0 + i;
+        bool in = false;
+        float k = 0.f;
+        unsigned wq = 0;
+        if (j < j1) {
+            k = x[j];
+            if (sel_bin(k, 0.f, bs) == d) {
+                in = true;
+                wq = wfn(k);
+                mn = fminf(mn, k);
+                mx = fmaxf(mx, k);
+            }
+        }
+        sel_append(sc, &c, in, k, wq, lane);
+    }
+    mn = __int_as_float(warp_min(__float_as_int(mn)));
+    mx = __int_as_float(warp_max(__float_as_int(mx)));
+    __syncwarp();
+    if (c <= kSelList)
+        return sel_finish(sc, c, below, W, mx, lane);
+    auto key = [](int, float v) { return v; };
+    return sel_refine(x, 0, j0, j1, per, key, qs, mn, mx, below, W, sc, lane, wfn);
 }
 
 } // namespace tt
