@@ -320,17 +320,23 @@ tt_status tt_transform_batch_stage_ms(tt_plan *plan, float *ms);
  * (n_sino x n_p x cols, the layout of tt_circus_device + tt_zscore_device),
  * for callers that cannot allocate device memory while they run -- a plugin
  * whose host application's allocator owns all device memory, or a loop that
- * cannot afford cudaMalloc/cudaFree stalls.  It allocates nothing: the raw
- * circus values and the P3 tables live in one file-scope device array of
- * 1048576 floats (4 MiB) that every GPU loading the library holds until the
- * process exits; larger requests (n_sino * n_p * cols plus, with P3, about
- * 5 * rows floats of tables) fail with TT_ERR_INVALID_ARG, P3 needs
- * rows <= 8192, and Hermite is TT_ERR_UNSUPPORTED (use tt_circus_device).
- * The first call on a device looks up the array's device address (set-up);
- * make that first call before any stream capture.  Every call shares the
- * array and it keeps the last call's contents (nothing in it needs to start
- * at zero); calls that overlap on the GPU race on it.  stream: a CUDA stream
- * handle, NULL for the legacy default stream. */
+ * cannot afford cudaMalloc/cudaFree stalls.  It runs the kernels of
+ * tt_circus_device (same results, bit for bit) and allocates nothing: their
+ * scratch -- raw circus values, P3 partial sums and tables, the P2 sort list --
+ * lives in one file-scope device array of 1048576 floats (4 MiB) that every
+ * GPU loading the library holds until the process exits.  Requests whose
+ * scratch exceeds it fail with TT_ERR_INVALID_ARG (about n_sino * cols *
+ * (n_p + 2) floats, plus with P3 n_sino * cols * ceil((rows / 2 + 1) / 64) +
+ * 2.5 rows); P3 needs rows <= 2048 (TT_ERR_INVALID_ARG beyond); Hermite is
+ * TT_ERR_UNSUPPORTED (use tt_circus_device).  The first call on a device
+ * looks up the array's device address; with CUDA's lazy module loading it is
+ * also where the array is allocated, so make that first call before any
+ * region that must not allocate (or set CUDA_MODULE_LOADING=EAGER), and
+ * before any stream capture.  cudaDeviceReset between calls is not supported.
+ * Every call shares the array and it keeps the last call's contents (the one
+ * counter that must start at zero is cleared by each call on its stream);
+ * calls that overlap on the GPU race on it.  stream: a CUDA stream handle,
+ * NULL for the legacy default stream. */
 tt_status tt_circus_zscore_noalloc(const float *d_sino, int rows, int cols, int n_sino,
                                    const tt_pfunctional *pfuncs, int n_p, float *d_signatures,
                                    void *stream);

@@ -413,13 +413,12 @@ struct tt_plan {
     tt_status get_p3dft(int n, const float2 **tw, const float **ck) {
         auto it = p3dft.find(n);
         if (it == p3dft.end()) {
-            std::vector<float2> t(n);
-            std::vector<float> c(n / 2 + 1);
-            tt::p3_dft_tables(n, t.data(), c.data());
             float2 *dt;
             float *dc;
-            TT_CHECK(upload(&dt, t));
-            TT_CHECK(upload(&dc, c));
+            TT_CHECK(upload(&dt, std::vector<float2>(n)));
+            TT_CHECK(upload(&dc, std::vector<float>(n / 2 + 1)));
+            TT_CUDA(tt::launch_p3_dft_tables(n, dt, dc, stream));
+            TT_CUDA(cudaStreamSynchronize(stream));
             it = p3dft.emplace(n, std::make_pair(dt, dc)).first;
         }
         *tw = it->second.first;
@@ -562,6 +561,37 @@ tt_status run_sinograms(tt_plan *p, const float *d_src, int src_rows, int src_co
 tt_status run_circus_stacks(tt_plan *p, const float *d_sino, int rows, int cols, int n_sino,
                             const tt_pfunctional *pf, int n_p, unsigned need, float *d_out,
                             cudaStream_t st) {
+    if ((need & (1u << 3)) && rows > tt::kP3DftMaxRows) {
+        // P3 of long columns: the chirp-z FFT kernel (its accumulation error
+        // does not grow with the column as the direct DFT's does), the rest here
+        CircusArgs a{};
+        a.sino = d_sino;
+        a.rows = rows;
+        a.cols = cols;
+        a.n_sino = n_sino;
+        a.n_p = n_p;
+        for (int i = 0; i < n_p; i++)
+            a.kind[i] = pf[i].kind;
+        a.need = 1u << 3;
+        a.out = d_out;
+        int sl = 1;
+        while (sl < rows)
+            sl <<= 1;
+        a.sort_len = sl;
+        const FftTables *f;
+        TT_CHECK(p->get_fft(rows, &f));
+        a.M = f->M;
+        a.chirp = f->chirp;
+        a.filt = f->filt;
+        a.twid = f->twid;
+        a.lin = f->lin;
+        if (tt::circus_smem_bytes(a) > 227 * 1024)
+            return fail(TT_ERR_UNSUPPORTED, "sinogram length %d exceeds the FFT buffers", rows);
+        TT_CUDA(tt::launch_circus(a, st));
+        need &= ~(1u << 3);
+        if (!(need & ((1u << 1) | (1u << 2))))
+            return TT_OK;
+    }
     if (tt::circus_warp_smem_bytes(rows) > 227 * 1024)
         return fail(TT_ERR_UNSUPPORTED, "sinogram length %d exceeds the shared-memory column "
                                         "buffers", rows);
@@ -585,7 +615,7 @@ tt_status run_circus_stacks(tt_plan *p, const float *d_sino, int rows, int cols,
     a.total_cols = S.cols;
     a.n_p = n_p;
     for (int i = 0; i < n_p; i++)
-        a.kind[i] = pf[i].kind;
+        a.kind[i] = (need & (1u << pf[i].kind)) ? pf[i].kind : -1; // -1: written elsewhere
     a.need = need;
     a.stride = tt::circus_warp_stride(rows);
     a.fb_count = (unsigned *)p->cfb.p;

@@ -340,7 +340,6 @@ int BatchEngine::build(cudaStream_t st) {
             p3_at[n] = std::make_pair((long long)p3tw.size(), (long long)p3ck.size());
             p3tw.resize(p3tw.size() + n);
             p3ck.resize(p3ck.size() + n / 2 + 1);
-            p3_dft_tables(n, p3tw.data() + p3_at[n].first, p3ck.data() + p3_at[n].second);
         }
         while (sort_len < n)
             sort_len <<= 1;
@@ -363,6 +362,10 @@ int BatchEngine::build(cudaStream_t st) {
     B_CHECK(tab_.upload(tab, st));
     B_CHECK(p3tw_.upload(p3tw, st));
     B_CHECK(p3ck_.upload(p3ck, st));
+    for (const auto &kv : p3_at)
+        B_CUDA(launch_p3_dft_tables(kv.first, p3tw_.p + kv.second.first,
+                                    p3ck_.p + kv.second.second, st));
+    B_CUDA(cudaStreamSynchronize(st));
     B_CHECK(sino_.resize((size_t)std::max<long long>(sino_total, 1)));
     B_CHECK(circ_.resize(std::max<size_t>(out_floats_, 1)));
     B_CHECK(sig_.resize(std::max<size_t>(out_floats_, 1)));
@@ -435,6 +438,9 @@ int BatchEngine::build(cudaStream_t st) {
     int sms = 0;
     B_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
     cargs_.fb_grid = 2 * sms;
+    if (p3 && n_max_ > kP3DftMaxRows)
+        return berr(TT_ERR_UNSUPPORTED, "batched P3 takes padded sides up to 2048 (images up to "
+                                        "about 1440 px); transform larger images one by one");
     circ_smem_ = circus_warp_smem_bytes(n_max_);
     if (circ_smem_ > 227 * 1024 || sizeof(float) * (size_t)sort_len > 227 * 1024)
         return berr(TT_ERR_UNSUPPORTED, "batch image too large for the P-stage buffers");

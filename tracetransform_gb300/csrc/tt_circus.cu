@@ -214,7 +214,8 @@ __device__ __forceinline__ void circus_column(const CircusArgs &a, int sidx, int
 
     if (tid == 0) {
         for (int p = 0; p < a.n_p; p++)
-            a.out[((size_t)sidx * a.n_p + p) * a.cols + colidx] = res[p];
+            if (a.need & (1u << a.kind[p])) // kinds left to another kernel stay as they are
+                a.out[((size_t)sidx * a.n_p + p) * a.cols + colidx] = res[p];
     }
 }
 
@@ -431,8 +432,8 @@ __global__ void __launch_bounds__(256) circus_p12_kernel(const CircusStackArgs a
         const int s = c / S.angles, ang = c - s * S.angles;
         for (int p = 0; p < a.n_p; p++) {
             const int k = a.kind[p];
-            if (k == 2 && bad)
-                continue; // written by p2_sort_kernel
+            if (k < 1 || (k == 2 && bad))
+                continue; // written by another kernel (P2: p2_sort_kernel)
             S.out[((size_t)s * a.n_p + p) * S.angles + ang] = k == 1 ? v1 : k == 2 ? v2 : v3;
         }
     }
@@ -520,6 +521,46 @@ cudaError_t launch_circus(const CircusArgs &a, cudaStream_t stream) {
         return cudaErrorInvalidValue;
     dim3 grid(a.cols, a.n_sino);
     circus_kernel<<<grid, kThreads, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+// Tables of the direct-DFT P3, built on the device so that every path (plans,
+// batches, the allocation-free entry point) uses bit-identical values:
+// tw[j] = (cos, -sin)(2 pi j / n) from sincospi in double, rounded to float;
+// ck[k] = the trapz weight of bin k summed over the positions that read it
+// (the reference's mirror reads bin n - p for p > n/2), each position's
+// weight (lin[p] - lin[p-1]) + (lin[p+1] - lin[p]) with the reference's
+// float linspace (c++/src/functionals.cpp:332-356); P3 = 0.5 sum_k ck |F_k/n|^4.
+__global__ void p3_dft_tables_kernel(int n, float2 *__restrict__ tw, float *__restrict__ ck) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) {
+        double sv, cv;
+        sincospi(2.0 * (double)j / (double)n, &sv, &cv);
+        tw[j] = make_float2((float)cv, (float)-sv);
+    }
+    if (j <= n / 2) {
+        double acc = 0.0;
+        if (n > 1) {
+            auto lin = [n](int p) { return (float)(-1 + p * 2.0 / (n - 1)); };
+            const int pos[2] = {j, n - j};
+            for (int q = 0; q < 2; q++) {
+                const int p = pos[q];
+                if (p >= n || (q == 1 && p == j))
+                    continue;
+                if (p > 0)
+                    acc += (double)__fsub_rn(lin(p), lin(p - 1));
+                if (p + 1 < n)
+                    acc += (double)__fsub_rn(lin(p + 1), lin(p));
+            }
+        }
+        ck[j] = (float)acc;
+    }
+}
+
+cudaError_t launch_p3_dft_tables(int n, float2 *tw, float *ck, cudaStream_t st) {
+    if (n <= 0)
+        return cudaSuccess;
+    p3_dft_tables_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, tw, ck);
     return cudaGetLastError();
 }
 

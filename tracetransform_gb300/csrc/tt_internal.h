@@ -81,8 +81,10 @@ struct CircusStackArgs {
     int fb_grid;        // CTAs of the exact-sort fallback
 };
 
-// Host tables of the direct-DFT P3 (tt_tables.cu): tw (n), ck (n / 2 + 1).
-void p3_dft_tables(int n, float2 *tw, float *ck);
+// Device tables of the direct-DFT P3: tw (n), ck (n / 2 + 1), built on stream.
+cudaError_t launch_p3_dft_tables(int n, float2 *tw, float *ck, cudaStream_t st);
+// Longest column whose P3 the direct DFT computes (longer ones: the FFT kernel).
+constexpr int kP3DftMaxRows = 2048;
 // P3 frequency tiles of a column length n.
 int p3_freq_tiles(int n);
 size_t circus_warp_smem_bytes(int n_max);

@@ -9,13 +9,22 @@
 // file-scope array below, which every GPU that loads this library holds
 // until the process exits.
 //
-// The array holds the raw circus functions (the intermediate between the
-// P-functional kernel and the z-score kernel) and, when P3 is requested, the
-// P3 tables.  Every call shares it and it keeps the last call's contents:
-// nothing in it needs to start at zero (every element is written before it is
-// read), but calls that overlap on the GPU -- on different streams, or from
-// different host threads -- race on it.
-#include <complex>
+// It runs the same kernels as the allocating path (tt_circus_device: the
+// direct-DFT P3, the warp-per-column P1/P2, the exact-sort fallback of P2,
+// then the z-scores), with their scratch carved out of the array: the raw
+// circus functions, the P3 partial sums, the P3 tables (built on the device
+// by a kernel, so nothing is copied from the host) and the P2 fallback list.
+// Every call shares the array and it keeps the last call's contents: the
+// fallback counter, the only part that must start at zero, is cleared by the
+// call on its stream before use; calls that overlap on the GPU -- on
+// different streams, or from different host threads -- race on it.
+//
+// The array's device address is looked up once per device (the first call
+// made with that device current); with CUDA's lazy module loading that first
+// call is also where the driver loads this module and allocates the array,
+// so make it before any region that must not allocate (or run with
+// CUDA_MODULE_LOADING=EAGER).  The cached address does not survive
+// cudaDeviceReset.
 #include <cstdio>
 #include <mutex>
 
@@ -25,19 +34,12 @@
 namespace {
 
 constexpr size_t kScratchFloats = size_t(1) << 20; // 4 MiB
-constexpr int kMaxRowsP3 = 8192;                    // P3 FFT length <= 16384
 constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) float g_noalloc_scratch[kScratchFloats];
 
 std::mutex g_setup_mu;
 float *g_scratch_addr[kMaxDevices]; // device address of the array, per device
-
-// host staging for the P3 tables (static: the call allocates nothing)
-std::mutex g_tables_mu;
-float2 g_chirp[kMaxRowsP3], g_filt[2 * kMaxRowsP3], g_twid[kMaxRowsP3];
-float g_lin[kMaxRowsP3];
-std::complex<double> g_work[2 * kMaxRowsP3];
 
 size_t align64(size_t floats) { return (floats + 63) & ~size_t(63); } // 256 bytes
 
@@ -77,23 +79,36 @@ extern "C" tt_status tt_circus_zscore_noalloc(const float *d_sino, int rows, int
         need |= 1u << pfuncs[p].kind;
     }
     const bool p3 = need & (1u << TT_P3);
-    if (p3 && rows > kMaxRowsP3)
+    if (p3 && rows > tt::kP3DftMaxRows)
         return fail(TT_ERR_INVALID_ARG,
                     "P3 without allocation supports sinograms of at most %d rows, got %d",
-                    kMaxRowsP3, rows);
-    const int M = p3 ? tt::p3_fft_length(rows) : 0;
-    // layout: circus | chirp | filter | twiddles | linspace (256-byte aligned)
+                    tt::kP3DftMaxRows, rows);
+    const size_t total_cols = (size_t)n_sino * cols;
+    if (total_cols > 0x7fffffffu / 8)
+        return fail(TT_ERR_INVALID_ARG, "%d sinograms of %d columns exceed the column limit",
+                    n_sino, cols);
+    if (tt::circus_warp_smem_bytes(rows) > 227 * 1024)
+        return fail(TT_ERR_UNSUPPORTED, "sinogram length %d exceeds the shared-memory buffers",
+                    rows);
+    const int mtiles = p3 ? tt::p3_freq_tiles(rows) : 0;
+    // layout (256-byte aligned): circus | P3 partials | twiddles | trapz
+    // weights | P2 fallback count + list (int2)
     const size_t circ_floats = (size_t)n_sino * n_p * cols;
-    const size_t off_chirp = align64(circ_floats);
-    const size_t off_filt = off_chirp + (p3 ? align64(2 * (size_t)rows) : 0);
-    const size_t off_twid = off_filt + (p3 ? align64(2 * (size_t)M) : 0);
-    const size_t off_lin = off_twid + (p3 ? align64((size_t)M) : 0);
-    const size_t total = off_lin + (p3 ? align64((size_t)rows) : 0);
+    const size_t off_part = align64(circ_floats);
+    const size_t off_tw = off_part + (p3 ? align64((size_t)mtiles * total_cols) : 0);
+    const size_t off_ck = off_tw + (p3 ? align64(2 * (size_t)rows) : 0);
+    const size_t off_fb = off_ck + (p3 ? align64((size_t)rows / 2 + 1) : 0);
+    const size_t total = off_fb + align64(2 * (total_cols + 1));
     if (total > kScratchFloats)
         return fail(TT_ERR_INVALID_ARG,
-                    "%d x %d circus values plus tables need %ld floats of scratch; the "
+                    "%d x %d circus values plus scratch need %ld floats; the "
                     "allocation-free limit is 1048576 floats (4 MiB)",
                     n_sino * n_p, cols, (long)total);
+    int sl = 1;
+    while (sl < rows)
+        sl <<= 1;
+    if (sizeof(float) * (size_t)sl > 227 * 1024)
+        return fail(TT_ERR_UNSUPPORTED, "sinogram length %d exceeds the sort buffer", rows);
 
     // one-time set-up per device: the array's device address
     int dev = 0;
@@ -103,6 +118,7 @@ extern "C" tt_status tt_circus_zscore_noalloc(const float *d_sino, int rows, int
     if (dev < 0 || dev >= kMaxDevices)
         return fail(TT_ERR_UNSUPPORTED, "device %d beyond the %d supported", dev, kMaxDevices);
     float *scratch;
+    int sms = 0;
     {
         std::lock_guard<std::mutex> lock(g_setup_mu);
         if (!g_scratch_addr[dev]) {
@@ -114,51 +130,46 @@ extern "C" tt_status tt_circus_zscore_noalloc(const float *d_sino, int rows, int
         }
         scratch = g_scratch_addr[dev];
     }
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaDeviceGetAttribute");
     cudaStream_t st = (cudaStream_t)stream;
 
-    tt::CircusArgs a{};
-    a.sino = d_sino;
-    a.rows = rows;
-    a.cols = cols;
-    a.n_sino = n_sino;
+    tt::CircusStackArgs a{};
+    tt::CircusStack &S = a.one;
+    S.sino = d_sino;
+    S.out = scratch;
+    S.n = rows;
+    S.angles = cols;
+    S.cols = (int)total_cols;
+    S.mtiles = mtiles;
+    S.partial = scratch + off_part;
+    if (p3) {
+        float2 *tw = reinterpret_cast<float2 *>(scratch + off_tw);
+        float *ck = scratch + off_ck;
+        e = tt::launch_p3_dft_tables(rows, tw, ck, st);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "P3 table kernel");
+        S.tw = tw;
+        S.ck = ck;
+    }
+    a.st = nullptr;
+    a.n_st = 1;
+    a.total_tiles = mtiles * (int)((total_cols + 127) / 128);
+    a.total_cols = (int)total_cols;
     a.n_p = n_p;
     for (int p = 0; p < n_p; p++)
         a.kind[p] = pfuncs[p].kind;
     a.need = need;
-    a.out = scratch;
-    int sl = 1;
-    while (sl < rows)
-        sl <<= 1;
-    a.sort_len = sl;
-    if (p3) {
-        a.M = M;
-        a.chirp = reinterpret_cast<const float2 *>(scratch + off_chirp);
-        a.filt = reinterpret_cast<const float2 *>(scratch + off_filt);
-        a.twid = reinterpret_cast<const float2 *>(scratch + off_twid);
-        a.lin = scratch + off_lin;
-        // copies from pageable host memory return once the source is staged,
-        // so the static staging buffers may be reused right after
-        std::lock_guard<std::mutex> lock(g_tables_mu);
-        tt::p3_tables(rows, g_chirp, g_filt, g_twid, g_lin, g_work);
-        const struct {
-            size_t off, bytes;
-            const void *src;
-        } copies[4] = {{off_chirp, sizeof(float2) * rows, g_chirp},
-                       {off_filt, sizeof(float2) * M, g_filt},
-                       {off_twid, sizeof(float2) * (M / 2), g_twid},
-                       {off_lin, sizeof(float) * rows, g_lin}};
-        for (const auto &c : copies) {
-            e = cudaMemcpyAsync(scratch + c.off, c.src, c.bytes, cudaMemcpyHostToDevice, st);
-            if (e != cudaSuccess)
-                return cuda_fail(e, "cudaMemcpyAsync(P3 tables)");
-        }
-    }
-    if (tt::circus_smem_bytes(a) > 227 * 1024)
-        return fail(TT_ERR_UNSUPPORTED, "sinogram length %d exceeds the shared-memory buffers",
-                    rows);
-    e = tt::launch_circus(a, st);
+    a.stride = tt::circus_warp_stride(rows);
+    a.fb_count = reinterpret_cast<unsigned *>(scratch + off_fb);
+    a.fb_list = reinterpret_cast<int2 *>(scratch + off_fb) + 1;
+    a.fb_capacity = (int)total_cols;
+    a.sort_len_max = sl;
+    a.fb_grid = 2 * sms;
+    e = tt::launch_circus_stacks(a, tt::circus_warp_smem_bytes(rows), st);
     if (e != cudaSuccess)
-        return cuda_fail(e, "circus kernel");
+        return cuda_fail(e, "circus kernels");
     e = tt::launch_zscore(scratch, n_sino * n_p, cols, d_signatures, st);
     if (e != cudaSuccess)
         return cuda_fail(e, "z-score kernel");

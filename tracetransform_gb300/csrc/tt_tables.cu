@@ -9,7 +9,6 @@
 // and the reference's linspace(-1, 1, N) rounded as it rounds it.  All are
 // computed here in double and rounded once to float.
 #include <cmath>
-#include <vector>
 #include <complex>
 
 #include "tt_internal.h"
@@ -70,35 +69,6 @@ void p3_tables(int n, float2 *chirp, float2 *filt, float2 *twid, float *lin,
                               (float)std::sin(-2.0 * M_PI * k / m));
     for (int p = 0; p < n; p++)
         lin[p] = (float)(-1 + p * 2.0 / (n - 1));
-}
-
-// Tables of the direct-DFT form of PFunctional3 (c++/src/functionals.cpp:
-// 332-360): tw[j] = (cos, -sin)(2 pi j / n), so that F_k = sum_p x_p
-// tw[(k p) mod n]; and ck[k] (k <= n/2), the trapz weight of |F_k / n|^4
-// summed over the positions p that read bin k (the reference's mirror reads
-// bin n - p for p > n/2): ck[k] = sum (lin[p] - lin[p-1]) + (lin[p+1] - lin[p])
-// over those p, with the reference's float linspace, so that
-// P3 = 0.5 sum_k ck[k] |F_k / n|^4.
-void p3_dft_tables(int n, float2 *tw, float *ck) {
-    for (int j = 0; j < n; j++) {
-        const double t = 2.0 * M_PI * (double)j / (double)n;
-        tw[j] = make_float2((float)std::cos(t), (float)-std::sin(t));
-    }
-    std::vector<float> lin(n);
-    for (int p = 0; p < n; p++)
-        lin[p] = (float)(-1 + p * 2.0 / (n - 1));
-    std::vector<double> acc(n / 2 + 1, 0.0);
-    for (int p = 0; p < n; p++) {
-        const int k = p <= n / 2 ? p : n - p;
-        double w = 0.0;
-        if (p > 0)
-            w += (double)(lin[p] - lin[p - 1]);
-        if (p + 1 < n)
-            w += (double)(lin[p + 1] - lin[p]);
-        acc[k] += w;
-    }
-    for (int k = 0; k <= n / 2; k++)
-        ck[k] = (float)acc[k];
 }
 
 // pad() of c++/src/auxiliary.cpp:257-275: side N of the zero frame that holds
