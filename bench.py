@@ -461,6 +461,7 @@ def run_batch(args, world, rank, local_rank):
         batched()
     torch.cuda.synchronize()
     barrier(world)
+    tile = eng.batch_tile()
     clocks = ClockSampler(local_rank)
     clocks.start()
     stages = []
@@ -534,6 +535,8 @@ def run_batch(args, world, rank, local_rank):
         "images_per_s": job_rate(len(imgs), world, ms),
         "gpu_launches": 3 * args.steps,
         "stage_ms": {"sinograms": sino_ms, "circus": circ_ms, "zscore": z_ms},
+        "tile": {"lines_per_cta": tile[0], "ctas_per_sm": tile[1], "lines_per_warp": tile[2],
+                 "chosen_by": "the engine's autotuner (timed on this batch)"},
         "roofline": {"bound": "hbm", "kernel": "sino_batch_kernel", "achieved": achieved,
                      "peak": peak, "peak_source": peak_kind, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,

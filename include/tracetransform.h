@@ -314,6 +314,15 @@ tt_status tt_transform_batch_sinograms_device(tt_plan *plan, float *d_out, int64
  * CUDA events recorded inside the captured graph; waits for that call. */
 tt_status tt_transform_batch_stage_ms(tt_plan *plan, float *ms);
 
+/* The persistent sinogram kernel's tile shape, tile = {lines per CTA, CTAs
+ * per SM, lines per warp}: lines per warp 0 is the CTA kernel (one warp per
+ * line, 8 or 4 lines per CTA, every T-functional); 1, 2 or 4 the
+ * warp-autonomous kernel (each warp samples and reduces that many lines of
+ * its own; T0-T5 only).  pin = 0: reads the shape the last batch used (the
+ * autotuner's choice).  pin != 0: fixes *tile for the following batches
+ * instead of tuning (CTAs per SM 0 returns to the tuner). */
+tt_status tt_transform_batch_tile(tt_plan *plan, int32_t *tile, int32_t pin);
+
 /* ---- allocation-free entry point ---------------------------------------- */
 /* No counterpart in the reference.  P1 / P2 / P3 circus functions of n_sino
  * stacked rows x cols sinograms (device), z-scored into d_signatures

@@ -27,12 +27,15 @@ def _images():
     return imgs, STEPS + [3]
 
 
-def run_batch(imgs, steps, tfs, pfs):
-    """The batch through tt_transform_batch_device; returns per image
-    (sinograms (nT, N, A), circus (nT, nP, A), signatures (nT, nP, A))."""
+def run_batch(imgs, steps, tfs, pfs, tile=None):
+    """The batch through tt_transform_batch_device (tile: a pinned tile shape
+    (lines per CTA, CTAs per SM, lines per warp), else the tuner's); returns
+    per image (sinograms (nT, N, A), circus (nT, nP, A), signatures)."""
     import torch
     from tracetransform_gb300.device import Engine
     eng = Engine(0)
+    if tile:
+        eng.batch_tile(pin=tile)
     bufs = [np.ascontiguousarray(np.asarray(im, np.float32).ravel(order="F")) for im in imgs]
     offsets = np.zeros(len(bufs), np.int64)
     offsets[1:] = np.cumsum([b.size for b in bufs])[:-1]
@@ -43,6 +46,8 @@ def run_batch(imgs, steps, tfs, pfs):
                                     [(k, -1, -1) for k in pfs])
     sino = eng.batch_sinograms(flat)
     torch.cuda.synchronize()
+    if tile:
+        assert eng.batch_tile() == tuple(tile)
     circ, sig, sino = circ.cpu().numpy(), sig.cpu().numpy(), sino.cpu().numpy()
     out, so, co = [], 0, 0
     for r, c, s in zip(rows, cols, steps):
@@ -58,11 +63,11 @@ def run_batch(imgs, steps, tfs, pfs):
     return out
 
 
-def account_batch(O, name, imgs, steps, tfs, pfs):
+def account_batch(O, name, imgs, steps, tfs, pfs, tile=None):
     pf = [(k, 0, 0) for k in pfs]
     totals = {"entries": 0, "median_ties": 0, "selection_ties": 0}
-    for i, (img, step, (sino, circ, sig)) in enumerate(zip(imgs, steps,
-                                                           run_batch(imgs, steps, tfs, pfs))):
+    results = run_batch(imgs, steps, tfs, pfs, tile)
+    for i, (img, step, (sino, circ, sig)) in enumerate(zip(imgs, steps, results)):
         padded = O.pad(img)
         ang = O.angles_for_step(step)
         ref = O.sinograms(padded, ang, tfs)
@@ -85,6 +90,25 @@ def account_batch(O, name, imgs, steps, tfs, pfs):
 def test_batch_vs_oracle(oracle_lib, tfs):
     imgs, steps = _images()
     account_batch(oracle_lib, f"batch11_T{''.join(map(str, tfs))}", imgs, steps, tfs, [1, 2, 3])
+
+
+@pytest.mark.parametrize("tile", [(8, 1, 0), (4, 2, 0), (4, 1, 1), (8, 1, 2), (16, 1, 4)])
+def test_batch_every_tile_shape_vs_oracle(oracle_lib, tile):
+    """Every tile shape the tuner can pick, pinned, T0-T5 (and T6/T7 for the
+    CTA kernel's shapes)."""
+    imgs, steps = _images()
+    account_batch(oracle_lib, f"batch11_tile{tile}", imgs, steps, [0, 1, 2, 3, 4, 5], [1, 2, 3],
+                  tile)
+    if tile[2] == 0:
+        account_batch(oracle_lib, f"batch11_T67_tile{tile}", imgs, steps, [6, 7, 1], [1],
+                      tile)
+
+
+def test_batch_pinned_warp_tile_rejects_t6():
+    from tracetransform_gb300._native import TTError
+    imgs, steps = _images()
+    with pytest.raises(TTError):
+        run_batch(imgs[:3], steps[:3], [0, 6], [1], (8, 1, 2))
 
 
 def test_batch512_images_vs_oracle(oracle_lib):

@@ -1052,6 +1052,28 @@ tt_status tt_transform_batch_stage_ms(tt_plan *plan, float *ms) {
     return (tt_status)tt::batch_stage_ms(p->batch, ms);
 }
 
+tt_status tt_transform_batch_tile(tt_plan *plan, int32_t *tile, int32_t pin) {
+    tt_plan *p;
+    TT_CHECK(resolve_plan(plan, &p));
+    if (!tile)
+        return fail(TT_ERR_INVALID_ARG, "NULL tile");
+    if (!p->batch)
+        p->batch = tt::batch_create(p->device);
+    int t[3] = {tile[0], tile[1], tile[2]};
+    if (pin) {
+        if (t[1] > 0 && !((t[2] == 0 && (t[0] == 8 || t[0] == 4)) ||
+                          t[2] == 1 || t[2] == 2 || t[2] == 4))
+            return fail(TT_ERR_INVALID_ARG, "tile: lines per CTA 8 or 4 (lines per warp 0), or "
+                                            "lines per warp 1, 2 or 4");
+        tt::batch_pin_tile(p->batch, t);
+        return TT_OK;
+    }
+    tt::batch_tile(p->batch, t);
+    for (int i = 0; i < 3; i++)
+        tile[i] = t[i];
+    return TT_OK;
+}
+
 // ---- backward ------------------------------------------------------------
 
 static tt_status check_grad_funcs(const int32_t *tfuncs, int n_t, const tt_pfunctional *pf,

@@ -102,8 +102,12 @@ struct Shape {
     }
 };
 
+// Tile shape of the persistent sinogram kernel: lpw = 0 -- the CTA kernel
+// with `lines` lines per CTA (one warp per line, the CTA sampling them
+// together); lpw = 1, 2, 4 -- the warp-autonomous kernel, lpw lines per warp
+// (T0-T5 only).  ctas_per_sm sizes the persistent grid.
 struct Tune {
-    int lines = 8, ctas_per_sm = 0;
+    int lines = 8, ctas_per_sm = 0, lpw = 0;
 };
 
 std::string tune_cache_path() {
@@ -113,7 +117,7 @@ std::string tune_cache_path() {
     return std::string(home ? home : "/tmp") + "/.cache/tracetransform_gb300_autotune.json";
 }
 
-// The cache is a flat JSON object {"key": [lines, ctas_per_sm], ...}.
+// The cache is a flat JSON object {"key": [lines, ctas_per_sm, lpw], ...}.
 std::map<std::string, Tune> load_tune_cache() {
     std::map<std::string, Tune> m;
     std::ifstream f(tune_cache_path());
@@ -129,7 +133,8 @@ std::map<std::string, Tune> load_tune_cache() {
             break;
         const std::string key = s.substr(pos + 1, end - pos - 1);
         Tune t;
-        if (sscanf(s.c_str() + end + 1, " : [ %d , %d ]", &t.lines, &t.ctas_per_sm) == 2)
+        if (sscanf(s.c_str() + end + 1, " : [ %d , %d , %d ]", &t.lines, &t.ctas_per_sm,
+                   &t.lpw) == 3)
             m[key] = t;
         pos = end + 1;
     }
@@ -148,7 +153,7 @@ void save_tune_cache(const std::map<std::string, Tune> &m) {
     size_t i = 0;
     for (const auto &kv : m)
         f << "  \"" << kv.first << "\": [" << kv.second.lines << ", " << kv.second.ctas_per_sm
-          << "]" << (++i < m.size() ? ",\n" : "\n");
+          << ", " << kv.second.lpw << "]" << (++i < m.size() ? ",\n" : "\n");
     f << "}\n";
 }
 
@@ -175,11 +180,24 @@ class BatchEngine {
             const tt_pfunctional *pf, int n_p, float *d_circus, float *d_sig, cudaStream_t st);
     int sinograms(float *d_out, size_t capacity, size_t *count, cudaStream_t st);
     int stage_ms(float ms[3]);
+    void tile(int out[3]) const {
+        out[0] = tune_.lines;
+        out[1] = tune_.ctas_per_sm;
+        out[2] = tune_.lpw;
+    }
+    void pin(const int t[3]) {
+        pinned_ = t[1] > 0;
+        pin_.lines = t[0];
+        pin_.ctas_per_sm = t[1];
+        pin_.lpw = t[2];
+        built_ = false; // the next call rebuilds and captures with the pinned shape
+    }
 
   private:
     int build(cudaStream_t st);
     int make_desc(int lines, std::vector<BatchImage> &desc, int *total_items) const;
-    int set_tile(int lines, cudaStream_t st);
+    int set_tile(const Tune &t, cudaStream_t st);
+    cudaError_t launch_sino(const Tune &t, int grid, cudaStream_t st);
     int autotune(cudaStream_t st);
     int capture(cudaStream_t st);
     void release();
@@ -204,7 +222,8 @@ class BatchEngine {
     int n_vec_ = 0, n_max_ = 0;
     size_t out_floats_ = 0, sino_floats_ = 0;
     std::vector<int> trig_off_, tab_off_;
-    Tune tune_;
+    Tune tune_, pin_;
+    bool pinned_ = false;
     size_t sino_smem_ = 0;
     cudaGraphExec_t exec_ = nullptr;
     // the graph is captured on and replayed from the engine's own stream
@@ -255,17 +274,29 @@ int BatchEngine::make_desc(int lines, std::vector<BatchImage> &desc, int *total_
     return TT_OK;
 }
 
-int BatchEngine::set_tile(int lines, cudaStream_t st) {
+int BatchEngine::set_tile(const Tune &t, cudaStream_t st) {
     std::vector<BatchImage> desc;
     int total = 0;
-    B_CHECK(make_desc(lines, desc, &total));
+    B_CHECK(make_desc(t.lpw ? t.lpw : t.lines, desc, &total));
     B_CHECK(img_.upload(desc, st));
-    sino_smem_ = sino_smem_bytes(n_max_, lines, sargs_.need);
-    B_CUDA(prepare_sino_batch(lines, sargs_.need & ((1u << 6) | (1u << 7)), sino_smem_));
+    if (t.lpw) {
+        sino_smem_ = sino_warp_smem_bytes(n_max_, t.lpw);
+        if (sino_batch_warp_occupancy(t.lpw, sino_smem_) <= 0)
+            return berr(TT_ERR_UNSUPPORTED, "warp tile does not fit the batch's largest image");
+        sargs_.stride = sino_warp_stride(n_max_, t.lpw);
+    } else {
+        sino_smem_ = sino_smem_bytes(n_max_, t.lines, sargs_.need);
+        B_CUDA(prepare_sino_batch(t.lines, sargs_.need & ((1u << 6) | (1u << 7)), sino_smem_));
+        sargs_.stride = sino_stride(n_max_, t.lines);
+    }
     sargs_.img = img_.p;
     sargs_.total_items = total;
-    sargs_.stride = sino_stride(n_max_, lines);
     return TT_OK;
+}
+
+cudaError_t BatchEngine::launch_sino(const Tune &t, int grid, cudaStream_t st) {
+    return t.lpw ? launch_sino_batch_warp(sargs_, t.lpw, grid, sino_smem_, st)
+                 : launch_sino_batch(sargs_, t.lines, grid, sino_smem_, st);
 }
 
 int BatchEngine::build(cudaStream_t st) {
@@ -461,14 +492,21 @@ int BatchEngine::autotune(cudaStream_t st) {
         n_min = std::min(n_min, n_[i]);
         angles += na_[i];
     }
+    if (pinned_) {
+        const bool sel = sargs_.need & ((1u << 6) | (1u << 7));
+        if (pin_.lpw && sel)
+            return berr(TT_ERR_UNSUPPORTED, "lines-per-warp tiles compute T0-T5 only");
+        tune_ = pin_;
+        return set_tile(tune_, st);
+    }
     std::ostringstream key;
-    key << prop.name << "|n" << n_min << "-" << n_max_ << "|imgs" << n_.size() << "|angles"
-        << angles << "|need" << sargs_.need;
+    key << "v2|" << prop.name << "|n" << n_min << "-" << n_max_ << "|imgs" << n_.size()
+        << "|angles" << angles << "|need" << sargs_.need;
     std::map<std::string, Tune> cache = load_tune_cache();
     auto hit = cache.find(key.str());
     if (hit != cache.end()) {
         tune_ = hit->second;
-        return set_tile(tune_.lines, st);
+        return set_tile(tune_, st);
     }
     // load the images once so the timed runs see real data
     for (int i = 0; i < (int)n_.size(); i++)
@@ -481,26 +519,50 @@ int BatchEngine::autotune(cudaStream_t st) {
     B_CUDA(cudaEventCreate(&e1));
     float best = 1e30f;
     Tune best_t;
+    best_t.ctas_per_sm = 0;
     const bool sel = sargs_.need & ((1u << 6) | (1u << 7));
+    // candidates: the CTA kernel with 8 or 4 lines per CTA, and (T0-T5) the
+    // warp-autonomous kernel with 1, 2 or 4 lines per warp; each at its
+    // occupancy and at half of it
+    std::vector<Tune> shapes;
     for (int lines : {8, 4}) {
-        const size_t smem = sino_smem_bytes(n_max_, lines, sargs_.need);
-        const int occ = sino_batch_occupancy(lines, sel, smem);
+        Tune t;
+        t.lines = lines;
+        t.lpw = 0;
+        shapes.push_back(t);
+    }
+    if (!sel)
+        for (int lpw : {1, 2, 4}) {
+            Tune t;
+            t.lines = lpw * sino_warp_cta_warps();
+            t.lpw = lpw;
+            shapes.push_back(t);
+        }
+    for (Tune t : shapes) {
+        int occ;
+        if (t.lpw) {
+            occ = sino_batch_warp_occupancy(t.lpw, sino_warp_smem_bytes(n_max_, t.lpw));
+        } else {
+            const size_t smem = sino_smem_bytes(n_max_, t.lines, sargs_.need);
+            occ = sino_batch_occupancy(t.lines, sel, smem);
+        }
         if (occ <= 0)
             continue;
-        B_CHECK(set_tile(lines, st));
+        if (set_tile(t, st) != TT_OK)
+            continue;
         for (int per_sm : {occ, std::max(1, occ / 2)}) {
             float ms = 0.f;
             for (int rep = 0; rep < 2; rep++) { // first run warms up
                 B_CUDA(cudaMemsetAsync(counter_.p, 0, sizeof(unsigned), st));
                 B_CUDA(cudaEventRecord(e0, st));
-                B_CUDA(launch_sino_batch(sargs_, lines, per_sm * dev_sms, sino_smem_, st));
+                B_CUDA(launch_sino(t, per_sm * dev_sms, st));
                 B_CUDA(cudaEventRecord(e1, st));
                 B_CUDA(cudaEventSynchronize(e1));
                 B_CUDA(cudaEventElapsedTime(&ms, e0, e1));
             }
             if (ms < best) {
                 best = ms;
-                best_t.lines = lines;
+                best_t = t;
                 best_t.ctas_per_sm = per_sm;
             }
             if (per_sm == 1)
@@ -514,7 +576,7 @@ int BatchEngine::autotune(cudaStream_t st) {
     tune_ = best_t;
     cache[key.str()] = tune_;
     save_tune_cache(cache);
-    return set_tile(tune_.lines, st);
+    return set_tile(tune_, st);
 }
 
 int BatchEngine::capture(cudaStream_t st) {
@@ -535,7 +597,7 @@ int BatchEngine::capture(cudaStream_t st) {
     if (e == cudaSuccess)
         e = cudaEventRecordWithFlags(stage_ev_[0], st, cudaEventRecordExternal);
     if (e == cudaSuccess)
-        e = launch_sino_batch(sargs_, tune_.lines, tune_.ctas_per_sm * dev_sms, sino_smem_, st);
+        e = launch_sino(tune_, tune_.ctas_per_sm * dev_sms, st);
     if (e == cudaSuccess)
         e = cudaEventRecordWithFlags(stage_ev_[1], st, cudaEventRecordExternal);
     if (e == cudaSuccess)
@@ -651,5 +713,9 @@ int batch_sinograms(BatchEngine *b, float *d_out, size_t capacity, size_t *count
 }
 
 int batch_stage_ms(BatchEngine *b, float ms[3]) { return b->stage_ms(ms); }
+
+void batch_tile(BatchEngine *b, int out[3]) { b->tile(out); }
+
+void batch_pin_tile(BatchEngine *b, const int t[3]) { b->pin(t); }
 
 } // namespace tt

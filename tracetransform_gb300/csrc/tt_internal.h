@@ -122,6 +122,10 @@ int batch_sinograms(BatchEngine *b, float *d_out, size_t capacity, size_t *count
 // Device milliseconds of the last replay's three kernels (sinograms,
 // P-functionals, z-scores), from events recorded inside the graph.
 int batch_stage_ms(BatchEngine *b, float ms[3]);
+// The persistent kernel's tile {lines per CTA, CTAs per SM, lines per warp
+// (0: one per warp)}; pinning one with CTAs per SM > 0 replaces the tuner.
+void batch_tile(BatchEngine *b, int out[3]);
+void batch_pin_tile(BatchEngine *b, const int t[3]);
 
 // Backward pass (tt_backward.cu), T = float or double.  cs: (cos, sin) per
 // angle as the forward used them; cosv / sinv: cos, sin(2 pi j / rows);
@@ -216,6 +220,15 @@ int sino_lines_per_block(int n, unsigned need);
 size_t sino_smem_bytes(int n, int lines, unsigned need);
 int sino_stride(int n, int lines);
 cudaError_t launch_sinograms(const SinoArgs &a, int lines, cudaStream_t stream);
+// Warp-autonomous sinogram kernels for T0-T5: each warp samples and reduces
+// lpw (1, 2 or 4) lines of its own; the CTA kernels above serve T6 / T7.
+int sino_warp_stride(int n, int lpw);
+size_t sino_warp_smem_bytes(int n, int lpw);
+int sino_warp_cta_warps();
+cudaError_t launch_sinograms_warp(const SinoArgs &a, int lpw, cudaStream_t stream);
+int sino_batch_warp_occupancy(int lpw, size_t smem);
+cudaError_t launch_sino_batch_warp(const BatchSinoArgs &a, int lpw, int grid, size_t smem,
+                                   cudaStream_t stream);
 cudaError_t launch_rotate(cudaTextureObject_t tex, int rows, int cols, float c, float s,
                           float *out, cudaStream_t stream);
 // resize() of the orthonormal mode; column-major device buffers.

@@ -450,6 +450,350 @@ __global__ void __launch_bounds__(32 * L)
     }
 }
 
+// ---- warp-autonomous lines (T0-T5) -------------------------------------------
+//
+// A warp owns LPW adjacent lines of one angle: each segment of SW = 32 / LPW
+// lanes samples its line into its own shared-memory row and reduces it, with
+// segment-wide (width SW) shuffles, so a warp's fixed per-line work -- scans,
+// crossing searches, reductions, the output writes -- is shared by LPW lines
+// when lines are short.  Warps never wait for one another (no CTA barrier);
+// the lines' rows are laid out so that the sampling stores (LPW lines x SW
+// consecutive rows per instruction) and the chunked reads (chunk length C odd,
+// line rows SW banks apart) are free of bank conflicts.
+
+template <int SW> __device__ __forceinline__ float seg_sum(float v) {
+#pragma unroll
+    for (int d = SW / 2; d > 0; d >>= 1)
+        v += __shfl_xor_sync(TT_FULL_MASK, v, d);
+    return v;
+}
+
+template <int SW> __device__ __forceinline__ int seg_min(int v) {
+#pragma unroll
+    for (int d = SW / 2; d > 0; d >>= 1)
+        v = min(v, __shfl_xor_sync(TT_FULL_MASK, v, d));
+    return v;
+}
+
+template <int SW> __device__ __forceinline__ float seg_incl_scan(float v, int sub) {
+#pragma unroll
+    for (int d = 1; d < SW; d <<= 1) {
+        const float t = __shfl_up_sync(TT_FULL_MASK, v, d, SW);
+        if (sub >= d)
+            v += t;
+    }
+    return v;
+}
+
+// The ballot bits of segment s (bit i: lane i of the segment).
+template <int SW> __device__ __forceinline__ unsigned seg_ballot(bool p, int s) {
+    const unsigned b = __ballot_sync(TT_FULL_MASK, p);
+    return SW == 32 ? b : (b >> (s * SW)) & ((1u << (SW & 31)) - 1u);
+}
+
+// find_crossing per segment; every lane runs the same (warp-uniform) loops.
+template <bool kSqrt, int SW>
+__device__ int seg_find_crossing(const float *x, int C, float inc, float exc, float total, int s,
+                                 int sub) {
+    const unsigned ball = seg_ballot<SW>(2.f * inc >= total, s);
+    int ln = ball ? __ffs(ball) - 1 : SW;
+    int found = INT_MAX;
+    bool active = ln < SW;
+    while (__any_sync(TT_FULL_MASK, active)) {
+        float basev = __shfl_sync(TT_FULL_MASK, exc, s * SW + min(ln, SW - 1));
+        for (int t0 = 0; t0 < C; t0 += SW) {
+            const int t = t0 + sub;
+            const bool in = active && t < C;
+            const float v = in ? elem<kSqrt>(x, ln * C + t) : 0.f;
+            const float p = seg_incl_scan<SW>(v, sub) + basev;
+            const unsigned b = seg_ballot<SW>(in && 2.f * p >= total, s);
+            if (active && b) {
+                found = ln * C + t0 + __ffs(b) - 1;
+                active = false;
+            }
+            basev = __shfl_sync(TT_FULL_MASK, p, s * SW + SW - 1);
+        }
+        if (active && ++ln >= SW)
+            active = false;
+    }
+    return found;
+}
+
+// find_crossing_walk per segment (values of any sign).
+template <int SW>
+__device__ int seg_walk(const float *x, int C, float exc, float total, int sub) {
+    float run = exc;
+    int f = INT_MAX;
+    for (int k = 0; k < C; k++) {
+        run += x[sub * C + k];
+        if (f == INT_MAX && 2.f * run >= total)
+            f = sub * C + k;
+    }
+    return seg_min<SW>(f);
+}
+
+// Floats per line row of the warp-autonomous layout: room for SW chunks of
+// the longest chunk length, then SW more so that rows sit SW banks apart.
+__host__ __device__ constexpr int warp_line_stride(int n, int lpw) {
+    return 32 * ((32 / lpw * (((n + 32 / lpw - 1) / (32 / lpw)) | 1) + 31) / 32) +
+           (32 / lpw) % 32;
+}
+
+template <int LPW>
+__device__ void warp_lines(const BlockJob &J, unsigned long long tf_code, int n_t,
+                           unsigned need, int stride, float *xw) {
+    constexpr int SW = 32 / LPW;
+    const int lane = threadIdx.x & 31, s = lane / SW, sub = lane % SW;
+    const int n = J.n, angle = J.angle;
+    const float c = J.c, sn = J.s;
+    const float o = (float)(n - 1) * 0.5f, nm1 = (float)(n - 1);
+    const int col = J.col0 + s;
+    const bool colok = col < n;
+    const int rr = max(J.rr, 0), rc = max(J.rc, 0);
+
+    // 1. rows of the warp's lines whose stencil can touch the image
+    int lo = n, hi = 0;
+    if (colok && rr > 0 && rc > 0)
+        line_support((float)col - o, c, sn, o, n, (float)J.coff - 2.f,
+                     (float)(J.coff + rc) + 1.f, (float)J.roff - 2.f,
+                     (float)(J.roff + rr) + 1.f, &lo, &hi);
+    lo = warp_min(lo);
+    hi = warp_max(hi);
+    if (hi <= lo) {
+        lo = 0;
+        hi = 0;
+    }
+    const int jlo = lo, jhi = hi, len = jhi - jlo;
+    const int C = max((len + SW - 1) / SW, 1) | 1; // odd: conflict-free chunks
+    float *x = xw + s * stride;
+
+    // 2. sampling: lane (s, sub) takes rows sub + SW i of line s
+    {
+        const float X = (float)col - o;
+        const float Xc = __fmul_rn(X, c), Xms = __fmul_rn(X, -sn);
+        const float tu = J.tu, tv = J.tv;
+        constexpr int U = 4;
+        for (int i0 = 0; i0 < C; i0 += U) {
+            float4 g[U];
+            float xf[U], yf[U];
+            bool ok[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int jr = sub + SW * (i0 + u);
+                const float Y = (float)(jlo + jr) - o;
+                const float qx = __fadd_rn(__fadd_rn(Xc, __fmul_rn(Y, sn)), o);
+                const float qy = __fadd_rn(__fadd_rn(Xms, __fmul_rn(Y, c)), o);
+                ok[u] = colok && jr < len && qx >= 0.f && qx < nm1 && qy >= 0.f && qy < nm1;
+                const float xi = truncf(qx), yi = truncf(qy);
+                xf[u] = __fsub_rn(qx, xi);
+                yf[u] = __fsub_rn(qy, yi);
+                g[u] = tex2Dgather<float4>(J.tex, yi + tu, xi + tv, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const float omx = __fsub_rn(1.f, xf[u]), omy = __fsub_rn(1.f, yf[u]);
+                const float t0 = __fmul_rn(__fmul_rn(g[u].w, omx), omy);
+                const float t1 = __fmul_rn(__fmul_rn(g[u].x, xf[u]), omy);
+                const float t2 = __fmul_rn(__fmul_rn(g[u].z, omx), yf[u]);
+                const float t3 = __fmul_rn(__fmul_rn(g[u].y, xf[u]), yf[u]);
+                const float v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
+                if (i0 + u < C)
+                    x[sub + SW * (i0 + u)] = ok[u] ? v : 0.f;
+            }
+        }
+    }
+    __syncwarp();
+
+    // 3. T0-T5 of each segment's line
+    const bool need_m1 = need & ((1u << 1) | (1u << 2));
+    const bool need_m2 = need & ((1u << 3) | (1u << 4) | (1u << 5));
+    const int base = sub * C;
+    float tot = 0.f, totq = 0.f;
+    bool neg = false;
+    for (int k = 0; k < C; k++) {
+        const float v = x[base + k];
+        tot += v;
+        neg |= v < 0.f;
+        if (need_m2)
+            totq += sqrt_nn(v);
+    }
+    const float inc = seg_incl_scan<SW>(tot, sub);
+    const float S = __shfl_sync(TT_FULL_MASK, inc, s * SW + SW - 1);
+    float exc = __shfl_up_sync(TT_FULL_MASK, inc, 1, SW);
+    float Q = 0.f, incq = 0.f, excq = 0.f;
+    if (need_m2) {
+        incq = seg_incl_scan<SW>(totq, sub);
+        Q = __shfl_sync(TT_FULL_MASK, incq, s * SW + SW - 1);
+        excq = __shfl_up_sync(TT_FULL_MASK, incq, 1, SW);
+    }
+    if (sub == 0) {
+        exc = 0.f;
+        excq = 0.f;
+    }
+    const bool any_neg = __any_sync(TT_FULL_MASK, neg);
+    int m1 = 0, m2 = 0;
+    if (need_m1) {
+        const int f = any_neg ? seg_walk<SW>(x, C, exc, S, sub)
+                              : seg_find_crossing<false, SW>(x, C, inc, exc, S, s, sub);
+        m1 = resolve_median(f, S, jlo, jhi, len, n);
+    }
+    if (need_m2)
+        m2 = resolve_median(seg_find_crossing<true, SW>(x, C, incq, excq, Q, s, sub), Q, jlo,
+                            jhi, len, n);
+
+    float r1v = 0.f, r2v = 0.f;
+    if (need_m1) {
+        float t1 = 0.f, t2 = 0.f;
+        for (int j = max(m1, jlo) + sub; j < jhi; j += SW) {
+            const float v = x[j - jlo];
+            const float r = (float)(j - m1);
+            const float vr = v * r;
+            t1 += vr;
+            t2 = fmaf(vr, r, t2);
+        }
+        r1v = seg_sum<SW>(t1);
+        r2v = seg_sum<SW>(t2);
+    }
+    float r345[3] = {0.f, 0.f, 0.f};
+    if (need_m2) {
+        const bool w3 = need & (1u << 3), w4 = need & (1u << 4), w5 = need & (1u << 5);
+        const float2 *tab3 = J.tab, *tab4 = J.tab + n, *tab5 = J.tab + 2 * n;
+        float re3 = 0.f, im3 = 0.f, re4 = 0.f, im4 = 0.f, re5 = 0.f, im5 = 0.f;
+        const int qlo = max(1, jlo - m2), qhi = min(n - m2, jhi - m2);
+        for (int q = qlo + sub; q < qhi; q += SW) {
+            const float v = x[m2 + q - jlo];
+            if (w3) {
+                const float2 w = __ldg(tab3 + q);
+                re3 = fmaf(w.x, v, re3);
+                im3 = fmaf(w.y, v, im3);
+            }
+            if (w4) {
+                const float2 w = __ldg(tab4 + q);
+                re4 = fmaf(w.x, v, re4);
+                im4 = fmaf(w.y, v, im4);
+            }
+            if (w5) {
+                const float2 w = __ldg(tab5 + q);
+                re5 = fmaf(w.x, v, re5);
+                im5 = fmaf(w.y, v, im5);
+            }
+        }
+        if (w3)
+            r345[0] = hypotf(seg_sum<SW>(re3), seg_sum<SW>(im3));
+        if (w4)
+            r345[1] = hypotf(seg_sum<SW>(re4), seg_sum<SW>(im4));
+        if (w5)
+            r345[2] = hypotf(seg_sum<SW>(re5), seg_sum<SW>(im5));
+    }
+
+    // 4. one lane per line writes its outputs
+    if (sub == 0 && colok) {
+        const size_t plane = J.plane;
+        const size_t at = (size_t)angle * n + col;
+        for (int t = 0; t < n_t; t++) {
+            const int f = (int)((tf_code >> (3 * t)) & 7ull);
+            float v;
+            int med;
+            switch (f) {
+            case 0: v = S; med = -1; break;
+            case 1: v = r1v; med = m1; break;
+            case 2: v = r2v; med = m1; break;
+            case 3: v = r345[0]; med = m2; break;
+            case 4: v = r345[1]; med = m2; break;
+            default: v = r345[2]; med = m2; break;
+            }
+            J.out[t * plane + at] = v;
+            if (J.medians)
+                J.medians[t * plane + at] = med;
+        }
+    }
+}
+
+// One image: warp w of CTA (bx, angle) takes lines (bx W + w) LPW ..
+template <int LPW, int W>
+__global__ void __launch_bounds__(32 * W) sino_warp_kernel(const SinoArgs a) {
+    extern __shared__ __align__(16) float smw[];
+    const int warp = threadIdx.x >> 5;
+    BlockJob J;
+    J.n = a.n;
+    J.col0 = (blockIdx.x * W + warp) * LPW;
+    if (J.col0 >= a.n)
+        return; // whole warps: no CTA barrier below
+    J.tex = a.tex;
+    J.tu = 1.f - (float)a.tex_row_off;
+    J.tv = 1.f - (float)a.tex_col_off;
+    J.angle = blockIdx.y;
+    const float2 cs = a.trig[blockIdx.y];
+    J.c = cs.x;
+    J.s = cs.y;
+    if (a.dyn_region) {
+        J.roff = a.dyn_region[0];
+        J.coff = a.dyn_region[1];
+        J.rr = a.dyn_region[2];
+        J.rc = a.dyn_region[3];
+    } else {
+        J.roff = a.row_off;
+        J.coff = a.col_off;
+        J.rr = a.src_rows;
+        J.rc = a.src_cols;
+    }
+    J.tab = a.tab;
+    J.out = a.out;
+    J.medians = a.medians;
+    J.plane = (size_t)a.n_angles * a.n;
+    unsigned long long code = 0;
+    for (int t = 0; t < a.n_t; t++)
+        code |= (unsigned long long)(a.tf[t] & 7) << (3 * t);
+    warp_lines<LPW>(J, code, a.n_t, a.need, a.stride, smw + (size_t)warp * LPW * a.stride);
+}
+
+// Batch: every warp claims (image, angle, LPW-line block) items from the
+// counter until all are taken (items numbered largest image first).
+template <int LPW, int W>
+__global__ void __launch_bounds__(32 * W) sino_batch_warp_kernel(const BatchSinoArgs b) {
+    extern __shared__ __align__(16) float smw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float *xw = smw + (size_t)warp * LPW * b.stride;
+    for (;;) {
+        int item = 0;
+        if (lane == 0)
+            item = (int)atomicAdd(b.counter, 1u);
+        item = __shfl_sync(TT_FULL_MASK, item, 0);
+        if (item >= b.total_items)
+            break;
+        int lo = 0, hi = b.n_img - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&b.img[mid].items_begin) <= item)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const BatchImage &im = b.img[lo];
+        const int k = item - im.items_begin;
+        BlockJob J;
+        J.tex = im.tex;
+        J.tu = 1.f - (float)im.row_off;
+        J.tv = 1.f - (float)im.col_off;
+        J.n = im.n;
+        J.angle = k / im.blocks;
+        J.col0 = (k - J.angle * im.blocks) * LPW;
+        const float2 cs = b.trig[im.trig_off + J.angle];
+        J.c = cs.x;
+        J.s = cs.y;
+        J.roff = im.row_off;
+        J.coff = im.col_off;
+        J.rr = im.rows;
+        J.rc = im.cols;
+        J.tab = b.tab + im.tab_off;
+        J.out = b.sino + im.sino_off;
+        J.medians = nullptr;
+        J.plane = (size_t)im.n_angles * im.n;
+        warp_lines<LPW>(J, b.tf_code, b.n_t, b.need, b.stride, xw);
+        __syncwarp(); // the line rows are rewritten by the next item
+    }
+}
+
 // rotate() of c++/src/auxiliary.cpp:223-255 about ((cols-1)/2, (rows-1)/2),
 // writing the rotated image (used to check the sampling arithmetic; the
 // fused kernel never materialises it).  Same texture path as the fused kernel.
@@ -671,6 +1015,76 @@ cudaError_t launch_sino_batch(const BatchSinoArgs &a, int lines, int grid, size_
         else
             sino_batch_kernel<4, false><<<grid, 128, smem, stream>>>(a);
     }
+    return cudaGetLastError();
+}
+
+// ---- warp-autonomous variants (T0-T5) ------------------------------------------
+
+namespace {
+constexpr int kWarpCtaWarps = 4; // warps per CTA of the warp-autonomous kernels
+
+template <int LPW> cudaError_t launch_warp_one(const SinoArgs &a, size_t smem,
+                                               cudaStream_t stream) {
+    const size_t limit = opt_in_smem((const void *)sino_warp_kernel<LPW, kWarpCtaWarps>);
+    if (limit == 0 || smem > limit)
+        return cudaErrorInvalidValue;
+    constexpr int L = LPW * kWarpCtaWarps;
+    dim3 grid((a.n + L - 1) / L, a.n_angles);
+    sino_warp_kernel<LPW, kWarpCtaWarps><<<grid, 32 * kWarpCtaWarps, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+template <int LPW> int batch_warp_occ(size_t smem) {
+    const void *k = (const void *)sino_batch_warp_kernel<LPW, kWarpCtaWarps>;
+    const size_t limit = opt_in_smem(k);
+    if (limit == 0 || smem > limit)
+        return 0;
+    int blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &blocks, sino_batch_warp_kernel<LPW, kWarpCtaWarps>, 32 * kWarpCtaWarps, smem);
+    return blocks;
+}
+} // namespace
+
+int sino_warp_stride(int n, int lpw) { return warp_line_stride(n, lpw); }
+
+size_t sino_warp_smem_bytes(int n, int lpw) {
+    return sizeof(float) * (size_t)kWarpCtaWarps * lpw * warp_line_stride(n, lpw);
+}
+
+cudaError_t launch_sinograms_warp(const SinoArgs &a, int lpw, cudaStream_t stream) {
+    if (a.need & ((1u << 6) | (1u << 7)))
+        return cudaErrorInvalidValue; // T6 / T7 take the CTA kernels
+    const size_t smem = sino_warp_smem_bytes(a.n, lpw);
+    if (lpw == 1)
+        return launch_warp_one<1>(a, smem, stream);
+    if (lpw == 2)
+        return launch_warp_one<2>(a, smem, stream);
+    return launch_warp_one<4>(a, smem, stream);
+}
+
+int sino_batch_warp_occupancy(int lpw, size_t smem) {
+    return lpw == 1 ? batch_warp_occ<1>(smem) : lpw == 2 ? batch_warp_occ<2>(smem)
+                                                          : batch_warp_occ<4>(smem);
+}
+
+int sino_warp_cta_warps() { return kWarpCtaWarps; }
+
+cudaError_t launch_sino_batch_warp(const BatchSinoArgs &a, int lpw, int grid, size_t smem,
+                                   cudaStream_t stream) {
+    if (grid <= 0 || a.total_items <= 0)
+        return cudaSuccess;
+    if (a.need & ((1u << 6) | (1u << 7)))
+        return cudaErrorInvalidValue;
+    if (sino_batch_warp_occupancy(lpw, smem) <= 0)
+        return cudaErrorInvalidValue;
+    const int threads = 32 * kWarpCtaWarps;
+    if (lpw == 1)
+        sino_batch_warp_kernel<1, kWarpCtaWarps><<<grid, threads, smem, stream>>>(a);
+    else if (lpw == 2)
+        sino_batch_warp_kernel<2, kWarpCtaWarps><<<grid, threads, smem, stream>>>(a);
+    else
+        sino_batch_warp_kernel<4, kWarpCtaWarps><<<grid, threads, smem, stream>>>(a);
     return cudaGetLastError();
 }
 

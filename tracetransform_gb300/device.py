@@ -229,6 +229,14 @@ class Engine:
         check(lib().tt_transform_batch_stage_ms(self.plan.handle, ms))
         return [float(v) for v in ms]
 
+    def batch_tile(self, pin=None):
+        """The batched sinogram kernel's tile (lines per CTA, CTAs per SM,
+        lines per warp) of the last batch; pin=(lines, ctas_per_sm,
+        lines_per_warp) fixes it for the next batches (ctas_per_sm 0: tune)."""
+        t = (ctypes.c_int32 * 3)(*(pin or (0, 0, 0)))
+        check(lib().tt_transform_batch_tile(self.plan.handle, t, 1 if pin else 0))
+        return tuple(int(v) for v in t)
+
     def transform(self, image_cm: torch.Tensor, rows: int, cols: int, angles_deg, tfuncs,
                   pfuncs, out_sino=None):
         """Regular (non-orthonormal) transform on the device: returns
