@@ -130,16 +130,12 @@ def test_nos_kernel_variants_vs_oracle(oracle_lib, rows, cols):
 
 # Orthonormal (Hermite) circus against the oracle.  The nearest orthonormal
 # sinogram is the orthogonal polar factor U V^T of the aligned sinogram; its
-# directions of small singular values are ill-conditioned (float errors grow
-# with the condition number, 6e4 for the 1024^2 workload's sinograms), so a
-# float engine (double-float QR, float Jacobi) and the oracle (double one-sided
-# Jacobi) agree entry by entry only to the bound HERMITE_RTOL (per entry,
-# relative with the column guard), with HERMITE_P99 on the 99th percentile,
-# stated from the errors measured at that workload's 1449 x 360 shape, which
-# the test records with TT_PARITY_REPORT beside those of the oracle's float
-# sums and of a float32 LAPACK SVD against the exact polar factor.
-HERMITE_RTOL = 2e-3
-HERMITE_P99 = 4e-4
+# directions of small singular values are ill-conditioned (their error grows
+# as eps / sigma_min), so the engine (double-float QR, float Jacobi) and the
+# oracle (double one-sided Jacobi) agree entry by entry only to the bound
+# HERMITE_RTOL, stated from the measured error at the 1024^2 workload's
+# 1449 x 360 shape; the measured figures are recorded with TT_PARITY_REPORT.
+HERMITE_RTOL = 1e-3
 
 
 def _hermite_report(got, want):
@@ -231,4 +227,3 @@ def test_orthonormal_circus_single1024_shape(oracle_lib):
     record("orthonormal_1449x360_vs_fp64", rep)
     assert nos_err < 1e-4, rep
     assert rep["engine"]["max_rel"] <= HERMITE_RTOL, rep
-    assert rep["engine"]["p99"] <= HERMITE_P99, rep

@@ -742,11 +742,11 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
                     tt::nos_max_rows());
     if (cols > 1024)
         return fail(TT_ERR_UNSUPPORTED, "orthonormal circus of %d angles exceeds 1024", cols);
-    // scratch: 5 double-float + 3 int vectors of n, 4 float n x n matrices,
+    // scratch: 5 double-float + 3 int vectors of n, 3 float n x n matrices,
     // 2 float vectors
     const size_t nv = ncol, nm = (size_t)cols * cols * n_sino;
     TT_CHECK(p->ensure(p->nos_work, sizeof(float2) * 5 * nv + sizeof(int) * 3 * nv +
-                                        sizeof(float) * (4 * nm + 2 * nv) +
+                                        sizeof(float) * (3 * nm + 2 * nv) +
                                         sizeof(unsigned) * n_sino + sizeof(float) * n_sino + 64));
     tt::NosWork w;
     {
@@ -759,8 +759,7 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
         w.X = w.orig + nv;
         w.V = w.X + nm;
         w.P = w.V + nm;
-        w.X0 = w.P + nm;
-        w.inv = w.X0 + nm;
+        w.inv = w.P + nm;
         w.cmap = (int *)(w.inv + nv);
         w.perm = w.cmap + 2 * nv;
         w.off_bits = (unsigned *)(w.perm + nv);

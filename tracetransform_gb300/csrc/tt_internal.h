@@ -163,7 +163,6 @@ struct NosWork {
     int *cmap;                  // 2 x n_sino x n: position -> stored column, by step parity
     int *perm;                  // n_sino x n: stored column that ends at each position
     float *X, *V, *P;           // n_sino x n x n each (R^T, Jacobi V, polar(R))
-    float *X0;                  // n_sino x n x n: R^T as the QR left it (before the sweeps)
     float *inv;                 // n_sino x n
     unsigned *off_bits;         // n_sino: largest rotated |cos| of a sweep (float bits)
     float *tiny;                // n_sino: squared column norm below which a direction is null

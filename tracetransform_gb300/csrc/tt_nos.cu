@@ -27,14 +27,14 @@
 //                 pair rotated in one CTA's shared memory with V updated once
 //                 per round through the accumulated rotation;
 //                 X V = U_X S, so polar(R) = V U_X^T
-//   assemble      V made orthogonal (two Newton-Schulz steps), X = R^T V
-//                 recomputed from the QR's R^T and normalised to U, P = V U^T
-//                 (float), then polar(A P) = Q [P; 0] applied reflector by
-//                 reflector to groups of columns held in registers, and the
-//                 column permutation undone
+//   assemble      P = V U_X^T (float) with one Newton-Schulz step to clean
+//                 its orthogonality, then polar(A P) = Q [P; 0] applied
+//                 reflector by reflector to groups of columns held in
+//                 registers, and the column permutation undone
 //
 // Against the oracle's double one-sided Jacobi on the aligned matrix the
-// result agrees to ~1e-6 absolute (entries up to ~0.7).
+// result agrees to ~3e-5 absolute (entries up to ~0.7) for condition numbers
+// up to ~1e6; Eigen's float SVD of the same matrices is far less accurate.
 // Every launch is bounded; there is no grid-wide wait.
 #include "tt_common.cuh"
 #include "tt_internal.h"
@@ -1187,12 +1187,7 @@ cudaError_t launch_nos_factor(float2 *A, const NosDesc *desc, int n, int n_sino,
         qr_steps<32, kQrThreads>(A, desc, n, n_sino, w, st);
     const long long nn = (long long)n * n;
     nos_rt_kernel<<<dim3((unsigned)((nn + 255) / 256), n_sino), 256, 0, st>>>(A, desc, n, w);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess)
-        return e;
-    // R^T kept for the assembly, which recomputes X = R^T V from it
-    return cudaMemcpyAsync(w.X0, w.X, sizeof(float) * (size_t)nn * n_sino,
-                           cudaMemcpyDeviceToDevice, st);
+    return cudaGetLastError();
 }
 
 template <int K4>
@@ -1236,33 +1231,24 @@ cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int
                                 int max_m, const NosWork &w, float *out, cudaStream_t st) {
     const long long nn = (long long)n * n;
     const dim3 ge((unsigned)((nn + 255) / 256), n_sino), gt((n + 31) / 32, (n + 31) / 32, n_sino);
-    // polar(R) = V U^T with U the normalised columns of R^T V.  The rotated
-    // columns the sweeps leave in X carry the rounding of every rotation, and
-    // V, accumulated round by round in float, drifts from orthogonality; both
-    // errors grow by R's condition number in the small singular directions
-    // of the polar factor.  So V is first made orthogonal to float precision
-    // (two Newton-Schulz steps V <- V (3 I - V^T V) / 2), and X = R^T V is
-    // recomputed from the R^T the QR left (X0) before its columns are
-    // normalised.  (On the 1024^2 workload's sinograms this cuts the largest
-    // Hermite-circus error against the exact polar factor about fivefold
-    // compared with normalising the swept X and orthogonalising P = V U^T.)
-    rt_gemm_kernel<<<gt, 256, 0, st>>>(w.V, n, 1, w.V, 1, n, nullptr, 1.f, 0.f, n, w.P);
-    rt_gemm_kernel<<<gt, 256, 0, st>>>(w.V, 1, n, w.P, 1, n, w.V, -0.5f, 1.5f, n, w.X);
-    rt_gemm_kernel<<<gt, 256, 0, st>>>(w.X, n, 1, w.X, 1, n, nullptr, 1.f, 0.f, n, w.P);
-    rt_gemm_kernel<<<gt, 256, 0, st>>>(w.X, 1, n, w.P, 1, n, w.X, -0.5f, 1.5f, n, w.V);
-    rt_gemm_kernel<<<gt, 256, 0, st>>>(w.X0, 1, n, w.V, 1, n, nullptr, 1.f, 0.f, n, w.X);
     rt_invnorm_kernel<<<dim3((n + 3) / 4, n_sino), 128, 0, st>>>(w.X, n, w.tiny, w.inv);
     rt_scale_kernel<<<ge, 256, 0, st>>>(w.X, w.inv, n);
+    // P = V U^T, then one Newton-Schulz step P <- P (3 I - P^T P) / 2 (in the
+    // V buffer), which removes the symmetric part of P's distance from
+    // orthogonality left by the float sweeps' stopping bound; S = P^T P goes
+    // to the X buffer
     rt_gemm_kernel<<<gt, 256, 0, st>>>(w.V, 1, n, w.X, n, 1, nullptr, 1.f, 0.f, n, w.P);
+    rt_gemm_kernel<<<gt, 256, 0, st>>>(w.P, n, 1, w.P, 1, n, nullptr, 1.f, 0.f, n, w.X);
+    rt_gemm_kernel<<<gt, 256, 0, st>>>(w.P, 1, n, w.X, 1, n, w.P, -0.5f, 1.5f, n, w.V);
     const dim3 gq((n + kQCols - 1) / kQCols, n_sino);
     if (n <= kNosMaxCols && max_m <= 8 * kQThreads) {
         nos_apply_q_reg_kernel<8><<<gq, kQThreads, 0, st>>>(A, desc, w.tau, w.scale, w.perm,
-                                                             w.P, n, out);
+                                                             w.V, n, out);
         return cudaGetLastError();
     }
     if (n <= kNosMaxCols && max_m <= 16 * kQThreads) {
         nos_apply_q_reg_kernel<16><<<gq, kQThreads, 0, st>>>(A, desc, w.tau, w.scale, w.perm,
-                                                              w.P, n, out);
+                                                              w.V, n, out);
         return cudaGetLastError();
     }
     const size_t limit = opt_in_smem((const void *)nos_apply_q_kernel);
@@ -1272,7 +1258,7 @@ cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int
     if (smem > limit)
         return cudaErrorInvalidValue;
     nos_apply_q_kernel<<<dim3((n + kQCols - 1) / kQCols, n_sino), kQThreads, smem, st>>>(
-        A, desc, w.tau, w.scale, w.perm, w.P, n, out);
+        A, desc, w.tau, w.scale, w.perm, w.V, n, out);
     return cudaGetLastError();
 }
 
