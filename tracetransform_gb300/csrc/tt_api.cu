@@ -533,6 +533,8 @@ tt_status run_sinograms(tt_plan *p, const float *d_src, int src_rows, int src_co
     a.tex_col_off = col_off;
     a.src_rows = src_rows;
     a.src_cols = src_cols;
+    a.interior = src_rows > 0 && src_cols > 0 &&
+                 tt::interior_source(n, row_off, col_off, src_rows, src_cols);
     a.row_off = row_off;
     a.col_off = col_off;
     a.dyn_region = d_region;
@@ -548,6 +550,13 @@ tt_status run_sinograms(tt_plan *p, const float *d_src, int src_rows, int src_co
     for (int t = 0; t < n_t; t++)
         a.tf[t] = tfuncs[t];
     a.need = need;
+    if (!(need & ((1u << 6) | (1u << 7))) && n <= 1024) {
+        // T0-T5 of short lines: two lines per warp (the shape the batch tuner
+        // picks for lines of this length)
+        a.stride = tt::sino_warp_stride(n, 2);
+        TT_CUDA(tt::launch_sinograms_warp(a, 2, st));
+        return TT_OK;
+    }
     const int L = tt::sino_lines_per_block(n, need);
     a.stride = tt::sino_stride(n, L);
     if (tt::sino_smem_bytes(n, L, need) > 227 * 1024)

@@ -281,12 +281,13 @@ int BatchEngine::set_tile(const Tune &t, cudaStream_t st) {
     B_CHECK(img_.upload(desc, st));
     if (t.lpw) {
         sino_smem_ = sino_warp_smem_bytes(n_max_, t.lpw);
-        if (sino_batch_warp_occupancy(t.lpw, sino_smem_) <= 0)
+        if (sino_batch_warp_occupancy(t.lpw, sargs_.all_interior, sino_smem_) <= 0)
             return berr(TT_ERR_UNSUPPORTED, "warp tile does not fit the batch's largest image");
         sargs_.stride = sino_warp_stride(n_max_, t.lpw);
     } else {
         sino_smem_ = sino_smem_bytes(n_max_, t.lines, sargs_.need);
-        B_CUDA(prepare_sino_batch(t.lines, sargs_.need & ((1u << 6) | (1u << 7)), sino_smem_));
+        B_CUDA(prepare_sino_batch(t.lines, sargs_.need & ((1u << 6) | (1u << 7)),
+                                  sargs_.all_interior, sino_smem_));
         sargs_.stride = sino_stride(n_max_, t.lines);
     }
     sargs_.img = img_.p;
@@ -452,6 +453,11 @@ int BatchEngine::build(cudaStream_t st) {
     sargs_.tf_code = code;
     sargs_.n_t = n_t;
     sargs_.need = tneed;
+    sargs_.all_interior = true;
+    for (int i = 0; i < n_img; i++)
+        sargs_.all_interior = sargs_.all_interior &&
+                              interior_source(n_[i], ro_[i], co_[i], shape_.rows[i],
+                                              shape_.cols[i]);
     cargs_ = CircusStackArgs{};
     cargs_.st = stacks_.p;
     cargs_.n_st = n_img;
@@ -541,10 +547,11 @@ int BatchEngine::autotune(cudaStream_t st) {
     for (Tune t : shapes) {
         int occ;
         if (t.lpw) {
-            occ = sino_batch_warp_occupancy(t.lpw, sino_warp_smem_bytes(n_max_, t.lpw));
+            occ = sino_batch_warp_occupancy(t.lpw, sargs_.all_interior,
+                                            sino_warp_smem_bytes(n_max_, t.lpw));
         } else {
             const size_t smem = sino_smem_bytes(n_max_, t.lines, sargs_.need);
-            occ = sino_batch_occupancy(t.lines, sel, smem);
+            occ = sino_batch_occupancy(t.lines, sel, sargs_.all_interior, smem);
         }
         if (occ <= 0)
             continue;

@@ -32,7 +32,16 @@ struct SinoArgs {
     int tf[kMaxT];
     unsigned need;      // bit f set when T-functional f is requested
     int stride;         // floats per line in shared memory
+    bool interior;      // the texture region lies >= 2 texels inside the frame
 };
+
+// Does a texture region of rows x cols at (row_off, col_off) lie at least two
+// texels inside the n x n frame on every side?  Then a rotated sample outside
+// [0, n-1) only ever reads border texels (value 0), and the sampler can skip
+// the reference's bounds test without changing any result.
+inline bool interior_source(int n, int row_off, int col_off, int rows, int cols) {
+    return row_off >= 2 && col_off >= 2 && row_off + rows <= n - 1 && col_off + cols <= n - 1;
+}
 
 // P-functionals over stacked sinograms.
 struct CircusArgs {
@@ -213,6 +222,7 @@ struct BatchSinoArgs {
     int n_t;
     unsigned need;
     int stride;              // floats per line buffer (for the largest n)
+    bool all_interior;       // every image passes interior_source
 };
 
 int sino_lines_per_block(int n, unsigned need);
@@ -225,7 +235,7 @@ int sino_warp_stride(int n, int lpw);
 size_t sino_warp_smem_bytes(int n, int lpw);
 int sino_warp_cta_warps();
 cudaError_t launch_sinograms_warp(const SinoArgs &a, int lpw, cudaStream_t stream);
-int sino_batch_warp_occupancy(int lpw, size_t smem);
+int sino_batch_warp_occupancy(int lpw, bool interior, size_t smem);
 cudaError_t launch_sino_batch_warp(const BatchSinoArgs &a, int lpw, int grid, size_t smem,
                                    cudaStream_t stream);
 cudaError_t launch_rotate(cudaTextureObject_t tex, int rows, int cols, float c, float s,
@@ -242,8 +252,8 @@ cudaError_t launch_zscore(const float *in, int n_vec, int len, float *out,
 
 // Batched engine kernels.  The persistent sinogram kernel runs `grid` CTAs
 // that claim work items from *counter; lines = 4 or 8.
-cudaError_t prepare_sino_batch(int lines, bool sel, size_t smem);
-int sino_batch_occupancy(int lines, bool sel, size_t smem);
+cudaError_t prepare_sino_batch(int lines, bool sel, bool interior, size_t smem);
+int sino_batch_occupancy(int lines, bool sel, bool interior, size_t smem);
 cudaError_t launch_sino_batch(const BatchSinoArgs &a, int lines, int grid, size_t smem,
                               cudaStream_t stream);
 cudaError_t launch_zscore_batch(const float *in, const long long *off, const int *len,

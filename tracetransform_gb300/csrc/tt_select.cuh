@@ -308,7 +308,7 @@ inline __device__ void select_t67(float *x, int jlo, int jhi, int m1, int m2, bo
         s7->hist[i] = 0u;
     }
     __syncwarp();
-    unsigned l6 = 0, l7 = 0;
+    unsigned l6 = 0, l7 = 0, l7max = 0;
     for (int jb = j0; jb < j1; jb += 4) {
         float vb[4]; // four loads in flight before the atomics
 #pragma unroll
@@ -323,6 +323,7 @@ inline __device__ void select_t67(float *x, int jlo, int jhi, int m1, int m2, bo
             const unsigned wq = __float2uint_rn(sqrt_nn(v) * qs);
             if (want7 && j >= b7) {
                 l7 += wq;
+                l7max += v == xmax ? wq : 0u;
                 atomicAdd(s7->hist + sel_bin(v, 0.f, bs7), wq);
             }
             if (want6 && j >= b6) {
@@ -333,6 +334,15 @@ inline __device__ void select_t67(float *x, int jlo, int jhi, int m1, int m2, bo
     }
     const unsigned long long W7 = __reduce_add_sync(TT_FULL_MASK, l7);
     const unsigned long long W6 = __reduce_add_sync(TT_FULL_MASK, l6);
+    // Saturated lines (samples clipped at the image's maximum) put the
+    // crossing on the largest key: when the keys below the maximum weigh less
+    // than half the total, 2 W(< xmax) < W, the answer is xmax -- exact in
+    // the fixed-point weights, no compaction or refinement needed.
+    const unsigned long long W7max = __reduce_add_sync(TT_FULL_MASK, l7max);
+    if (want7 && W7max > 0 && 2ull * (W7 - W7max) < W7) {
+        *r7 = xmax;
+        want7 = false;
+    }
     __syncwarp();
 
     if (want6) {

@@ -144,7 +144,7 @@ struct BlockJob {
 // The fused body: support, sampling, T-functionals of one BlockJob.  Every
 // thread of the CTA calls it; it synchronises the CTA but never returns early.
 // tf_code holds the T-functional id of output t in bits [3t, 3t + 3).
-template <int L, bool kSel>
+template <int L, bool kSel, bool kInterior>
 __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long tf_code,
                                            int n_t, unsigned need, int stride, float *sm,
                                            int *s_range) {
@@ -206,7 +206,9 @@ __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long
                 // (x c + y s) + o and (x (-s) + y c) + o, each operation rounded
                 const float qx = __fadd_rn(__fadd_rn(Xc, __fmul_rn(Y, s)), o);
                 const float qy = __fadd_rn(__fadd_rn(Xms, __fmul_rn(Y, c)), o);
-                ok[u] = colok && jr < len && qx >= 0.f && qx < nm1 && qy >= 0.f && qy < nm1;
+                ok[u] = colok && jr < len;
+                if (!kInterior) // see warp_sample: border texels answer the test
+                    ok[u] = ok[u] && qx >= 0.f && qx < nm1 && qy >= 0.f && qy < nm1;
                 const float xi = truncf(qx), yi = truncf(qy);
                 xf[u] = __fsub_rn(qx, xi);
                 yf[u] = __fsub_rn(qy, yi);
@@ -354,7 +356,7 @@ __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long
     } // col < n
 }
 
-template <int L, bool kSel>
+template <int L, bool kSel, bool kInterior>
 __global__ void __launch_bounds__(32 * L)
     sino_kernel(const SinoArgs a) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -396,14 +398,14 @@ __global__ void __launch_bounds__(32 * L)
     unsigned long long code = 0;
     for (int t = 0; t < a.n_t; t++)
         code |= (unsigned long long)(a.tf[t] & 7) << (3 * t);
-    sino_block<L, kSel>(J, code, a.n_t, a.need, a.stride, reinterpret_cast<float *>(smraw),
-                        s_range);
+    sino_block<L, kSel, kInterior>(J, code, a.n_t, a.need, a.stride,
+                                   reinterpret_cast<float *>(smraw), s_range);
 }
 
 // Persistent kernel over a batch of images of different sizes and angle
 // counts: each CTA claims work items (image, angle, line block) from a
 // counter until all are taken; items are numbered largest image first.
-template <int L, bool kSel>
+template <int L, bool kSel, bool kInterior>
 __global__ void __launch_bounds__(32 * L)
     sino_batch_kernel(const BatchSinoArgs b) {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -445,8 +447,8 @@ __global__ void __launch_bounds__(32 * L)
         J.out = b.sino + im.sino_off;
         J.medians = nullptr;
         J.plane = (size_t)im.n_angles * im.n;
-        sino_block<L, kSel>(J, b.tf_code, b.n_t, b.need, b.stride,
-                            reinterpret_cast<float *>(smraw), s_range);
+        sino_block<L, kSel, kInterior>(J, b.tf_code, b.n_t, b.need, b.stride,
+                                       reinterpret_cast<float *>(smraw), s_range);
     }
 }
 
@@ -539,14 +541,63 @@ __host__ __device__ constexpr int warp_line_stride(int n, int lpw) {
            (32 / lpw) % 32;
 }
 
-template <int LPW>
+// Sampling of the warp-autonomous path: lane (s, sub) takes rows sub + SW i
+// of line s into x.  kBounds = false when the texture's region sits at least
+// two texels inside the frame on every side (interior_source): a sample the
+// reference's bounds test rejects then has a stencil of border texels only,
+// whose bilinear combination is +0, the value the test would give.
+template <int SW, bool kBounds>
+__device__ __forceinline__ void warp_sample(const BlockJob &J, float *x, int col, bool colok,
+                                            int jlo, int len, int C, int sub) {
+    const int n = J.n;
+    const float c = J.c, sn = J.s;
+    const float o = (float)(n - 1) * 0.5f, nm1 = (float)(n - 1);
+    const float X = (float)col - o;
+    const float Xc = __fmul_rn(X, c), Xms = __fmul_rn(X, -sn);
+    const float tu = J.tu, tv = J.tv;
+    constexpr int U = 4;
+    float Y0 = (float)(jlo + sub) - o; // exact: integers below 2^24
+    for (int i0 = 0; i0 < C; i0 += U) {
+        float4 g[U];
+        float xf[U], yf[U];
+        bool ok[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int jr = sub + SW * (i0 + u);
+            const float Y = Y0 + (float)(SW * u);
+            const float qx = __fadd_rn(__fadd_rn(Xc, __fmul_rn(Y, sn)), o);
+            const float qy = __fadd_rn(__fadd_rn(Xms, __fmul_rn(Y, c)), o);
+            ok[u] = colok && jr < len;
+            if (kBounds)
+                ok[u] = ok[u] && qx >= 0.f && qx < nm1 && qy >= 0.f && qy < nm1;
+            const float xi = truncf(qx), yi = truncf(qy);
+            xf[u] = __fsub_rn(qx, xi);
+            yf[u] = __fsub_rn(qy, yi);
+            g[u] = tex2Dgather<float4>(J.tex, yi + tu, xi + tv, 0);
+        }
+        Y0 += (float)(SW * U);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const float omx = __fsub_rn(1.f, xf[u]), omy = __fsub_rn(1.f, yf[u]);
+            const float t0 = __fmul_rn(__fmul_rn(g[u].w, omx), omy);
+            const float t1 = __fmul_rn(__fmul_rn(g[u].x, xf[u]), omy);
+            const float t2 = __fmul_rn(__fmul_rn(g[u].z, omx), yf[u]);
+            const float t3 = __fmul_rn(__fmul_rn(g[u].y, xf[u]), yf[u]);
+            const float v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
+            if (i0 + u < C)
+                x[sub + SW * (i0 + u)] = ok[u] ? v : 0.f;
+        }
+    }
+}
+
+template <int LPW, bool kInterior>
 __device__ void warp_lines(const BlockJob &J, unsigned long long tf_code, int n_t,
                            unsigned need, int stride, float *xw) {
     constexpr int SW = 32 / LPW;
     const int lane = threadIdx.x & 31, s = lane / SW, sub = lane % SW;
     const int n = J.n, angle = J.angle;
     const float c = J.c, sn = J.s;
-    const float o = (float)(n - 1) * 0.5f, nm1 = (float)(n - 1);
+    const float o = (float)(n - 1) * 0.5f;
     const int col = J.col0 + s;
     const bool colok = col < n;
     const int rr = max(J.rr, 0), rc = max(J.rc, 0);
@@ -567,41 +618,8 @@ __device__ void warp_lines(const BlockJob &J, unsigned long long tf_code, int n_
     const int C = max((len + SW - 1) / SW, 1) | 1; // odd: conflict-free chunks
     float *x = xw + s * stride;
 
-    // 2. sampling: lane (s, sub) takes rows sub + SW i of line s
-    {
-        const float X = (float)col - o;
-        const float Xc = __fmul_rn(X, c), Xms = __fmul_rn(X, -sn);
-        const float tu = J.tu, tv = J.tv;
-        constexpr int U = 4;
-        for (int i0 = 0; i0 < C; i0 += U) {
-            float4 g[U];
-            float xf[U], yf[U];
-            bool ok[U];
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-                const int jr = sub + SW * (i0 + u);
-                const float Y = (float)(jlo + jr) - o;
-                const float qx = __fadd_rn(__fadd_rn(Xc, __fmul_rn(Y, sn)), o);
-                const float qy = __fadd_rn(__fadd_rn(Xms, __fmul_rn(Y, c)), o);
-                ok[u] = colok && jr < len && qx >= 0.f && qx < nm1 && qy >= 0.f && qy < nm1;
-                const float xi = truncf(qx), yi = truncf(qy);
-                xf[u] = __fsub_rn(qx, xi);
-                yf[u] = __fsub_rn(qy, yi);
-                g[u] = tex2Dgather<float4>(J.tex, yi + tu, xi + tv, 0);
-            }
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-                const float omx = __fsub_rn(1.f, xf[u]), omy = __fsub_rn(1.f, yf[u]);
-                const float t0 = __fmul_rn(__fmul_rn(g[u].w, omx), omy);
-                const float t1 = __fmul_rn(__fmul_rn(g[u].x, xf[u]), omy);
-                const float t2 = __fmul_rn(__fmul_rn(g[u].z, omx), yf[u]);
-                const float t3 = __fmul_rn(__fmul_rn(g[u].y, xf[u]), yf[u]);
-                const float v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
-                if (i0 + u < C)
-                    x[sub + SW * (i0 + u)] = ok[u] ? v : 0.f;
-            }
-        }
-    }
+    // 2. sampling
+    warp_sample<SW, !kInterior>(J, x, col, colok, jlo, len, C, sub);
     __syncwarp();
 
     // 3. T0-T5 of each segment's line
@@ -710,8 +728,8 @@ __device__ void warp_lines(const BlockJob &J, unsigned long long tf_code, int n_
 }
 
 // One image: warp w of CTA (bx, angle) takes lines (bx W + w) LPW ..
-template <int LPW, int W>
-__global__ void __launch_bounds__(32 * W) sino_warp_kernel(const SinoArgs a) {
+template <int LPW, int W, bool kInterior>
+__global__ void __launch_bounds__(32 * W, 32 / W) sino_warp_kernel(const SinoArgs a) {
     extern __shared__ __align__(16) float smw[];
     const int warp = threadIdx.x >> 5;
     BlockJob J;
@@ -744,13 +762,14 @@ __global__ void __launch_bounds__(32 * W) sino_warp_kernel(const SinoArgs a) {
     unsigned long long code = 0;
     for (int t = 0; t < a.n_t; t++)
         code |= (unsigned long long)(a.tf[t] & 7) << (3 * t);
-    warp_lines<LPW>(J, code, a.n_t, a.need, a.stride, smw + (size_t)warp * LPW * a.stride);
+    warp_lines<LPW, kInterior>(J, code, a.n_t, a.need, a.stride,
+                               smw + (size_t)warp * LPW * a.stride);
 }
 
 // Batch: every warp claims (image, angle, LPW-line block) items from the
 // counter until all are taken (items numbered largest image first).
-template <int LPW, int W>
-__global__ void __launch_bounds__(32 * W) sino_batch_warp_kernel(const BatchSinoArgs b) {
+template <int LPW, int W, bool kInterior>
+__global__ void __launch_bounds__(32 * W, 32 / W) sino_batch_warp_kernel(const BatchSinoArgs b) {
     extern __shared__ __align__(16) float smw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float *xw = smw + (size_t)warp * LPW * b.stride;
@@ -789,7 +808,7 @@ __global__ void __launch_bounds__(32 * W) sino_batch_warp_kernel(const BatchSino
         J.out = b.sino + im.sino_off;
         J.medians = nullptr;
         J.plane = (size_t)im.n_angles * im.n;
-        warp_lines<LPW>(J, b.tf_code, b.n_t, b.need, b.stride, xw);
+        warp_lines<LPW, kInterior>(J, b.tf_code, b.n_t, b.need, b.stride, xw);
         __syncwarp(); // the line rows are rewritten by the next item
     }
 }
@@ -903,14 +922,16 @@ __global__ void bbox_finish(int *r) {
 
 template <int L, bool kSel>
 cudaError_t launch_one(const SinoArgs &a, size_t smem, cudaStream_t stream) {
-    const size_t limit = opt_in_smem((const void *)sino_kernel<L, kSel>);
+    const void *k = a.interior ? (const void *)sino_kernel<L, kSel, true>
+                               : (const void *)sino_kernel<L, kSel, false>;
+    const size_t limit = opt_in_smem(k);
     if (limit == 0)
         return cudaErrorInvalidValue;
     if (smem > limit)
         return cudaErrorInvalidValue;
     dim3 grid((a.n + L - 1) / L, a.n_angles);
-    sino_kernel<L, kSel><<<grid, 32 * L, smem, stream>>>(a);
-    return cudaGetLastError();
+    void *args[] = {(void *)&a};
+    return cudaLaunchKernel(k, grid, dim3(32 * L), args, smem, stream);
 }
 
 } // namespace
@@ -970,33 +991,33 @@ cudaError_t launch_sinograms(const SinoArgs &a, int lines, cudaStream_t stream) 
 }
 
 namespace {
-template <int L, bool kSel> cudaError_t set_batch_attr(size_t smem) {
-    const size_t limit = opt_in_smem((const void *)sino_batch_kernel<L, kSel>);
+const void *batch_cta_kernel(int lines, bool sel, bool in) {
+    if (lines == 8)
+        return sel ? (in ? (const void *)sino_batch_kernel<8, true, true>
+                         : (const void *)sino_batch_kernel<8, true, false>)
+                   : (in ? (const void *)sino_batch_kernel<8, false, true>
+                         : (const void *)sino_batch_kernel<8, false, false>);
+    return sel ? (in ? (const void *)sino_batch_kernel<4, true, true>
+                     : (const void *)sino_batch_kernel<4, true, false>)
+               : (in ? (const void *)sino_batch_kernel<4, false, true>
+                     : (const void *)sino_batch_kernel<4, false, false>);
+}
+} // namespace
+
+cudaError_t prepare_sino_batch(int lines, bool sel, bool interior, size_t smem) {
+    const size_t limit = opt_in_smem(batch_cta_kernel(lines, sel, interior));
     if (limit == 0)
         return cudaErrorInvalidValue;
     return smem > limit ? cudaErrorInvalidValue : cudaSuccess;
 }
 
-template <int L, bool kSel> int batch_occ(size_t smem) {
-    int blocks = 0;
-    if (set_batch_attr<L, kSel>(smem) != cudaSuccess)
+int sino_batch_occupancy(int lines, bool sel, bool interior, size_t smem) {
+    if (prepare_sino_batch(lines, sel, interior, smem) != cudaSuccess)
         return 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sino_batch_kernel<L, kSel>, 32 * L,
-                                                  smem);
+    int blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, batch_cta_kernel(lines, sel, interior),
+                                                  32 * lines, smem);
     return blocks;
-}
-} // namespace
-
-cudaError_t prepare_sino_batch(int lines, bool sel, size_t smem) {
-    if (lines == 8)
-        return sel ? set_batch_attr<8, true>(smem) : set_batch_attr<8, false>(smem);
-    return sel ? set_batch_attr<4, true>(smem) : set_batch_attr<4, false>(smem);
-}
-
-int sino_batch_occupancy(int lines, bool sel, size_t smem) {
-    if (lines == 8)
-        return sel ? batch_occ<8, true>(smem) : batch_occ<8, false>(smem);
-    return sel ? batch_occ<4, true>(smem) : batch_occ<4, false>(smem);
 }
 
 cudaError_t launch_sino_batch(const BatchSinoArgs &a, int lines, int grid, size_t smem,
@@ -1004,18 +1025,9 @@ cudaError_t launch_sino_batch(const BatchSinoArgs &a, int lines, int grid, size_
     if (grid <= 0 || a.total_items <= 0)
         return cudaSuccess;
     const bool sel = a.need & ((1u << 6) | (1u << 7));
-    if (lines == 8) {
-        if (sel)
-            sino_batch_kernel<8, true><<<grid, 256, smem, stream>>>(a);
-        else
-            sino_batch_kernel<8, false><<<grid, 256, smem, stream>>>(a);
-    } else {
-        if (sel)
-            sino_batch_kernel<4, true><<<grid, 128, smem, stream>>>(a);
-        else
-            sino_batch_kernel<4, false><<<grid, 128, smem, stream>>>(a);
-    }
-    return cudaGetLastError();
+    void *args[] = {(void *)&a};
+    return cudaLaunchKernel(batch_cta_kernel(lines, sel, a.all_interior), dim3(grid),
+                            dim3(32 * lines), args, smem, stream);
 }
 
 // ---- warp-autonomous variants (T0-T5) ------------------------------------------
@@ -1023,26 +1035,27 @@ cudaError_t launch_sino_batch(const BatchSinoArgs &a, int lines, int grid, size_
 namespace {
 constexpr int kWarpCtaWarps = 4; // warps per CTA of the warp-autonomous kernels
 
-template <int LPW> cudaError_t launch_warp_one(const SinoArgs &a, size_t smem,
-                                               cudaStream_t stream) {
-    const size_t limit = opt_in_smem((const void *)sino_warp_kernel<LPW, kWarpCtaWarps>);
+template <int LPW, bool kI> cudaError_t launch_warp_one(const SinoArgs &a, size_t smem,
+                                                        cudaStream_t stream) {
+    const size_t limit = opt_in_smem((const void *)sino_warp_kernel<LPW, kWarpCtaWarps, kI>);
     if (limit == 0 || smem > limit)
         return cudaErrorInvalidValue;
     constexpr int L = LPW * kWarpCtaWarps;
     dim3 grid((a.n + L - 1) / L, a.n_angles);
-    sino_warp_kernel<LPW, kWarpCtaWarps><<<grid, 32 * kWarpCtaWarps, smem, stream>>>(a);
+    sino_warp_kernel<LPW, kWarpCtaWarps, kI><<<grid, 32 * kWarpCtaWarps, smem, stream>>>(a);
     return cudaGetLastError();
 }
 
-template <int LPW> int batch_warp_occ(size_t smem) {
-    const void *k = (const void *)sino_batch_warp_kernel<LPW, kWarpCtaWarps>;
-    const size_t limit = opt_in_smem(k);
-    if (limit == 0 || smem > limit)
-        return 0;
-    int blocks = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &blocks, sino_batch_warp_kernel<LPW, kWarpCtaWarps>, 32 * kWarpCtaWarps, smem);
-    return blocks;
+template <int LPW, bool kI> const void *batch_warp_fn() {
+    return (const void *)sino_batch_warp_kernel<LPW, kWarpCtaWarps, kI>;
+}
+
+const void *batch_warp_kernel(int lpw, bool interior) {
+    if (lpw == 1)
+        return interior ? batch_warp_fn<1, true>() : batch_warp_fn<1, false>();
+    if (lpw == 2)
+        return interior ? batch_warp_fn<2, true>() : batch_warp_fn<2, false>();
+    return interior ? batch_warp_fn<4, true>() : batch_warp_fn<4, false>();
 }
 } // namespace
 
@@ -1056,16 +1069,25 @@ cudaError_t launch_sinograms_warp(const SinoArgs &a, int lpw, cudaStream_t strea
     if (a.need & ((1u << 6) | (1u << 7)))
         return cudaErrorInvalidValue; // T6 / T7 take the CTA kernels
     const size_t smem = sino_warp_smem_bytes(a.n, lpw);
+    const bool in = a.interior;
     if (lpw == 1)
-        return launch_warp_one<1>(a, smem, stream);
+        return in ? launch_warp_one<1, true>(a, smem, stream)
+                  : launch_warp_one<1, false>(a, smem, stream);
     if (lpw == 2)
-        return launch_warp_one<2>(a, smem, stream);
-    return launch_warp_one<4>(a, smem, stream);
+        return in ? launch_warp_one<2, true>(a, smem, stream)
+                  : launch_warp_one<2, false>(a, smem, stream);
+    return in ? launch_warp_one<4, true>(a, smem, stream)
+              : launch_warp_one<4, false>(a, smem, stream);
 }
 
-int sino_batch_warp_occupancy(int lpw, size_t smem) {
-    return lpw == 1 ? batch_warp_occ<1>(smem) : lpw == 2 ? batch_warp_occ<2>(smem)
-                                                          : batch_warp_occ<4>(smem);
+int sino_batch_warp_occupancy(int lpw, bool interior, size_t smem) {
+    const void *k = batch_warp_kernel(lpw, interior);
+    const size_t limit = opt_in_smem(k);
+    if (limit == 0 || smem > limit)
+        return 0;
+    int blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k, 32 * kWarpCtaWarps, smem);
+    return blocks;
 }
 
 int sino_warp_cta_warps() { return kWarpCtaWarps; }
@@ -1076,16 +1098,11 @@ cudaError_t launch_sino_batch_warp(const BatchSinoArgs &a, int lpw, int grid, si
         return cudaSuccess;
     if (a.need & ((1u << 6) | (1u << 7)))
         return cudaErrorInvalidValue;
-    if (sino_batch_warp_occupancy(lpw, smem) <= 0)
+    if (sino_batch_warp_occupancy(lpw, a.all_interior, smem) <= 0)
         return cudaErrorInvalidValue;
-    const int threads = 32 * kWarpCtaWarps;
-    if (lpw == 1)
-        sino_batch_warp_kernel<1, kWarpCtaWarps><<<grid, threads, smem, stream>>>(a);
-    else if (lpw == 2)
-        sino_batch_warp_kernel<2, kWarpCtaWarps><<<grid, threads, smem, stream>>>(a);
-    else
-        sino_batch_warp_kernel<4, kWarpCtaWarps><<<grid, threads, smem, stream>>>(a);
-    return cudaGetLastError();
+    void *args[] = {(void *)&a};
+    return cudaLaunchKernel(batch_warp_kernel(lpw, a.all_interior), dim3(grid),
+                            dim3(32 * kWarpCtaWarps), args, smem, stream);
 }
 
 cudaError_t launch_rotate(cudaTextureObject_t tex, int rows, int cols, float c, float s,
