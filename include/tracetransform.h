@@ -39,7 +39,9 @@ typedef enum {
                                boost::program_options::validation_error) */
     TT_ERR_UNSUPPORTED = 2, /* valid request this build does not handle */
     TT_ERR_CUDA = 3,        /* CUDA runtime error (reference: CUDAHelper::Error) */
-    TT_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+    TT_ERR_TIMEOUT = 4,     /* reserved: no entry point waits on the device (the
+                               engine's kernels contain no spin-waits), so none
+                               returns it */
     TT_ERR_OOM = 5          /* device or host allocation failed */
 } tt_status;
 
@@ -322,6 +324,13 @@ tt_status tt_transform_batch_stage_ms(tt_plan *plan, float *ms);
  * autotuner's choice).  pin != 0: fixes *tile for the following batches
  * instead of tuning (CTAs per SM 0 returns to the tuner). */
 tt_status tt_transform_batch_tile(tt_plan *plan, int32_t *tile, int32_t pin);
+
+/* Testing aid (no counterpart in the reference): the next `count` device
+ * allocations the library makes fail as if the device were out of memory,
+ * without touching the device, so callers can test their handling of
+ * TT_ERR_OOM (the reference's CUDAHelper::Error on cudaMalloc,
+ * cuda/src/cudahelper/errorhandling.hpp:24-31).  count = 0 disarms it. */
+tt_status tt_debug_fail_allocations(int count);
 
 /* ---- allocation-free entry point ---------------------------------------- */
 /* No counterpart in the reference.  P1 / P2 / P3 circus functions of n_sino

@@ -27,6 +27,7 @@ EXPORTS = (
     "tt_circus_f64_device", "tt_circus_backward_f64_device", "tt_sinograms_backward_f64_device",
     "tt_circus_orthonormal_device", "tt_nos", "tt_transform_batch_sinograms_device",
     "tt_transform_batch_stage_ms", "tt_transform_extended", "tt_transform_batch_tile",
+    "tt_debug_fail_allocations",
 )
 
 
@@ -106,6 +107,7 @@ def lib():
         "tt_transform_batch_sinograms_device": [_P, _P, ctypes.c_int64, _I64, _P],
         "tt_transform_batch_stage_ms": [_P, _F],
         "tt_transform_batch_tile": [_P, _I32, ctypes.c_int32],
+        "tt_debug_fail_allocations": [_int],
         "tt_transform_extended": [_P, _F, _int, _int, _F, _int, _I32, _int,
                                   ctypes.POINTER(PFunctionalC), _int, _I32, _int, _F, _F, _F,
                                   _F, _I32],

@@ -8,6 +8,7 @@
 //   P3 linspace   -1 + p * 2.0 / (N - 1) in double, rounded once (c++/src/functionals.cpp:346-355)
 //   Hermite       hermite_function with its double intermediates (c++/src/functionals.cpp:62-84, 369-386)
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -268,7 +269,7 @@ struct tt_plan {
     }
 
     tt_status alloc(void **p, size_t bytes) {
-        TT_CUDA(cudaMalloc(p, bytes > 0 ? bytes : 1));
+        TT_CUDA(tt::dev_malloc(p, bytes > 0 ? bytes : 1));
         owned.push_back(*p);
         return TT_OK;
     }
@@ -307,7 +308,7 @@ struct tt_plan {
             b.p = nullptr;
             b.bytes = 0;
         }
-        TT_CUDA(cudaMalloc(&b.p, bytes > 0 ? bytes : 1));
+        TT_CUDA(tt::dev_malloc(&b.p, bytes > 0 ? bytes : 1));
         b.bytes = bytes;
         return TT_OK;
     }
@@ -333,7 +334,7 @@ struct tt_plan {
             TT_CUDA(cudaDeviceSynchronize());
             src.release();
             cudaChannelFormatDesc desc = cudaCreateChannelDesc<float>();
-            TT_CUDA(cudaMallocArray(&src.arr, &desc, rows, cols, cudaArrayTextureGather));
+            TT_CUDA(tt::dev_malloc_array(&src.arr, &desc, rows, cols, cudaArrayTextureGather));
             cudaResourceDesc res{};
             res.resType = cudaResourceTypeArray;
             res.res.array.array = src.arr;
@@ -826,6 +827,33 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
 
 } // namespace
 
+namespace {
+std::atomic<int> g_fail_allocs{0};
+}
+
+cudaError_t tt::dev_malloc(void **p, size_t bytes) {
+    int left = g_fail_allocs.load();
+    while (left > 0 && !g_fail_allocs.compare_exchange_weak(left, left - 1)) {
+    }
+    if (left > 0) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
+cudaError_t tt::dev_malloc_array(cudaArray_t *a, const cudaChannelFormatDesc *desc, size_t w,
+                                 size_t h, unsigned flags) {
+    int left = g_fail_allocs.load();
+    while (left > 0 && !g_fail_allocs.compare_exchange_weak(left, left - 1)) {
+    }
+    if (left > 0) {
+        *a = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMallocArray(a, desc, w, h, flags);
+}
+
 int tt::record_error(int status, const char *message) {
     g_error = message;
     return status;
@@ -1240,6 +1268,13 @@ tt_status tt_circus_f64_device(tt_plan *plan, const double *d_sino, int rows, in
     TT_CHECK(p->get_kinds(pfuncs, n_p, &kinds));
     TT_CUDA(tt::launch_circus_f64(d_sino, rows, cols, n_sino, kinds, n_p, cosv, sinv, lin, d_out,
                                   pick_stream(p, stream)));
+    return TT_OK;
+}
+
+tt_status tt_debug_fail_allocations(int count) {
+    if (count < 0)
+        return fail(TT_ERR_INVALID_ARG, "negative count");
+    g_fail_allocs.store(count);
     return TT_OK;
 }
 

@@ -63,7 +63,7 @@ template <typename T> struct DevArray {
         cudaFree(p);
         p = nullptr;
         n = 0;
-        B_CUDA(cudaMalloc(&p, sizeof(T) * std::max<size_t>(count, 1)));
+        B_CUDA(dev_malloc(reinterpret_cast<void **>(&p), sizeof(T) * std::max<size_t>(count, 1)));
         n = count;
         return TT_OK;
     }
@@ -330,7 +330,7 @@ int BatchEngine::build(cudaStream_t st) {
         if (shape_.rows[i] > 32768 || shape_.cols[i] > 32768)
             return berr(TT_ERR_UNSUPPORTED, "batch image exceeds the 32768 texture-gather limit");
         cudaChannelFormatDesc desc = cudaCreateChannelDesc<float>();
-        B_CUDA(cudaMallocArray(&tex_[i].arr, &desc, shape_.rows[i], shape_.cols[i],
+        B_CUDA(dev_malloc_array(&tex_[i].arr, &desc, shape_.rows[i], shape_.cols[i],
                                cudaArrayTextureGather));
         cudaResourceDesc res{};
         res.resType = cudaResourceTypeArray;

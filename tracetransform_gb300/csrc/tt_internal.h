@@ -195,6 +195,14 @@ cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int
 // Record a failure for tt_last_error() on this thread; returns status.
 int record_error(int status, const char *message);
 
+// Every device allocation of the library goes through these: cudaMalloc /
+// cudaMallocArray, unless tt_debug_fail_allocations armed a simulated
+// failure, which they report as cudaErrorMemoryAllocation without touching
+// the device.
+cudaError_t dev_malloc(void **p, size_t bytes);
+cudaError_t dev_malloc_array(cudaArray_t *a, const cudaChannelFormatDesc *desc, size_t w,
+                             size_t h, unsigned flags);
+
 // Opt-in shared memory per block minus the kernel's static shared memory.
 size_t dynamic_smem_limit(const void *kernel);
 // Raises the kernel's dynamic shared memory cap to dynamic_smem_limit on the

@@ -147,9 +147,12 @@ __device__ __forceinline__ void sel_append(SelScratch *sc, int *count, bool in, 
     *count += __popc(m);
 }
 
-// Histogram bin of key k in [klo, klo + 256 / bs]: monotone in k.
+// Histogram bin of key k in [klo, klo + 256 / bs]: monotone in k, and always a
+// valid bin: keys below klo (negative samples of an image with negative
+// pixels) go to bin 0 and NaN keys convert to 0, so no input can index
+// outside the histogram.
 __device__ __forceinline__ int sel_bin(float k, float klo, float bs) {
-    return min(kSelBins - 1, (int)((k - klo) * bs));
+    return min(kSelBins - 1, max(0, (int)((k - klo) * bs)));
 }
 
 // Weighted selection over a list of keys stored in shared memory whose
