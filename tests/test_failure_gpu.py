@@ -82,16 +82,23 @@ def test_nan_inf_images_radon_pattern_matches_reference(oracle_lib):
                               [1, 2])
 
 
-def test_negative_images_run_every_functional():
+def test_negative_images_run_every_functional(oracle_lib):
     """Negative pixels reach the selections of T6 / T7 (negative keys) and P2's
-    exact-sort fallback; every entry point returns and the Radon sinogram is
-    the plain sum it always is."""
+    exact-sort fallback; every entry point returns, and the Radon sinogram --
+    a plain sum -- is the reference's.  (Where the reference takes square roots
+    of negative samples, T3-T7, its results are NaN-propagated; the engine's
+    are not specified there.)"""
+    from parity import close_mask
     img = (blob_image(33, 29, 4, (3, 9), (40, 200), 4) - 0.5).astype(np.float32, order="F")
     tfs = [str(t) for t in range(8)]
     tr = tt.Transformer(img, "neg", 4, False)
     sig = tr.getTransform(tfs, ["1", "2", "3"], write_data=False)
-    assert np.isfinite(tr.circus).all() and sig.shape == (90, 24)
+    assert sig.shape == (90, 24)
     tt.transform_batch([img, np.abs(img)], [4, 3], tfs, ["1", "2", "3"])
+    padded = oracle_lib.pad(img)
+    ref = oracle_lib.sinograms(padded, oracle_lib.angles_for_step(4), [0])[0]
+    got = tt.getSinograms(padded, 4, ["0"])[0]
+    assert close_mask(got.T, ref.T).all()
 
 
 def test_nan_sinograms_through_the_p_stage_and_zscore(oracle_lib):
