@@ -42,8 +42,6 @@ template <typename T> struct Coord;
 template <> struct Coord<float> {
     static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
     static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-    static constexpr float kEps = 1.1920929e-7f; // 2^-23
-    static __device__ __forceinline__ float rcp(float a) { return __frcp_rn(a); }
     static __device__ __forceinline__ void q(float X, float Y, float c, float s, float o,
                                              float &qx, float &qy) {
         qx = add(add(mul(X, c), mul(Y, s)), o);
@@ -53,8 +51,6 @@ template <> struct Coord<float> {
 template <> struct Coord<double> {
     static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
     static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-    static constexpr double kEps = 2.220446049250313e-16; // 2^-52
-    static __device__ __forceinline__ double rcp(double a) { return 1.0 / a; }
     static __device__ __forceinline__ void q(double X, double Y, double c, double s, double o,
                                              double &qx, double &qy) {
         qx = add(add(mul(X, c), mul(Y, s)), o);
@@ -229,35 +225,6 @@ template <> struct Quad<double> {
 
 constexpr int kAdjWarps = 8; // angle groups per pixel group
 
-// Rows j of rotated-grid column cc whose point q can lie within a unit of the
-// pixel (px, py) on both axes: |X c + Y s + o - px| < 1 and |-X s + Y c + o -
-// py| < 1 with Y = j - o, as two intervals of Y intersected, each widened by a
-// margin that covers the rounding of the forward's coordinates (a few ulps of
-// n) and of this estimate; [*jl, *jh] is empty when jl > jh.  Only the rows
-// in it are then tested exactly, with the forward's own arithmetic.
-template <typename T>
-__device__ __forceinline__ void row_window(T X, T ca, T sa, T ica, T isa, T fpx, T fpy, T o,
-                                           T mg, int n, int *jl, int *jh) {
-    T lo = -o - (T)1, hi = (T)n - o; // Y of rows 0 .. n - 1, with slack
-    const T t1 = fpx - o - X * ca, t2 = fpy - o + X * sa;
-    if (fabs(sa) > (T)1e-6) {
-        const T a0 = (t1 - (T)1) * isa, a1 = (t1 + (T)1) * isa, m = mg * fabs(isa);
-        lo = fmax(lo, fmin(a0, a1) - m);
-        hi = fmin(hi, fmax(a0, a1) + m);
-    } else if (fabs(t1) >= (T)1 + mg + (T)n * fabs(sa)) { // |Y s| <= n |s|
-        hi = lo - (T)2;
-    }
-    if (fabs(ca) > (T)1e-6) {
-        const T a0 = (t2 - (T)1) * ica, a1 = (t2 + (T)1) * ica, m = mg * fabs(ica);
-        lo = fmax(lo, fmin(a0, a1) - m);
-        hi = fmin(hi, fmax(a0, a1) + m);
-    } else if (fabs(t2) >= (T)1 + mg + (T)n * fabs(ca)) {
-        hi = lo - (T)2;
-    }
-    *jl = max(0, (int)ceil(lo + o));
-    *jh = min(n - 1, (int)floor(hi + o));
-}
-
 // Rotation adjoint by gathering.  Pixel (r, c) of a rows x cols image sits at
 // frame point (px, py) = (c + col_off, r + row_off).  A rotated-grid point
 // (column cc, sample j) with frame coordinates q = (qx, qy) feeds it the
@@ -265,14 +232,18 @@ __device__ __forceinline__ void row_window(T X, T ca, T sa, T ica, T isa, T fpx,
 // (1 - xf) or xf factor exactly, since qx - px and 1 - |qx - px| are exact in
 // floating point for |qx - px| < 1 -- provided the forward sampled q at all
 // (0 <= qx, qy < n - 1).  Such points lie within sqrt(2) of the pixel's
-// inverse-rotated position, so in the 3 columns around its nearest lattice
-// column; in each column only the rows of row_window (one to three, about
-// 1.6 on average) are recomputed with the forward's arithmetic and tested.
+// inverse-rotated position, i.e. in the 3 x 3 lattice block around its
+// nearest lattice point; each is recomputed with the forward's arithmetic.
+//
+// kInterior: the image lies at least two pixels inside its frame, so a
+// candidate with non-zero weight (within a unit of the pixel on both axes)
+// lies inside [1, n - 2] and always passed the forward's bounds test; only
+// the grid indices still need their range checks.
 //
 // CTA: 32 consecutive pixels (lanes) x kAdjWarps warps; warp w sums the angles
 // a = w (mod kAdjWarps) in increasing order and the warps' partial sums are
 // added in warp order, so the result is deterministic.  blockIdx.y = image.
-template <typename T>
+template <typename T, bool kInterior>
 __global__ void __launch_bounds__(32 * kAdjWarps)
 adjoint_gather_kernel(int rows, int cols, int row_off, int col_off, int n, int n_angles,
                       const T *__restrict__ cs, const T *__restrict__ params,
@@ -289,36 +260,45 @@ adjoint_gather_kernel(int rows, int cols, int row_off, int col_off, int n, int n
         const T fpx = (T)(c + col_off), fpy = (T)(r + row_off);
         const T o = (T)(n - 1) * (T)0.5, nm1 = (T)(n - 1);
         const T dx = fpx - o, dy = fpy - o;
-        const T mg = (T)16 * (T)n * C::kEps + (T)1e-6;
         for (int a = warp; a < n_angles; a += kAdjWarps) {
             const T ca = __ldg(cs + 2 * a), sa = __ldg(cs + 2 * a + 1);
-            const T ica = C::rcp(ca), isa = C::rcp(sa);
-            // inverse of (X, Y) -> (X c + Y s, -X s + Y c), nearest lattice column
+            // inverse of (X, Y) -> (X c + Y s, -X s + Y c), nearest lattice point
             const int c0 = (int)rint(ca * dx - sa * dy + o);
+            const int j0 = (int)rint(sa * dx + ca * dy + o);
+            T ys[3], yc[3];
+#pragma unroll
+            for (int u = 0; u < 3; u++) {
+                const T Y = (T)(j0 - 1 + u) - o;
+                ys[u] = C::mul(Y, sa);
+                yc[u] = C::mul(Y, ca);
+            }
             const T *pa = params + (size_t)4 * a * n;
 #pragma unroll
             for (int v = 0; v < 3; v++) {
                 const int cc = c0 - 1 + v;
                 if (cc < 0 || cc >= n)
                     continue;
-                const T X = (T)cc - o;
-                int jl, jh;
-                row_window<T>(X, ca, sa, ica, isa, fpx, fpy, o, mg, n, &jl, &jh);
-                if (jl > jh)
-                    continue;
                 T g0, g1, g2, mf;
                 Quad<T>::load(pa + 4 * cc, g0, g1, g2, mf);
+                const T X = (T)cc - o;
                 const T xc = C::mul(X, ca), xs = C::mul(X, -sa);
-                for (int j = jl; j <= jh; j++) {
-                    const T Y = (T)j - o;
-                    const T qx = C::add(C::add(xc, C::mul(Y, sa)), o);
-                    const T qy = C::add(C::add(xs, C::mul(Y, ca)), o);
-                    const T wx = (T)1 - fabs(qx - fpx), wy = (T)1 - fabs(qy - fpy);
-                    const bool in = qx >= (T)0 && qx < nm1 && qy >= (T)0 && qy < nm1 &&
-                                    wx > (T)0 && wy > (T)0;
+#pragma unroll
+                for (int u = 0; u < 3; u++) {
+                    const int j = j0 - 1 + u;
+                    const T qx = C::add(C::add(xc, ys[u]), o);
+                    const T qy = C::add(C::add(xs, yc[u]), o);
+                    // (1 - |qx - px|)+ (1 - |qy - py|)+: zero outside the stencil
+                    const T wx = fmax((T)1 - fabs(qx - fpx), (T)0);
+                    const T wy = fmax((T)1 - fabs(qy - fpy), (T)0);
                     const T rr = (T)j - mf;
                     const T g = rr >= (T)0 ? g0 + rr * (g1 + rr * g2) : g0;
-                    acc += in ? wx * wy * g : (T)0;
+                    if (kInterior) {
+                        acc += (j >= 0 && j < n) ? wx * wy * g : (T)0;
+                    } else {
+                        const bool in = j >= 0 && j < n && qx >= (T)0 && qx < nm1 &&
+                                        qy >= (T)0 && qy < nm1;
+                        acc += in ? wx * wy * g : (T)0;
+                    }
                 }
             }
         }
@@ -474,10 +454,15 @@ cudaError_t launch_sino_backward(const T *grad_sino, const int *medians, int n_i
     if (lines > 0)
         line_params_kernel<T><<<(unsigned)((lines + 255) / 256), 256, 0, st>>>(
             grad_sino, medians, n_images, n, n_angles, tf_code, n_t, params);
-    if (pix > 0)
-        adjoint_gather_kernel<T><<<dim3((unsigned)((pix + 31) / 32), n_images), 32 * kAdjWarps,
-                                   0, st>>>(rows, cols, row_off, col_off, n, n_angles, cs,
-                                            params, grad_img);
+    if (pix > 0) {
+        const dim3 grid((unsigned)((pix + 31) / 32), n_images);
+        if (interior_source(n, row_off, col_off, rows, cols))
+            adjoint_gather_kernel<T, true><<<grid, 32 * kAdjWarps, 0, st>>>(
+                rows, cols, row_off, col_off, n, n_angles, cs, params, grad_img);
+        else
+            adjoint_gather_kernel<T, false><<<grid, 32 * kAdjWarps, 0, st>>>(
+                rows, cols, row_off, col_off, n, n_angles, cs, params, grad_img);
+    }
     return cudaGetLastError();
 }
 
