@@ -99,6 +99,9 @@ def parse_args():
     ap.add_argument("--images", type=int, default=0,
                     help="with --profile-steps on batch512: only the first IMAGES images (a "
                          "small case for profiler captures)")
+    ap.add_argument("--tile", default=None, metavar="LINES,CTAS_PER_SM,LINES_PER_WARP",
+                    help="with --profile-steps on batch512: pin the sinogram kernel's tile "
+                         "shape instead of the autotuner's choice")
     ap.add_argument("--tfuncs", default=None,
                     help="comma-separated T-functional ids overriding the workload's")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
@@ -977,6 +980,8 @@ def run_profile_steps(args):
         offsets[1:] = np.cumsum([b.size for b in bufs])[:-1]
         flat = torch.from_numpy(np.concatenate(bufs)).cuda()
         eng = Engine(0)
+        if args.tile:
+            eng.batch_tile(pin=tuple(int(v) for v in args.tile.split(",")))
         for _ in range(args.profile_steps):
             eng.transform_batch(flat, offsets, [im.shape[0] for im in imgs],
                                 [im.shape[1] for im in imgs], steps, BATCH_T,
