@@ -77,9 +77,15 @@ template <typename T> __device__ __forceinline__ T block_sum_t(T v, T *red) {
     return t;
 }
 
+template <typename T> struct CS {
+    T c, s;
+};
+
 // P-stage adjoint.  Block per column (sinogram s, column a); dynamic shared
-// memory: x (rows), F (2 * (rows / 2 + 1)), d (rows / 2 + 1), all of T.
-// grad_circus: n_sino x n_p x cols; out: n_sino x cols x rows.
+// memory: x (rows), F (2 * (rows / 2 + 1)), the weighted coefficients
+// (2 * (rows / 2 + 1)), all of T, then -- when they fit -- the (cos, sin)
+// twiddle pairs (2 * rows).  grad_circus: n_sino x n_p x cols; out: n_sino x
+// cols x rows.
 template <typename T>
 __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int cols,
                                        int n_sino, const int *__restrict__ kinds, int n_p,
@@ -90,22 +96,20 @@ __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int
     extern __shared__ __align__(16) unsigned char smraw[];
     T *x = reinterpret_cast<T *>(smraw);
     const int nb = rows / 2 + 1;
-    T *Fr = x + rows, *Fi = Fr + nb, *d = Fi + nb;
+    T *Fr = x + rows, *Fi = Fr + nb, *wr = Fi + nb, *wi = wr + nb;
     const int a = blockIdx.x, s = blockIdx.y, tid = threadIdx.x, bd = blockDim.x;
     const T *col = sino + ((size_t)s * cols + a) * rows;
     for (int i = tid; i < rows; i += bd)
         x[i] = col[i];
-    // twiddles cos / sin(2 pi i / rows), staged in shared memory when they fit
-    const T *ct = cosv, *stw = sinv;
-    if (tab_in_smem) {
-        T *c_s = d + nb, *s_s = c_s + rows;
-        for (int i = tid; i < rows; i += bd) {
-            c_s[i] = cosv[i];
-            s_s[i] = sinv[i];
-        }
-        ct = c_s;
-        stw = s_s;
-    }
+    // twiddles (cos, sin)(2 pi i / rows), paired in shared memory when they fit
+    const int tw_off = (rows + 4 * nb + 1) & ~1; // pairs start at an even T
+    CS<T> *tw = reinterpret_cast<CS<T> *>(x + tw_off);
+    if (tab_in_smem)
+        for (int i = tid; i < rows; i += bd)
+            tw[i] = CS<T>{cosv[i], sinv[i]};
+    auto twid = [&](long idx) {
+        return tab_in_smem ? tw[idx] : CS<T>{__ldg(cosv + idx), __ldg(sinv + idx)};
+    };
     T g1 = 0, g3 = 0;
     for (int p = 0; p < n_p; p++) {
         const T g = grad_circus[((size_t)s * n_p + p) * cols + a];
@@ -121,8 +125,9 @@ __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int
             T re = 0, im = 0;
             long idx = 0;
             for (int n = 0; n < rows; n++) {
-                re += x[n] * ct[idx];
-                im -= x[n] * stw[idx];
+                const CS<T> w = twid(idx);
+                re += x[n] * w.c;
+                im -= x[n] * w.s;
                 idx += k;
                 if (idx >= rows)
                     idx -= rows;
@@ -131,7 +136,8 @@ __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int
             Fi[k] = im;
         }
         __syncthreads();
-        // d_k = 2 |F_k|^2 / N^4 * sum of trapz weights of the p that read bin k
+        // d_k = 2 |F_k|^2 / N^4 * sum of trapz weights of the p that read bin k;
+        // the inverse sum below takes 2 d_k F_k
         const T n4 = (T)rows * rows * rows * rows;
         for (int k = tid; k < nb; k += bd) {
             T wsum = 0;
@@ -147,7 +153,9 @@ __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int
                     w += (T)0.5 * (lin[p] - lin[p - 1]);
                 wsum += w;
             }
-            d[k] = (T)2 * (Fr[k] * Fr[k] + Fi[k] * Fi[k]) / n4 * wsum;
+            const T dk = (T)2 * (Fr[k] * Fr[k] + Fi[k] * Fi[k]) / n4 * wsum;
+            wr[k] = (T)2 * dk * Fr[k];
+            wi[k] = (T)2 * dk * Fi[k];
         }
         __syncthreads();
     }
@@ -167,7 +175,8 @@ __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int
             T acc = 0;
             long idx = 0;
             for (int k = 0; k < nb; k++) {
-                acc += (T)2 * d[k] * (Fr[k] * ct[idx] - Fi[k] * stw[idx]);
+                const CS<T> w = twid(idx);
+                acc += wr[k] * w.c - wi[k] * w.s;
                 idx += n;
                 if (idx >= rows)
                     idx -= rows;
@@ -429,7 +438,9 @@ cudaError_t launch_circus_backward(const T *sino, int rows, int cols, int n_sino
                                    cudaStream_t st) {
     if (rows <= 0 || cols <= 0 || n_sino <= 0)
         return cudaSuccess;
-    const size_t base = sizeof(T) * ((size_t)rows + 3 * (size_t)(rows / 2 + 1));
+    // x, F (re, im), 2 d F (re, im); the twiddle pairs after, at an even offset
+    const size_t head = (size_t)rows + 4 * (size_t)(rows / 2 + 1);
+    const size_t base = sizeof(T) * ((head + 1) & ~size_t(1));
     const size_t with_tab = base + sizeof(T) * 2 * (size_t)rows;
     const size_t limit = opt_in_smem((const void *)circus_backward_kernel<T>);
     if (limit == 0)
