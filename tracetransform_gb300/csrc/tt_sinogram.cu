@@ -14,11 +14,8 @@
 // reference's order with scalar round-to-nearest operations, so every
 // rotated sample is bit-identical to rotate()/interpolate()
 // (c++/src/auxiliary.cpp:182-196, 223-255): the host rounds cos/sin as the
-// reference does and no multiply-add is fused.  The independent pairs (the
-// two coordinates, the two terms of each bilinear product) run as packed
-// f32x2 operations with explicit round-to-nearest, which are never fused, so
-// every lane rounds exactly as the scalar reference does (tt_rotate runs the
-// same helpers and its output is tested bit for bit).  Each thread keeps
+// reference does and no multiply-add is fused.  (Packed f32x2 multiply + add
+// measured fused on this part, so they are not used here.)  Each thread keeps
 // four gathers in flight.  Only rows whose stencil can touch the image are
 // sampled; all others are exact zeros in the reference too.
 //
@@ -38,26 +35,6 @@
 
 namespace tt {
 namespace {
-
-// The reference's rotated coordinates ((X c + Y s) + o, (X (-s) + Y c) + o)
-// with X c and X (-s) given, each operation rounded to nearest.
-__device__ __forceinline__ float2 rot_coords(float Xc, float Xms, float Y, float s, float c,
-                                             float ox, float oy) {
-    const float2 ys = mul2_rn(make_float2(Y, Y), make_float2(s, c));
-    return add2_rn(add2_rn(make_float2(Xc, Xms), ys), make_float2(ox, oy));
-}
-
-// interpolate()'s combination of the 2x2 stencil g (tld4 order w, x, z, y =
-// s00, s10, s01, s11) with the fractions (xf, yf): ((s00 (1-xf)) (1-yf) +
-// (s10 xf) (1-yf)) + (s01 (1-xf)) yf) + (s11 xf) yf, every operation rounded.
-__device__ __forceinline__ float bilinear_rn(float4 g, float xf, float yf) {
-    const float2 om = add2_rn(make_float2(1.f, 1.f), make_float2(-xf, -yf));
-    const float2 t01 = mul2_rn(mul2_rn(make_float2(g.w, g.x), make_float2(om.x, xf)),
-                               make_float2(om.y, om.y));
-    const float2 t23 = mul2_rn(mul2_rn(make_float2(g.z, g.y), make_float2(om.x, xf)),
-                               make_float2(yf, yf));
-    return __fadd_rn(__fadd_rn(__fadd_rn(t01.x, t01.y), t23.x), t23.y);
-}
 
 // Rows [lo, hi) of a line whose samples can be non-zero: the reference's
 // bounds test 0 <= q < n-1 intersected with the band where the 2x2 stencil
@@ -226,21 +203,26 @@ __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long
             for (int u = 0; u < U; u++) {
                 const int jr = first + 32 * (i0 + u);
                 const float Y = (float)(jlo + jr) - o;
-                const float2 q = rot_coords(Xc, Xms, Y, s, c, o, o);
-                const float qx = q.x, qy = q.y;
+                // (x c + y s) + o and (x (-s) + y c) + o, each operation rounded
+                const float qx = __fadd_rn(__fadd_rn(Xc, __fmul_rn(Y, s)), o);
+                const float qy = __fadd_rn(__fadd_rn(Xms, __fmul_rn(Y, c)), o);
                 ok[u] = colok && jr < len;
                 if (!kInterior) // see warp_sample: border texels answer the test
                     ok[u] = ok[u] && qx >= 0.f && qx < nm1 && qy >= 0.f && qy < nm1;
                 const float xi = truncf(qx), yi = truncf(qy);
-                const float2 f = add2_rn(q, make_float2(-xi, -yi));
-                xf[u] = f.x;
-                yf[u] = f.y;
+                xf[u] = __fsub_rn(qx, xi);
+                yf[u] = __fsub_rn(qy, yi);
                 // texel (u, v) = image (row, col); w/z/x/y = s00, s10, s01, s11
                 g[u] = tex2Dgather<float4>(J.tex, yi + tu, xi + tv, 0);
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
-                const float v = bilinear_rn(g[u], xf[u], yf[u]);
+                const float omx = __fsub_rn(1.f, xf[u]), omy = __fsub_rn(1.f, yf[u]);
+                const float t0 = __fmul_rn(__fmul_rn(g[u].w, omx), omy);
+                const float t1 = __fmul_rn(__fmul_rn(g[u].x, xf[u]), omy);
+                const float t2 = __fmul_rn(__fmul_rn(g[u].z, omx), yf[u]);
+                const float t3 = __fmul_rn(__fmul_rn(g[u].y, xf[u]), yf[u]);
+                const float v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
                 if (i0 + u < C)
                     dst[first + 32 * (i0 + u)] = ok[u] ? v : 0.f;
             }
@@ -583,21 +565,25 @@ __device__ __forceinline__ void warp_sample(const BlockJob &J, float *x, int col
         for (int u = 0; u < U; u++) {
             const int jr = sub + SW * (i0 + u);
             const float Y = Y0 + (float)(SW * u);
-            const float2 q = rot_coords(Xc, Xms, Y, sn, c, o, o);
-            const float qx = q.x, qy = q.y;
+            const float qx = __fadd_rn(__fadd_rn(Xc, __fmul_rn(Y, sn)), o);
+            const float qy = __fadd_rn(__fadd_rn(Xms, __fmul_rn(Y, c)), o);
             ok[u] = colok && jr < len;
             if (kBounds)
                 ok[u] = ok[u] && qx >= 0.f && qx < nm1 && qy >= 0.f && qy < nm1;
             const float xi = truncf(qx), yi = truncf(qy);
-            const float2 f = add2_rn(q, make_float2(-xi, -yi));
-            xf[u] = f.x;
-            yf[u] = f.y;
+            xf[u] = __fsub_rn(qx, xi);
+            yf[u] = __fsub_rn(qy, yi);
             g[u] = tex2Dgather<float4>(J.tex, yi + tu, xi + tv, 0);
         }
         Y0 += (float)(SW * U);
 #pragma unroll
         for (int u = 0; u < U; u++) {
-            const float v = bilinear_rn(g[u], xf[u], yf[u]);
+            const float omx = __fsub_rn(1.f, xf[u]), omy = __fsub_rn(1.f, yf[u]);
+            const float t0 = __fmul_rn(__fmul_rn(g[u].w, omx), omy);
+            const float t1 = __fmul_rn(__fmul_rn(g[u].x, xf[u]), omy);
+            const float t2 = __fmul_rn(__fmul_rn(g[u].z, omx), yf[u]);
+            const float t3 = __fmul_rn(__fmul_rn(g[u].y, xf[u]), yf[u]);
+            const float v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
             if (i0 + u < C)
                 x[sub + SW * (i0 + u)] = ok[u] ? v : 0.f;
         }
@@ -838,15 +824,19 @@ __global__ void rotate_kernel(cudaTextureObject_t tex, int rows, int cols, float
     const int row = (int)(i % rows), col = (int)(i / rows);
     const float ox = (float)(cols - 1) * 0.5f, oy = (float)(rows - 1) * 0.5f;
     const float X = (float)col - ox, Y = (float)row - oy;
-    const float2 xcs = mul2_rn(make_float2(X, X), make_float2(cs.x, -cs.y));
-    const float2 q = rot_coords(xcs.x, xcs.y, Y, cs.y, cs.x, ox, oy);
-    const float qx = q.x, qy = q.y;
+    const float qx = __fadd_rn(__fadd_rn(__fmul_rn(X, cs.x), __fmul_rn(Y, cs.y)), ox);
+    const float qy = __fadd_rn(__fadd_rn(__fmul_rn(X, -cs.y), __fmul_rn(Y, cs.x)), oy);
     float v = 0.f;
     if (qx >= 0.f && qx < (float)(cols - 1) && qy >= 0.f && qy < (float)(rows - 1)) {
         const float xi = truncf(qx), yi = truncf(qy);
-        const float2 f = add2_rn(q, make_float2(-xi, -yi));
+        const float xf = __fsub_rn(qx, xi), yf = __fsub_rn(qy, yi);
         const float4 g = tex2Dgather<float4>(tex, yi + 1.f, xi + 1.f, 0);
-        v = bilinear_rn(g, f.x, f.y);
+        const float omx = __fsub_rn(1.f, xf), omy = __fsub_rn(1.f, yf);
+        const float t0 = __fmul_rn(__fmul_rn(g.w, omx), omy);
+        const float t1 = __fmul_rn(__fmul_rn(g.x, xf), omy);
+        const float t2 = __fmul_rn(__fmul_rn(g.z, omx), yf);
+        const float t3 = __fmul_rn(__fmul_rn(g.y, xf), yf);
+        v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
     }
     out[i] = v;
 }
