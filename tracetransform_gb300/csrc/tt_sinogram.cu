@@ -773,6 +773,7 @@ __global__ void __launch_bounds__(32 * W, 32 / W) sino_batch_warp_kernel(const B
     extern __shared__ __align__(16) float smw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float *xw = smw + (size_t)warp * LPW * b.stride;
+    int lo = 0; // image of the warp's previous item: claims only grow
     for (;;) {
         int item = 0;
         if (lane == 0)
@@ -780,13 +781,16 @@ __global__ void __launch_bounds__(32 * W, 32 / W) sino_batch_warp_kernel(const B
         item = __shfl_sync(TT_FULL_MASK, item, 0);
         if (item >= b.total_items)
             break;
-        int lo = 0, hi = b.n_img - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (__ldg(&b.img[mid].items_begin) <= item)
-                lo = mid;
-            else
-                hi = mid - 1;
+        if (lo + 1 < b.n_img && __ldg(&b.img[lo + 1].items_begin) <= item) {
+            int hi = b.n_img - 1; // a later image: search [lo + 1, n_img)
+            ++lo;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (__ldg(&b.img[mid].items_begin) <= item)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
         }
         const BatchImage &im = b.img[lo];
         const int k = item - im.items_begin;
