@@ -1147,16 +1147,26 @@ static tt_status circus_backward_impl(tt_plan *plan, const T *d_sino, int rows, 
         return fail(TT_ERR_INVALID_ARG, "bad sinogram stack for the backward pass");
     const T *cosv, *sinv, *lin;
     const int *kinds;
-    TT_CHECK(p->get_dft<T>(rows, &cosv, &sinv));
     TT_CHECK(p->get_kinds(pf, n_p, &kinds));
     if (sizeof(T) == sizeof(float)) {
         const FftTables *f;
-        TT_CHECK(p->get_fft(rows, &f)); // the forward's float linspace
+        TT_CHECK(p->get_fft(rows, &f)); // the forward's float linspace and FFT tables
         lin = (const T *)f->lin;
+        // both DFTs of a column by the chirp-z FFT where its M-point buffer
+        // fits in shared memory, else the direct sums below
+        if (tt::circus_backward_fft_fits(rows, f->M)) {
+            TT_CUDA(tt::launch_circus_backward_fft(
+                (const float *)d_sino, rows, cols, n_sino, kinds, n_p,
+                (const float *)d_grad_circus, f->chirp, f->filt, f->twid, f->M, f->lin,
+                (float *)d_grad_sino, pick_stream(p, stream)));
+            return TT_OK;
+        }
+        TT_CHECK(p->get_dft<T>(rows, &cosv, &sinv));
     } else {
         const double *l;
         TT_CHECK(p->get_lin64(rows, &l));
         lin = (const T *)l;
+        TT_CHECK(p->get_dft<T>(rows, &cosv, &sinv));
     }
     TT_CUDA(tt::launch_circus_backward<T>(d_sino, rows, cols, n_sino, kinds, n_p, d_grad_circus,
                                           cosv, sinv, lin, d_grad_sino, pick_stream(p, stream)));

@@ -11,7 +11,10 @@
 //                            P3 = trapz(lin, y), so with w_p the trapz weights and
 //                            d_k = 2 |F_k|^2 / N^4 sum_{m(p) = k} w_p,
 //                            dP3/dx_n = sum_{k <= N/2} 2 d_k Re(conj(F_k) e^{-2 pi i k n / N})
-//                     (direct DFTs with an exact twiddle index; the P-stage is small)
+//                     (float: both DFTs of a column by the chirp-z FFT on the
+//                     forward's tables, O(M log M); double, and float columns
+//                     whose FFT buffer exceeds shared memory: direct sums with an
+//                     exact twiddle index)
 //   line_params       per line (angle, column): (G0, G1, G2, m) with G_t the
 //                     gradient of sinogram t at that entry and m the weighted
 //                     median the forward used -- dT1/dx_j = (j - m)+,
@@ -183,6 +186,137 @@ __global__ void circus_backward_kernel(const T *__restrict__ sino, int rows, int
             }
             g += g3 * acc;
         }
+        out[((size_t)s * cols + a) * rows + n] = g;
+    }
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// In-place chirp-z convolution step on M = 2^logM points: forward radix-2
+// DIT of the bit-reversed input (natural-order result), times the filter,
+// inverse radix-2 DIF with conjugate twiddles (bit-reversed result).  The
+// input must be scattered to fft[brev(j)] before; every thread calls it.
+__device__ void chirp_convolve(float2 *fft, int M, const float2 *__restrict__ twid,
+                               const float2 *__restrict__ filt) {
+    const int tid = threadIdx.x, bd = blockDim.x;
+    for (int h = 1; h < M; h <<= 1) {
+        const int tstep = M / (2 * h);
+        for (int i = tid; i < M / 2; i += bd) {
+            const int pos = i & (h - 1);
+            const int ia = ((i - pos) << 1) + pos, ib = ia + h;
+            const float2 t = cmulf(fft[ib], __ldg(twid + pos * tstep));
+            const float2 u = fft[ia];
+            fft[ia] = make_float2(u.x + t.x, u.y + t.y);
+            fft[ib] = make_float2(u.x - t.x, u.y - t.y);
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < M; i += bd)
+        fft[i] = cmulf(fft[i], __ldg(filt + i));
+    __syncthreads();
+    for (int h = M / 2; h >= 1; h >>= 1) {
+        const int tstep = M / (2 * h);
+        for (int i = tid; i < M / 2; i += bd) {
+            const int pos = i & (h - 1);
+            const int ia = ((i - pos) << 1) + pos, ib = ia + h;
+            const float2 u = fft[ia], w = fft[ib];
+            const float2 tw = __ldg(twid + pos * tstep);
+            fft[ia] = make_float2(u.x + w.x, u.y + w.y);
+            fft[ib] = cmulf(make_float2(u.x - w.x, u.y - w.y), make_float2(tw.x, -tw.y));
+        }
+        __syncthreads();
+    }
+}
+
+// The float P-stage adjoint with both DFTs of a column by the chirp-z
+// identity (the forward's tables: chirp w_j = exp(-i pi j^2 / N), the
+// M-point filter and twiddles, M >= 2N - 1 a power of two), O(M log M) per
+// column instead of the direct sums' O(N^2):
+//   F_k = w_k conv(x w, conj w)_k                     (k <= N/2)
+//   W_k = 2 d_k F_k,  dP3/dx_n = Re sum_k W_k e^{2 pi i k n / N}
+//       = Re w_n conv(conj(W) w, conj w)_n            (n < N)
+// Block per column; dynamic shared memory: the M-point buffer, x (rows) and
+// W (N/2 + 1 pairs).
+__global__ void circus_backward_fft_kernel(const float *__restrict__ sino, int rows, int cols,
+                                           const int *__restrict__ kinds, int n_p,
+                                           const float *__restrict__ grad_circus,
+                                           const float2 *__restrict__ chirp,
+                                           const float2 *__restrict__ filt,
+                                           const float2 *__restrict__ twid, int M,
+                                           const float *__restrict__ lin,
+                                           float *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2 *fft = reinterpret_cast<float2 *>(smraw);
+    const int nb = rows / 2 + 1;
+    float2 *W = fft + M;
+    float *x = reinterpret_cast<float *>(W + nb);
+    const int a = blockIdx.x, s = blockIdx.y, tid = threadIdx.x, bd = blockDim.x;
+    const int logM = 31 - __clz(M);
+    const float *col = sino + ((size_t)s * cols + a) * rows;
+    for (int i = tid; i < rows; i += bd)
+        x[i] = col[i];
+    float g1 = 0.f, g3 = 0.f;
+    for (int p = 0; p < n_p; p++) {
+        const float g = grad_circus[((size_t)s * n_p + p) * cols + a];
+        if (kinds[p] == 1)
+            g1 += g;
+        else if (kinds[p] == 3)
+            g3 += g;
+    }
+    if (g3 != 0.f) {
+        for (int i = tid; i < M; i += bd)
+            fft[i] = make_float2(0.f, 0.f);
+        __syncthreads();
+        for (int j = tid; j < rows; j += bd) {
+            const float2 w = __ldg(chirp + j);
+            fft[__brev(j) >> (32 - logM)] = make_float2(x[j] * w.x, x[j] * w.y);
+        }
+        __syncthreads();
+        chirp_convolve(fft, M, twid, filt);
+        const float n4 = (float)rows * rows * (float)rows * rows;
+        for (int k = tid; k < nb; k += bd) {
+            const float2 F = cmulf(fft[__brev(k) >> (32 - logM)], __ldg(chirp + k));
+            float wsum = 0.f;
+            const int ps[2] = {k, rows - k};
+            for (int u = 0; u < 2; u++) {
+                const int p = ps[u];
+                if (p < 0 || p >= rows || (u == 1 && (p <= rows / 2 || p == k)))
+                    continue;
+                if (p + 1 <= rows - 1)
+                    wsum += 0.5f * (__ldg(lin + p + 1) - __ldg(lin + p));
+                if (p >= 1)
+                    wsum += 0.5f * (__ldg(lin + p) - __ldg(lin + p - 1));
+            }
+            const float dk2 = 4.f * (F.x * F.x + F.y * F.y) / n4 * wsum; // 2 d_k
+            W[k] = make_float2(dk2 * F.x, dk2 * F.y);
+        }
+        __syncthreads();
+        for (int i = tid; i < M; i += bd)
+            fft[i] = make_float2(0.f, 0.f);
+        __syncthreads();
+        for (int k = tid; k < nb; k += bd) {
+            const float2 w = __ldg(chirp + k);
+            fft[__brev(k) >> (32 - logM)] = cmulf(make_float2(W[k].x, -W[k].y), w);
+        }
+        __syncthreads();
+        chirp_convolve(fft, M, twid, filt);
+    } else {
+        __syncthreads();
+    }
+    for (int n = tid; n < rows; n += bd) {
+        float g = 0.f;
+        if (g1 != 0.f) {
+            float v = 0.f;
+            if (n >= 1)
+                v += sgn(x[n] - x[n - 1]);
+            if (n + 1 < rows)
+                v -= sgn(x[n + 1] - x[n]);
+            g += g1 * v;
+        }
+        if (g3 != 0.f)
+            g += g3 * cmulf(fft[__brev(n) >> (32 - logM)], __ldg(chirp + n)).x;
         out[((size_t)s * cols + a) * rows + n] = g;
     }
 }
@@ -513,6 +647,31 @@ cudaError_t launch_circus_f64(const double *sino, int rows, int cols, int n_sino
     circus_f64_kernel<<<dim3(cols, n_sino), 256, smem, st>>>(sino, rows, cols, d_kinds, n_p, cosv,
                                                              sinv, lin, out);
     return cudaGetLastError();
+}
+
+cudaError_t launch_circus_backward_fft(const float *sino, int rows, int cols, int n_sino,
+                                       const int *d_kinds, int n_p, const float *grad_circus,
+                                       const float2 *chirp, const float2 *filt,
+                                       const float2 *twid, int M, const float *lin, float *out,
+                                       cudaStream_t st) {
+    if (rows <= 0 || cols <= 0 || n_sino <= 0)
+        return cudaSuccess;
+    const size_t smem = circus_backward_fft_smem(rows, M);
+    const size_t limit = opt_in_smem((const void *)circus_backward_fft_kernel);
+    if (limit == 0 || smem > limit || M < 2 * rows - 1 || (M & (M - 1)))
+        return cudaErrorInvalidValue;
+    circus_backward_fft_kernel<<<dim3(cols, n_sino), 512, smem, st>>>(
+        sino, rows, cols, d_kinds, n_p, grad_circus, chirp, filt, twid, M, lin, out);
+    return cudaGetLastError();
+}
+
+size_t circus_backward_fft_smem(int rows, int M) {
+    return sizeof(float2) * ((size_t)M + rows / 2 + 1) + sizeof(float) * (size_t)rows;
+}
+
+bool circus_backward_fft_fits(int rows, int M) {
+    return circus_backward_fft_smem(rows, M) <=
+           opt_in_smem((const void *)circus_backward_fft_kernel);
 }
 
 template cudaError_t launch_circus_backward<float>(const float *, int, int, int, const int *, int,

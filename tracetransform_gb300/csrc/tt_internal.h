@@ -144,6 +144,16 @@ cudaError_t launch_circus_backward(const T *sino, int rows, int cols, int n_sino
                                    const int *d_kinds, int n_p, const T *grad_circus,
                                    const T *cosv, const T *sinv, const T *lin, T *out,
                                    cudaStream_t st);
+// The float P-stage adjoint by the chirp-z identity on the forward's FFT
+// tables (chirp, filter, twiddles of length M); cudaErrorInvalidValue when
+// its shared memory (circus_backward_fft_smem) exceeds the device's.
+cudaError_t launch_circus_backward_fft(const float *sino, int rows, int cols, int n_sino,
+                                       const int *d_kinds, int n_p, const float *grad_circus,
+                                       const float2 *chirp, const float2 *filt,
+                                       const float2 *twid, int M, const float *lin, float *out,
+                                       cudaStream_t st);
+size_t circus_backward_fft_smem(int rows, int M);
+bool circus_backward_fft_fits(int rows, int M);
 template <typename T>
 cudaError_t launch_sino_backward(const T *grad_sino, const int *medians, int n_images, int n,
                                  int n_angles, unsigned long long tf_code, int n_t, T *params,
