@@ -704,25 +704,18 @@ __device__ void warp_lines(const BlockJob &J, unsigned long long tf_code, int n_
             r345[2] = hypotf(seg_sum<SW>(re5), seg_sum<SW>(im5));
     }
 
-    // 4. one lane per line writes its outputs
-    if (sub == 0 && colok) {
+    // 4. lane t of a segment writes its line's output t (every lane of the
+    // segment holds the line's sums and medians)
+    if (colok) {
         const size_t plane = J.plane;
         const size_t at = (size_t)angle * n + col;
-        for (int t = 0; t < n_t; t++) {
+        for (int t = sub; t < n_t; t += SW) {
             const int f = (int)((tf_code >> (3 * t)) & 7ull);
-            float v;
-            int med;
-            switch (f) {
-            case 0: v = S; med = -1; break;
-            case 1: v = r1v; med = m1; break;
-            case 2: v = r2v; med = m1; break;
-            case 3: v = r345[0]; med = m2; break;
-            case 4: v = r345[1]; med = m2; break;
-            default: v = r345[2]; med = m2; break;
-            }
+            const float v = f == 0 ? S : f == 1 ? r1v : f == 2 ? r2v
+                          : f == 3 ? r345[0] : f == 4 ? r345[1] : r345[2];
             J.out[t * plane + at] = v;
             if (J.medians)
-                J.medians[t * plane + at] = med;
+                J.medians[t * plane + at] = f == 0 ? -1 : f <= 2 ? m1 : m2;
         }
     }
 }
