@@ -204,8 +204,10 @@ tt_status tt_circus_device(tt_plan *plan, const float *d_sino, int rows, int col
  * stretched to tt_ortho_size; here it takes sinograms of any size, so a
  * Hermite circus can sit beside P1-P3 of the regular sinograms.
  * Synchronises the stream once (the aligned matrices' sizes depend on the
- * weighted medians) and then once per Jacobi sweep; *sweeps (may be NULL)
- * receives the number of sweeps. */
+ * weighted medians); the Jacobi sweeps loop on the device (a conditional
+ * graph node whose stop rule runs after each sweep).  *sweeps (may be NULL)
+ * receives the number of sweeps -- asking for it adds a synchronisation at
+ * the end. */
 tt_status tt_circus_orthonormal_device(tt_plan *plan, const float *d_sino, int rows, int cols,
                                        int n_sino, const tt_pfunctional *pfuncs, int n_p,
                                        float *d_out, int32_t *centers, int32_t *sweeps,

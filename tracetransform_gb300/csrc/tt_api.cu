@@ -299,6 +299,49 @@ struct tt_plan {
         g.key = key;
         return TT_OK;
     }
+    // A graph that runs the body fn captures while the body keeps its
+    // condition set (cudaGraphSetConditional from a body kernel); each
+    // launch of the graph starts with the condition at 1, so the body runs
+    // at least once.
+    template <typename F>
+    tt_status while_graph(Graph &g, const std::vector<const void *> &key, F fn) {
+        if (g.exec && g.key == key)
+            return TT_OK;
+        if (g.exec) {
+            TT_CUDA(cudaGraphExecDestroy(g.exec));
+            g.exec = nullptr;
+        }
+        if (!capture_stream)
+            TT_CUDA(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking));
+        cudaGraph_t gr = nullptr;
+        TT_CUDA(cudaGraphCreate(&gr, 0));
+        cudaGraphConditionalHandle loop = 0;
+        cudaError_t e = cudaGraphConditionalHandleCreate(&loop, gr, 1, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = loop;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        if (e == cudaSuccess)
+            e = cudaGraphAddNode(&node, gr, nullptr, nullptr, 0, &np);
+        if (e == cudaSuccess)
+            e = cudaStreamBeginCaptureToGraph(capture_stream, np.conditional.phGraph_out[0],
+                                              nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const cudaError_t le = fn(capture_stream, loop);
+            cudaGraph_t body = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(capture_stream, &body);
+            e = le != cudaSuccess ? le : ce;
+        }
+        if (e == cudaSuccess)
+            e = cudaGraphInstantiate(&g.exec, gr, 0);
+        cudaGraphDestroy(gr);
+        TT_CUDA(e);
+        g.key = key;
+        return TT_OK;
+    }
     tt_status ensure(DevBuf &b, size_t bytes) {
         if (b.bytes >= bytes && b.p)
             return TT_OK;
@@ -712,7 +755,8 @@ tt_status run_circus(tt_plan *p, const float *d_sino, int rows, int cols, int n_
 // Nearest orthonormal sinograms (c++/src/circus.cpp:68-102) of n_sino device
 // sinograms of rows x cols: results in p->nos, desc[s].out_off / .m per
 // sinogram, centers[s] the new Hermite centers.  One host synchronisation:
-// the aligned matrices' sizes depend on the weighted medians.
+// the aligned matrices' sizes depend on the weighted medians (a second, at
+// the end, only when *sweeps is asked for).
 tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sino,
                   cudaStream_t st, std::vector<NosDesc> &desc, std::vector<int> &centers,
                   int *sweeps = nullptr) {
@@ -753,11 +797,12 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
     if (cols > 1024)
         return fail(TT_ERR_UNSUPPORTED, "orthonormal circus of %d angles exceeds 1024", cols);
     // scratch: 5 double-float + 3 int vectors of n, 3 float n x n matrices,
-    // 2 float vectors
+    // 2 float vectors, the sweep loop's state
     const size_t nv = ncol, nm = (size_t)cols * cols * n_sino;
     TT_CHECK(p->ensure(p->nos_work, sizeof(float2) * 5 * nv + sizeof(int) * 3 * nv +
                                         sizeof(float) * (3 * nm + 2 * nv) +
-                                        sizeof(unsigned) * n_sino + sizeof(float) * n_sino + 64));
+                                        sizeof(unsigned) * n_sino + sizeof(float) * n_sino +
+                                        sizeof(unsigned) * 2 + 64));
     tt::NosWork w;
     {
         char *q = (char *)p->nos_work.p;
@@ -774,6 +819,7 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
         w.perm = w.cmap + 2 * nv;
         w.off_bits = (unsigned *)(w.perm + nv);
         w.tiny = (float *)(w.off_bits + n_sino);
+        w.sweep_state = (unsigned *)(w.tiny + n_sino);
     }
     TT_CUDA(cudaMemcpyAsync(p->nos_desc.p, desc.data(), sizeof(NosDesc) * n_sino,
                             cudaMemcpyHostToDevice, st));
@@ -792,36 +838,23 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
     TT_CHECK(p->graph(p->nos_factor_graph, key, [&](cudaStream_t cs) {
         return tt::launch_nos_factor(A, d_desc, cols, n_sino, max_m, w, cs);
     }));
-    TT_CHECK(p->graph(p->nos_sweep_graph, key, [&](cudaStream_t cs) {
-        return tt::launch_nos_sweep(cols, n_sino, w, cs);
-    }));
+    // the sweeps: a device-side while loop (the stop rule runs after each
+    // sweep on the device), at most 40
+    TT_CHECK(p->while_graph(p->nos_sweep_graph, key,
+                            [&](cudaStream_t cs, cudaGraphConditionalHandle loop) {
+                                return tt::launch_nos_sweep(cols, n_sino, w, 40, loop, cs);
+                            }));
     TT_CUDA(cudaGraphLaunch(p->nos_factor_graph.exec, st));
-    // Stop when the largest rotated pair's cosine is below the done bound, or
-    // when it has stopped falling (quadratic convergence takes it down by
-    // orders of magnitude per sweep; a plateau below 1e-3 is the float
-    // rounding floor of the rotated columns, which grows with sqrt(A)).
-    std::vector<unsigned> bits(n_sino);
-    float prev = 1.f;
-    if (sweeps)
-        *sweeps = 0;
-    for (int sweep = 0; sweep < 40; sweep++) {
-        if (sweeps)
-            *sweeps = sweep + 1;
-        TT_CUDA(cudaGraphLaunch(p->nos_sweep_graph.exec, st));
-        TT_CUDA(cudaMemcpyAsync(bits.data(), w.off_bits, sizeof(unsigned) * n_sino,
-                                cudaMemcpyDeviceToHost, st));
-        TT_CUDA(cudaStreamSynchronize(st));
-        float worst = 0.f;
-        for (unsigned b : bits) {
-            float v;
-            std::memcpy(&v, &b, sizeof v);
-            worst = std::max(worst, v);
-        }
-        if (worst < tt::nos_sweep_done_bound() || (worst < 1e-3f && worst > 0.25f * prev))
-            break;
-        prev = worst;
-    }
+    TT_CUDA(cudaMemsetAsync(w.sweep_state, 0, sizeof(unsigned) * 2, st));
+    TT_CUDA(cudaGraphLaunch(p->nos_sweep_graph.exec, st));
     TT_CUDA(tt::launch_nos_assemble(A, d_desc, cols, n_sino, max_m, w, (float *)p->nos.p, st));
+    if (sweeps) { // the count is read back only when asked for
+        unsigned done = 0;
+        TT_CUDA(cudaMemcpyAsync(&done, w.sweep_state + 1, sizeof done, cudaMemcpyDeviceToHost,
+                                st));
+        TT_CUDA(cudaStreamSynchronize(st));
+        *sweeps = (int)done;
+    }
     return TT_OK;
 }
 
@@ -1375,10 +1408,7 @@ tt_status tt_circus_orthonormal_device(tt_plan *plan, const float *d_sino, int r
     cudaStream_t st = pick_stream(p, stream);
     std::vector<NosDesc> desc;
     std::vector<int> c;
-    int nsw = 0;
-    TT_CHECK(run_nos(p, d_sino, rows, cols, n_sino, st, desc, c, &nsw));
-    if (sweeps)
-        *sweeps = nsw;
+    TT_CHECK(run_nos(p, d_sino, rows, cols, n_sino, st, desc, c, sweeps));
     for (int s = 0; s < n_sino; s++) {
         const int32_t c32 = c[s];
         TT_CHECK(run_circus(p, (const float *)p->nos.p + desc[s].out_off, desc[s].m, cols, 1,

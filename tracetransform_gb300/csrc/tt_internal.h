@@ -185,6 +185,7 @@ struct NosWork {
     float *inv;                 // n_sino x n
     unsigned *off_bits;         // n_sino: largest rotated |cos| of a sweep (float bits)
     float *tiny;                // n_sino: squared column norm below which a direction is null
+    unsigned *sweep_state;      // 2: the last sweep's largest cos (float bits), sweeps done
 };
 cudaError_t launch_nos_offsets(const float *sino, int rows, int cols, int n_sino, int center,
                                int *offsets, cudaStream_t st);
@@ -195,9 +196,12 @@ cudaError_t launch_nos_align(const float *sino, int rows, int cols, int n_sino,
 cudaError_t launch_nos_factor(float2 *A, const NosDesc *desc, int n, int n_sino, int max_m,
                               const NosWork &w, cudaStream_t st);
 int nos_max_rows(); // aligned rows the QR kernels hold in registers
-// One Jacobi sweep on X (n - 1 + (n & 1) launches).
-cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, cudaStream_t st);
-float nos_sweep_done_bound();
+// One Jacobi sweep on X (n - 1 + (n & 1) launches), then the stop rule on
+// the device: the sweep sets the while-loop condition `loop` to 0 when the
+// iteration has converged or max_sweeps sweeps are done (w.sweep_state,
+// zeroed before the loop, counts them).
+cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, int max_sweeps,
+                             cudaGraphConditionalHandle loop, cudaStream_t st);
 size_t nos_apply_smem(int max_m);
 cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int n_sino,
                                 int max_m, const NosWork &w, float *out, cudaStream_t st);

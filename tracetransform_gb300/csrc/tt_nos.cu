@@ -1129,6 +1129,32 @@ nos_apply_q_reg_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__
     }
 }
 
+// The stop rule after a sweep: the largest rotated cosine over the
+// sinograms below kJacDone, or below 1e-3 and no longer falling by 4x (the
+// float rounding floor of the rotated columns, which grows with sqrt(n) --
+// near convergence the cyclic method is quadratic, so a real decrease is by
+// orders of magnitude), or max_sweeps done.  state = {previous sweep's
+// largest cosine (float bits; 1 before the first), sweeps done}.
+__global__ void nos_sweep_check_kernel(const unsigned *__restrict__ off_bits, int n_sino,
+                                       unsigned *__restrict__ state, int max_sweeps,
+                                       cudaGraphConditionalHandle loop) {
+    float worst = 0.f;
+    for (int i = threadIdx.x; i < n_sino; i += 32)
+        worst = fmaxf(worst, __uint_as_float(off_bits[i]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        worst = fmaxf(worst, __shfl_xor_sync(TT_FULL_MASK, worst, o));
+    if (threadIdx.x != 0)
+        return;
+    const unsigned done = state[1] + 1;
+    const float prev = done == 1 ? 1.f : __uint_as_float(state[0]);
+    state[0] = __float_as_uint(worst);
+    state[1] = done;
+    const bool stop = worst < kJacDone || (worst < 1e-3f && worst > 0.25f * prev) ||
+                      (int)done >= max_sweeps;
+    cudaGraphSetConditional(loop, stop ? 0u : 1u);
+}
+
 } // namespace
 
 cudaError_t launch_nos_offsets(const float *sino, int rows, int cols, int n_sino, int center,
@@ -1204,26 +1230,31 @@ static cudaError_t block_rounds(int n, int n_sino, const NosWork &w, cudaStream_
     return cudaGetLastError();
 }
 
-cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, cudaStream_t st) {
+cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, int max_sweeps,
+                             cudaGraphConditionalHandle loop, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(w.off_bits, 0, sizeof(unsigned) * n_sino, st);
     if (e != cudaSuccess)
         return e;
     if (n <= 128)
-        return block_rounds<1>(n, n_sino, w, st);
-    if (n <= 256)
-        return block_rounds<2>(n, n_sino, w, st);
-    if (n <= 384)
-        return block_rounds<3>(n, n_sino, w, st);
-    if (n <= 512)
-        return block_rounds<4>(n, n_sino, w, st);
-    if (n <= 768)
-        return block_rounds<6>(n, n_sino, w, st);
-    if (n <= 1024)
-        return block_rounds<8>(n, n_sino, w, st);
-    return cudaErrorInvalidValue; // more than 1024 angles
+        e = block_rounds<1>(n, n_sino, w, st);
+    else if (n <= 256)
+        e = block_rounds<2>(n, n_sino, w, st);
+    else if (n <= 384)
+        e = block_rounds<3>(n, n_sino, w, st);
+    else if (n <= 512)
+        e = block_rounds<4>(n, n_sino, w, st);
+    else if (n <= 768)
+        e = block_rounds<6>(n, n_sino, w, st);
+    else if (n <= 1024)
+        e = block_rounds<8>(n, n_sino, w, st);
+    else
+        e = cudaErrorInvalidValue; // more than 1024 angles
+    if (e != cudaSuccess)
+        return e;
+    nos_sweep_check_kernel<<<1, 32, 0, st>>>(w.off_bits, n_sino, w.sweep_state, max_sweeps,
+                                             loop);
+    return cudaGetLastError();
 }
-
-float nos_sweep_done_bound() { return kJacDone; }
 
 size_t nos_apply_smem(int max_m) { return sizeof(float) * (size_t)kQCols * max_m; }
 
