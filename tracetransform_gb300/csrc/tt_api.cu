@@ -594,7 +594,7 @@ tt_status run_sinograms(tt_plan *p, const float *d_src, int src_rows, int src_co
     for (int t = 0; t < n_t; t++)
         a.tf[t] = tfuncs[t];
     a.need = need;
-    if (!(need & ((1u << 6) | (1u << 7))) && n <= 1024) {
+    if (!(need & ((1u << 6) | (1u << 7))) && n <= 1024 && n_t <= tt::kWarpMaxOutputs) {
         // T0-T5 of short lines: two lines per warp (the shape the batch tuner
         // picks for lines of this length)
         a.stride = tt::sino_warp_stride(n, 2);

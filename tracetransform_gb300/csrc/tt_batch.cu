@@ -500,8 +500,9 @@ int BatchEngine::autotune(cudaStream_t st) {
     }
     if (pinned_) {
         const bool sel = sargs_.need & ((1u << 6) | (1u << 7));
-        if (pin_.lpw && sel)
-            return berr(TT_ERR_UNSUPPORTED, "lines-per-warp tiles compute T0-T5 only");
+        if (pin_.lpw && (sel || sargs_.n_t > kWarpMaxOutputs))
+            return berr(TT_ERR_UNSUPPORTED, "lines-per-warp tiles compute T0-T5, at most 8 "
+                                            "sinograms per image");
         tune_ = pin_;
         return set_tile(tune_, st);
     }
@@ -537,7 +538,7 @@ int BatchEngine::autotune(cudaStream_t st) {
         t.lpw = 0;
         shapes.push_back(t);
     }
-    if (!sel)
+    if (!sel && sargs_.n_t <= kWarpMaxOutputs)
         for (int lpw : {1, 2, 4}) {
             Tune t;
             t.lines = lpw * sino_warp_cta_warps();

@@ -13,6 +13,10 @@ namespace tt {
 
 constexpr int kMaxT = 16; // T-functional entries per call
 constexpr int kMaxP = 16; // P-functional entries per call
+// Sinograms per line the warp-autonomous kernels write (one lane each; at
+// most 4 lines per warp, so a line has 8 lanes or more): calls with more
+// T-functional entries take the CTA kernels.
+constexpr int kWarpMaxOutputs = 8;
 
 // Fused rotate + T-functional sweep over one image.
 struct SinoArgs {

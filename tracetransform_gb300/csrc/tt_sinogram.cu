@@ -47,14 +47,14 @@ __device__ __forceinline__ void line_support(float X, float c, float s, float o,
     float jl = 0.f, jh = (float)(n - 1);
     const float bx = X * c + o, by = -X * s + o;
     if (fabsf(s) > 1e-7f) {
-        float a0 = o + (xlo - bx) / s, a1 = o + (xhi - bx) / s;
+        float a0 = o + __fdividef(xlo - bx, s), a1 = o + __fdividef(xhi - bx, s);
         jl = fmaxf(jl, fminf(a0, a1));
         jh = fminf(jh, fmaxf(a0, a1));
     } else if (bx < xlo || bx > xhi) {
         jh = -1.f;
     }
     if (fabsf(c) > 1e-7f) {
-        float a0 = o + (ylo - by) / c, a1 = o + (yhi - by) / c;
+        float a0 = o + __fdividef(ylo - by, c), a1 = o + __fdividef(yhi - by, c);
         jl = fmaxf(jl, fminf(a0, a1));
         jh = fminf(jh, fmaxf(a0, a1));
     } else if (by < ylo || by > yhi) {
@@ -521,6 +521,79 @@ __device__ int seg_find_crossing(const float *x, int C, float inc, float exc, fl
     return found;
 }
 
+// Both crossings of a segment's line at once: the plain values' (total
+// tot1, chunk prefix sums inc1 / exc1) and their square roots' (tot2, inc2 /
+// exc2); the same result as two seg_find_crossing calls, in one loop.
+template <int SW>
+__device__ void seg_find_crossing2(const float *x, int C, float inc1, float exc1, float tot1,
+                                   float inc2, float exc2, float tot2, int s, int sub, int &f1,
+                                   int &f2) {
+    const unsigned b1 = seg_ballot<SW>(2.f * inc1 >= tot1, s);
+    const unsigned b2 = seg_ballot<SW>(2.f * inc2 >= tot2, s);
+    int ln1 = b1 ? __ffs(b1) - 1 : SW, ln2 = b2 ? __ffs(b2) - 1 : SW;
+    f1 = INT_MAX;
+    f2 = INT_MAX;
+    bool a1 = ln1 < SW, a2 = ln2 < SW;
+    while (__any_sync(TT_FULL_MASK, a1 || a2)) {
+        float base1 = __shfl_sync(TT_FULL_MASK, exc1, s * SW + min(ln1, SW - 1));
+        float base2 = __shfl_sync(TT_FULL_MASK, exc2, s * SW + min(ln2, SW - 1));
+        for (int t0 = 0; t0 < C; t0 += SW) {
+            const int t = t0 + sub;
+            const bool in1 = a1 && t < C, in2 = a2 && t < C;
+            const float v1 = in1 ? x[ln1 * C + t] : 0.f;
+            const float v2 = in2 ? sqrt_nn(x[ln2 * C + t]) : 0.f;
+            const float p1 = seg_incl_scan<SW>(v1, sub) + base1;
+            const float p2 = seg_incl_scan<SW>(v2, sub) + base2;
+            const unsigned c1 = seg_ballot<SW>(in1 && 2.f * p1 >= tot1, s);
+            const unsigned c2 = seg_ballot<SW>(in2 && 2.f * p2 >= tot2, s);
+            if (a1 && c1) {
+                f1 = ln1 * C + t0 + __ffs(c1) - 1;
+                a1 = false;
+            }
+            if (a2 && c2) {
+                f2 = ln2 * C + t0 + __ffs(c2) - 1;
+                a2 = false;
+            }
+            base1 = __shfl_sync(TT_FULL_MASK, p1, s * SW + SW - 1);
+            base2 = __shfl_sync(TT_FULL_MASK, p2, s * SW + SW - 1);
+        }
+        if (a1 && ++ln1 >= SW)
+            a1 = false;
+        if (a2 && ++ln2 >= SW)
+            a2 = false;
+    }
+}
+
+// Eight sums over a segment of SW >= 8 lanes, transposed: three halving
+// exchanges (each lane keeps the half of the values its offset bit selects
+// and adds its partner's copy of it), then plain butterflies over the rest;
+// lane sub ends with sum k = (sub / (SW / 8)) % 8 of (a0, ..., a7).
+template <int SW>
+__device__ __forceinline__ float seg_sum8(float a0, float a1, float a2, float a3, float a4,
+                                          float a5, float a6, float a7, int sub) {
+    static_assert(SW >= 8, "eight sums need eight lanes");
+    constexpr int d1 = SW / 2, d2 = SW / 4, d3 = SW / 8;
+    bool hi = sub & d1; // keep a4..a7
+    float k0 = hi ? a4 : a0, k1 = hi ? a5 : a1, k2 = hi ? a6 : a2, k3 = hi ? a7 : a3;
+    const float s0 = hi ? a0 : a4, s1 = hi ? a1 : a5, s2 = hi ? a2 : a6, s3 = hi ? a3 : a7;
+    k0 += __shfl_xor_sync(TT_FULL_MASK, s0, d1);
+    k1 += __shfl_xor_sync(TT_FULL_MASK, s1, d1);
+    k2 += __shfl_xor_sync(TT_FULL_MASK, s2, d1);
+    k3 += __shfl_xor_sync(TT_FULL_MASK, s3, d1);
+    hi = sub & d2; // keep k2, k3
+    float m0 = hi ? k2 : k0, m1 = hi ? k3 : k1;
+    const float t0 = hi ? k0 : k2, t1 = hi ? k1 : k3;
+    m0 += __shfl_xor_sync(TT_FULL_MASK, t0, d2);
+    m1 += __shfl_xor_sync(TT_FULL_MASK, t1, d2);
+    hi = sub & d3; // keep m1
+    float r = hi ? m1 : m0;
+    r += __shfl_xor_sync(TT_FULL_MASK, hi ? m0 : m1, d3);
+#pragma unroll
+    for (int d = d3 / 2; d > 0; d >>= 1)
+        r += __shfl_xor_sync(TT_FULL_MASK, r, d);
+    return r;
+}
+
 // find_crossing_walk per segment (values of any sign).
 template <int SW>
 __device__ int seg_walk(const float *x, int C, float exc, float total, int sub) {
@@ -650,33 +723,36 @@ __device__ void warp_lines(const BlockJob &J, unsigned long long tf_code, int n_
     }
     const bool any_neg = __any_sync(TT_FULL_MASK, neg);
     int m1 = 0, m2 = 0;
-    if (need_m1) {
-        const int f = any_neg ? seg_walk<SW>(x, C, exc, S, sub)
-                              : seg_find_crossing<false, SW>(x, C, inc, exc, S, s, sub);
-        m1 = resolve_median(f, S, jlo, jhi, len, n);
+    if (need_m1 && need_m2 && !any_neg) {
+        int f1, f2;
+        seg_find_crossing2<SW>(x, C, inc, exc, S, incq, excq, Q, s, sub, f1, f2);
+        m1 = resolve_median(f1, S, jlo, jhi, len, n);
+        m2 = resolve_median(f2, Q, jlo, jhi, len, n);
+    } else {
+        if (need_m1) {
+            const int f = any_neg ? seg_walk<SW>(x, C, exc, S, sub)
+                                  : seg_find_crossing<false, SW>(x, C, inc, exc, S, s, sub);
+            m1 = resolve_median(f, S, jlo, jhi, len, n);
+        }
+        if (need_m2)
+            m2 = resolve_median(seg_find_crossing<true, SW>(x, C, incq, excq, Q, s, sub), Q, jlo,
+                                jhi, len, n);
     }
-    if (need_m2)
-        m2 = resolve_median(seg_find_crossing<true, SW>(x, C, incq, excq, Q, s, sub), Q, jlo,
-                            jhi, len, n);
 
-    float r1v = 0.f, r2v = 0.f;
+    float t1 = 0.f, t2 = 0.f;
     if (need_m1) {
-        float t1 = 0.f, t2 = 0.f;
-        for (int j = max(m1, jlo) + sub; j < jhi; j += SW) {
-            const float v = x[j - jlo];
-            const float r = (float)(j - m1);
-            const float vr = v * r;
+        int j = max(m1, jlo) + sub;
+        float r = (float)(j - m1); // exact: integers below 2^24
+        for (; j < jhi; j += SW, r += (float)SW) {
+            const float vr = x[j - jlo] * r;
             t1 += vr;
             t2 = fmaf(vr, r, t2);
         }
-        r1v = seg_sum<SW>(t1);
-        r2v = seg_sum<SW>(t2);
     }
-    float r345[3] = {0.f, 0.f, 0.f};
+    float re3 = 0.f, im3 = 0.f, re4 = 0.f, im4 = 0.f, re5 = 0.f, im5 = 0.f;
     if (need_m2) {
         const bool w3 = need & (1u << 3), w4 = need & (1u << 4), w5 = need & (1u << 5);
         const float2 *tab3 = J.tab, *tab4 = J.tab + n, *tab5 = J.tab + 2 * n;
-        float re3 = 0.f, im3 = 0.f, re4 = 0.f, im4 = 0.f, re5 = 0.f, im5 = 0.f;
         const int qlo = max(1, jlo - m2), qhi = min(n - m2, jhi - m2);
         for (int q = qlo + sub; q < qhi; q += SW) {
             const float v = x[m2 + q - jlo];
@@ -696,27 +772,29 @@ __device__ void warp_lines(const BlockJob &J, unsigned long long tf_code, int n_
                 im5 = fmaf(w.y, v, im5);
             }
         }
-        if (w3)
-            r345[0] = hypotf(seg_sum<SW>(re3), seg_sum<SW>(im3));
-        if (w4)
-            r345[1] = hypotf(seg_sum<SW>(re4), seg_sum<SW>(im4));
-        if (w5)
-            r345[2] = hypotf(seg_sum<SW>(re5), seg_sum<SW>(im5));
     }
 
-    // 4. lane t of a segment writes its line's output t (every lane of the
-    // segment holds the line's sums and medians)
-    if (colok) {
-        const size_t plane = J.plane;
-        const size_t at = (size_t)angle * n + col;
-        for (int t = sub; t < n_t; t += SW) {
-            const int f = (int)((tf_code >> (3 * t)) & 7ull);
-            const float v = f == 0 ? S : f == 1 ? r1v : f == 2 ? r2v
-                          : f == 3 ? r345[0] : f == 4 ? r345[1] : r345[2];
-            J.out[t * plane + at] = v;
-            if (J.medians)
-                J.medians[t * plane + at] = f == 0 ? -1 : f <= 2 ? m1 : m2;
-        }
+    // 4. the eight sums of a segment reduced transposed: after the halving
+    // exchanges lane (s, sub) holds sum k = (sub / (SW / 8)) % 8 of
+    // (t1, t2, re3, im3, re4, im4, re5, im5), the moduli |re + i im| are
+    // taken once per lane, and lane t writes output t (T0's sum S and the
+    // medians are held by every lane of the segment)
+    const float v8 = seg_sum8<SW>(t1, t2, re3, im3, re4, im4, re5, im5, sub);
+    constexpr int unit = SW / 8;
+    const int k8 = (sub / unit) & 7;
+    const float other = __shfl_xor_sync(TT_FULL_MASK, v8, unit);
+    const float res = k8 >= 2 ? hypotf(k8 & 1 ? other : v8, k8 & 1 ? v8 : other) : v8;
+    // n_t <= kWarpMaxOutputs <= SW (the hosts' choice of this path)
+    const size_t plane = J.plane;
+    const size_t at = (size_t)angle * n + col;
+    const int t = sub < n_t ? sub : 0;
+    const int f = (int)((tf_code >> (3 * t)) & 7ull);
+    const int kf = f == 1 ? 0 : f == 2 ? 1 : f == 3 ? 2 : f == 4 ? 4 : 6;
+    const float got = __shfl_sync(TT_FULL_MASK, res, s * SW + kf * unit);
+    if (colok && sub < n_t) {
+        J.out[t * plane + at] = f == 0 ? S : got;
+        if (J.medians)
+            J.medians[t * plane + at] = f == 0 ? -1 : f <= 2 ? m1 : m2;
     }
 }
 
