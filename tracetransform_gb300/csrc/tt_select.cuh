@@ -312,27 +312,27 @@ inline __device__ void select_t67(float *x, int jlo, int jhi, int m1, int m2, bo
     }
     __syncwarp();
     unsigned l6 = 0, l7 = 0, l7max = 0;
-    for (int jb = j0; jb < j1; jb += 4) {
+    // a warp-uniform trip count (per), lanes past their chunk predicated off
+    for (int i0 = 0; i0 < per; i0 += 4) {
         float vb[4]; // four loads in flight before the atomics
 #pragma unroll
-        for (int u = 0; u < 4; u++)
-            vb[u] = jb + u < j1 ? x[jb + u - jlo] : 0.f;
+        for (int u = 0; u < 4; u++) {
+            const int j = j0 + i0 + u;
+            vb[u] = j < j1 ? x[j - jlo] : 0.f;
+        }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const int j = jb + u;
-            if (j >= j1)
-                break;
+            const int j = j0 + i0 + u;
             const float v = vb[u];
             const unsigned wq = __float2uint_rn(sqrt_nn(v) * qs);
-            if (want7 && j >= b7) {
-                l7 += wq;
-                l7max += v == xmax ? wq : 0u;
+            const bool in7 = want7 && j >= b7 && j < j1, in6 = want6 && j >= b6 && j < j1;
+            l7 += in7 ? wq : 0u;
+            l7max += in7 && v == xmax ? wq : 0u;
+            l6 += in6 ? wq : 0u;
+            if (in7)
                 atomicAdd(s7->hist + sel_bin(v, 0.f, bs7), wq);
-            }
-            if (want6 && j >= b6) {
-                l6 += wq;
+            if (in6)
                 atomicAdd(s6->hist + sel_bin(key6(j, v), 0.f, bs6), wq);
-            }
         }
     }
     const unsigned long long W7 = __reduce_add_sync(TT_FULL_MASK, l7);

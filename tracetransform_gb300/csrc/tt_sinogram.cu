@@ -241,6 +241,7 @@ __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long
 
     float tot = 0.f, totq = 0.f, lmax = 0.f;
     bool neg = false;
+#pragma unroll 4
     for (int k = 0; k < C; k++) {
         const float v = x[base + k];
         tot += v;
@@ -277,6 +278,7 @@ __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long
     float r1v = 0.f, r2v = 0.f;
     if (need & ((1u << 1) | (1u << 2))) {
         float t1 = 0.f, t2 = 0.f;
+#pragma unroll 4
         for (int j = max(m1, jlo) + lane; j < jhi; j += 32) {
             const float v = x[j - jlo];
             const float r = (float)(j - m1);
@@ -294,6 +296,7 @@ __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long
         const float2 *tab3 = J.tab, *tab4 = J.tab + n, *tab5 = J.tab + 2 * n;
         float re3 = 0.f, im3 = 0.f, re4 = 0.f, im4 = 0.f, re5 = 0.f, im5 = 0.f;
         const int lo = max(1, jlo - m2), hi = min(n - m2, jhi - m2);
+#pragma unroll 4
         for (int q = lo + lane; q < hi; q += 32) {
             const float v = x[m2 + q - jlo];
             if (w3) {
