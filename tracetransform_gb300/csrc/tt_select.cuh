@@ -237,10 +237,11 @@ __device__ float sel_refine(const float *x, int jlo, int j0, int j1, int per, Ke
         for (int i = lane; i < kSelBins; i += 32)
             sc->hist[i] = 0u;
         __syncwarp();
-        for (int j = j0; j < j1; j++) {
-            const float v = x[j - jlo];
+        for (int i = 0; i < per; i++) { // warp-uniform trip count
+            const int j = j0 + i;
+            const float v = j < j1 ? x[j - jlo] : 0.f;
             const float k = keyfn(j, v);
-            if (k >= klo && k <= khi)
+            if (j < j1 && k >= klo && k <= khi)
                 atomicAdd(sc->hist + sel_bin(k, klo, bs), wfn(v));
         }
         __syncwarp();
@@ -250,19 +251,12 @@ __device__ float sel_refine(const float *x, int jlo, int j0, int j1, int per, Ke
         float bmin = __int_as_float(0x7f800000), bmax = 0.f;
         for (int i = 0; i < per; i++) {
             const int j = j0 + i;
-            bool in = false;
-            float k = 0.f;
-            unsigned wq = 0;
-            if (j < j1) {
-                const float v = x[j - jlo];
-                k = keyfn(j, v);
-                if (k >= klo && k <= khi && sel_bin(k, klo, bs) == d) {
-                    in = true;
-                    wq = wfn(v);
-                    bmin = fminf(bmin, k);
-                    bmax = fmaxf(bmax, k);
-                }
-            }
+            const float v = j < j1 ? x[j - jlo] : 0.f;
+            const float k = keyfn(j, v);
+            const bool in = j < j1 && k >= klo && k <= khi && sel_bin(k, klo, bs) == d;
+            const unsigned wq = in ? wfn(v) : 0u;
+            bmin = in ? fminf(bmin, k) : bmin;
+            bmax = in ? fmaxf(bmax, k) : bmax;
             sel_append(sc, &count, in, k, wq, lane);
         }
         bmin = __int_as_float(warp_min(__float_as_int(bmin)));
@@ -356,19 +350,12 @@ inline __device__ void select_t67(float *x, int jlo, int jhi, int m1, int m2, bo
         float mn = __int_as_float(0x7f800000), mx = 0.f;
         for (int i = 0; i < per; i++) {
             const int j = j0 + i;
-            bool in = false;
-            float k = 0.f;
-            unsigned wq = 0;
-            if (j < j1) {
-                const float v = x[j - jlo];
-                k = key6(j, v);
-                if (j >= b6 && sel_bin(k, 0.f, bs6) == d) {
-                    in = true;
-                    wq = __float2uint_rn(sqrt_nn(v) * qs);
-                    mn = fminf(mn, k);
-                    mx = fmaxf(mx, k);
-                }
-            }
+            const float v = j < j1 ? x[j - jlo] : 0.f;
+            const float k = key6(j, v);
+            const bool in = j < j1 && j >= b6 && sel_bin(k, 0.f, bs6) == d;
+            const unsigned wq = in ? __float2uint_rn(sqrt_nn(v) * qs) : 0u;
+            mn = in ? fminf(mn, k) : mn;
+            mx = in ? fmaxf(mx, k) : mx;
             sel_append(s6, &c, in, k, wq, lane);
         }
         mn = __int_as_float(warp_min(__float_as_int(mn)));
@@ -429,11 +416,21 @@ inline __device__ float select_p2(const float *x, int n, float xmax, float xsum,
         sc->hist[i] = 0u;
     __syncwarp();
     unsigned lw = 0;
-    for (int j = j0; j < j1; j++) {
-        const float v = x[j];
-        const unsigned wq = wfn(v);
-        lw += wq;
-        atomicAdd(sc->hist + sel_bin(v, 0.f, bs), wq);
+    for (int i0 = 0; i0 < per; i0 += 4) { // warp-uniform trip count
+        float vb[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int j = j0 + i0 + u;
+            vb[u] = j < j1 ? x[j] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const bool in = j0 + i0 + u < j1;
+            const unsigned wq = wfn(vb[u]);
+            lw += in ? wq : 0u;
+            if (in)
+                atomicAdd(sc->hist + sel_bin(vb[u], 0.f, bs), wq);
+        }
     }
     const unsigned long long W = __reduce_add_sync(TT_FULL_MASK, lw);
     __syncwarp();
@@ -444,18 +441,11 @@ inline __device__ float select_p2(const float *x, int n, float xmax, float xsum,
     float mn = __int_as_float(0x7f800000), mx = 0.f;
     for (int i = 0; i < per; i++) {
         const int j = j0 + i;
-        bool in = false;
-        float k = 0.f;
-        unsigned wq = 0;
-        if (j < j1) {
-            k = x[j];
-            if (sel_bin(k, 0.f, bs) == d) {
-                in = true;
-                wq = wfn(k);
-                mn = fminf(mn, k);
-                mx = fmaxf(mx, k);
-            }
-        }
+        const float k = j < j1 ? x[j] : 0.f;
+        const bool in = j < j1 && sel_bin(k, 0.f, bs) == d;
+        const unsigned wq = in ? wfn(k) : 0u;
+        mn = in ? fminf(mn, k) : mn;
+        mx = in ? fmaxf(mx, k) : mx;
         sel_append(sc, &c, in, k, wq, lane);
     }
     mn = __int_as_float(warp_min(__float_as_int(mn)));
