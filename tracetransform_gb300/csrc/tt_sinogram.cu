@@ -142,9 +142,10 @@ struct BlockJob {
 };
 
 // The fused body: support, sampling, T-functionals of one BlockJob.  Every
-// thread of the CTA calls it; it synchronises the CTA but never returns early.
-// tf_code holds the T-functional id of output t in bits [3t, 3t + 3).
-template <int L, bool kSel, bool kInterior>
+// thread of the CTA (W >= L warps) calls it; it synchronises the CTA but
+// never returns early.  All W warps sample; warps 0..L-1 then take one line
+// each.  tf_code holds the T-functional id of output t in bits [3t, 3t + 3).
+template <int L, bool kSel, bool kInterior, int W = L>
 __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long tf_code,
                                            int n_t, unsigned need, int stride, float *sm,
                                            int *s_range) {
@@ -183,25 +184,25 @@ __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long
     const int C = max((len + 31) >> 5, 1) | 1; // odd: conflict-free chunks
 
 
-    // 2. Sample the lines into shared memory (zeros past len).
+    // 2. Sample the lines into shared memory (zeros past len, rows < 32 C).
     {
-        constexpr int RPW = 32 / L;
-        const int l = lane % L, r = lane / L;
+        constexpr int RS = 32 * W / L; // row streams per line
+        const int l = lane % L, r = (warp * 32 + lane) / L;
         const int col = col0 + l;
         const bool colok = col < n;
         const float X = (float)col - o;
         const float Xc = __fmul_rn(X, c), Xms = __fmul_rn(X, -s);
         const float tu = J.tu, tv = J.tv;
         float *dst = sm + l * stride;
-        const int first = warp * RPW + r; // this thread's rows: first + 32 i, i < C
-        constexpr int U = 4;              // gathers in flight per thread
-        for (int i0 = 0; i0 < C; i0 += U) {
+        const int rows = 32 * C, iters = (rows + RS - 1) / RS; // this thread: r + RS i
+        constexpr int U = 4;                                   // gathers in flight per thread
+        for (int i0 = 0; i0 < iters; i0 += U) {
             float4 g[U];
             float xf[U], yf[U];
             bool ok[U];
 #pragma unroll
             for (int u = 0; u < U; u++) {
-                const int jr = first + 32 * (i0 + u);
+                const int jr = r + RS * (i0 + u);
                 const float Y = (float)(jlo + jr) - o;
                 // (x c + y s) + o and (x (-s) + y c) + o, each operation rounded
                 const float qx = __fadd_rn(__fadd_rn(Xc, __fmul_rn(Y, s)), o);
@@ -223,8 +224,9 @@ __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long
                 const float t2 = __fmul_rn(__fmul_rn(g[u].z, omx), yf[u]);
                 const float t3 = __fmul_rn(__fmul_rn(g[u].y, xf[u]), yf[u]);
                 const float v = __fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), t3);
-                if (i0 + u < C)
-                    dst[first + 32 * (i0 + u)] = ok[u] ? v : 0.f;
+                const int jr = r + RS * (i0 + u);
+                if (jr < rows)
+                    dst[jr] = ok[u] ? v : 0.f;
             }
         }
     }
@@ -232,7 +234,7 @@ __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long
 
     // 3. One warp per line: T-functionals.
     const int col = col0 + warp;
-    if (col < n) {
+    if (warp < L && col < n) {
     float *x = sm + warp * stride;
     const bool need_m1 = need & ((1u << 1) | (1u << 2) | (1u << 7));
     const bool need_m2 = need & ((1u << 3) | (1u << 4) | (1u << 5) | (1u << 6));
@@ -359,8 +361,8 @@ __device__ __forceinline__ void sino_block(const BlockJob &J, unsigned long long
     } // col < n
 }
 
-template <int L, bool kSel, bool kInterior>
-__global__ void __launch_bounds__(32 * L)
+template <int L, bool kSel, bool kInterior, int W = L>
+__global__ void __launch_bounds__(32 * W, W > L ? 2 : 1)
     sino_kernel(const SinoArgs a) {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ int s_range[2];
@@ -401,8 +403,8 @@ __global__ void __launch_bounds__(32 * L)
     unsigned long long code = 0;
     for (int t = 0; t < a.n_t; t++)
         code |= (unsigned long long)(a.tf[t] & 7) << (3 * t);
-    sino_block<L, kSel, kInterior>(J, code, a.n_t, a.need, a.stride,
-                                   reinterpret_cast<float *>(smraw), s_range);
+    sino_block<L, kSel, kInterior, W>(J, code, a.n_t, a.need, a.stride,
+                                      reinterpret_cast<float *>(smraw), s_range);
 }
 
 // Persistent kernel over a batch of images of different sizes and angle
@@ -1000,8 +1002,11 @@ __global__ void bbox_finish(int *r) {
 
 template <int L, bool kSel>
 cudaError_t launch_one(const SinoArgs &a, size_t smem, cudaStream_t stream) {
-    const void *k = a.interior ? (const void *)sino_kernel<L, kSel, true>
-                               : (const void *)sino_kernel<L, kSel, false>;
+    // 4 lines per CTA (long lines: 2 CTAs per SM by shared memory) are
+    // sampled by 16 warps, so that more gathers are in flight per SM
+    constexpr int W = L == 4 ? 16 : L;
+    const void *k = a.interior ? (const void *)sino_kernel<L, kSel, true, W>
+                               : (const void *)sino_kernel<L, kSel, false, W>;
     const size_t limit = opt_in_smem(k);
     if (limit == 0)
         return cudaErrorInvalidValue;
@@ -1009,7 +1014,7 @@ cudaError_t launch_one(const SinoArgs &a, size_t smem, cudaStream_t stream) {
         return cudaErrorInvalidValue;
     dim3 grid((a.n + L - 1) / L, a.n_angles);
     void *args[] = {(void *)&a};
-    return cudaLaunchKernel(k, grid, dim3(32 * L), args, smem, stream);
+    return cudaLaunchKernel(k, grid, dim3(32 * W), args, smem, stream);
 }
 
 } // namespace
