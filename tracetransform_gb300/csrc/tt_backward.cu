@@ -398,6 +398,7 @@ adjoint_gather_kernel(int rows, int cols, int row_off, int col_off, int n, int n
     const long long i = (long long)blockIdx.x * 32 + lane;
     params += (size_t)blockIdx.y * 4 * (size_t)n * n_angles;
     T acc = 0;
+    const unsigned live = __ballot_sync(TT_FULL_MASK, i < pix);
     if (i < pix) {
         const int r = (int)(i % rows), c = (int)(i / rows);
         const T fpx = (T)(c + col_off), fpy = (T)(r + row_off);
@@ -416,6 +417,31 @@ adjoint_gather_kernel(int rows, int cols, int row_off, int col_off, int n, int n
                 yc[u] = C::mul(Y, ca);
             }
             const T *pa = params + (size_t)4 * a * n;
+            // every lane's 3 x 3 block inside the lattice (all but the frame's
+            // corners): no per-candidate index checks
+            const bool inner = (unsigned)(c0 - 1) < (unsigned)(n - 2) &&
+                               (unsigned)(j0 - 1) < (unsigned)(n - 2);
+            if (kInterior && __all_sync(live, inner)) {
+#pragma unroll
+                for (int v = 0; v < 3; v++) {
+                    const int cc = c0 - 1 + v;
+                    T g0, g1, g2, mf;
+                    Quad<T>::load(pa + 4 * cc, g0, g1, g2, mf);
+                    const T X = (T)cc - o;
+                    const T xc = C::mul(X, ca), xs = C::mul(X, -sa);
+#pragma unroll
+                    for (int u = 0; u < 3; u++) {
+                        const T qx = C::add(C::add(xc, ys[u]), o);
+                        const T qy = C::add(C::add(xs, yc[u]), o);
+                        const T wx = fmax((T)1 - fabs(qx - fpx), (T)0);
+                        const T wy = fmax((T)1 - fabs(qy - fpy), (T)0);
+                        const T rr = (T)(j0 - 1 + u) - mf;
+                        const T g = rr >= (T)0 ? g0 + rr * (g1 + rr * g2) : g0;
+                        acc += wx * wy * g;
+                    }
+                }
+                continue;
+            }
 #pragma unroll
             for (int v = 0; v < 3; v++) {
                 const int cc = c0 - 1 + v;
