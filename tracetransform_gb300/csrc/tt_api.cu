@@ -159,6 +159,7 @@ struct tt_plan {
     // P-stage scratch: P3 partial sums, the exact-sort list of P2 (count + entries)
     DevBuf cpart, cfb;
     std::map<int, std::pair<float2 *, float *>> p3dft; // n -> twiddles, trapz weights
+    std::map<int, float *> p3tc;                        // n -> tensor-core twiddle blocks
     int sms = 0;
     // nearest orthonormal sinogram scratch (double matrices, V, norms, ...)
     DevBuf nos_a, nos_work, nos_desc, nos_off;
@@ -470,6 +471,20 @@ struct tt_plan {
         return TT_OK;
     }
 
+    // The tensor-core P3's twiddle blocks of n (built once from the twiddles).
+    tt_status get_p3tc(int n, const float2 *tw, const float **out) {
+        auto it = p3tc.find(n);
+        if (it == p3tc.end()) {
+            float *d;
+            TT_CHECK(alloc((void **)&d, sizeof(float) * tt::p3_tc_table_floats(n)));
+            TT_CUDA(tt::launch_p3_tc_tables(n, tw, d, stream));
+            TT_CUDA(cudaStreamSynchronize(stream));
+            it = p3tc.emplace(n, d).first;
+        }
+        *out = it->second;
+        return TT_OK;
+    }
+
     tt_status get_herm(int n, int order, int center, const float **out) {
         auto key = std::make_tuple(n, order, center);
         auto it = herm.find(key);
@@ -656,8 +671,11 @@ tt_status run_circus_stacks(tt_plan *p, const float *d_sino, int rows, int cols,
     S.angles = cols;
     S.cols = cols * n_sino;
     S.mtiles = (need & (1u << 3)) ? tt::p3_freq_tiles(rows) : 0;
-    if (need & (1u << 3))
+    if (need & (1u << 3)) {
         TT_CHECK(p->get_p3dft(rows, &S.tw, &S.ck));
+        TT_CHECK(p->get_p3tc(rows, S.tw, &S.wtc));
+        a.tc_tables = 1;
+    }
     const size_t part = (size_t)S.mtiles * S.cols;
     TT_CHECK(p->ensure(p->cpart, sizeof(float) * std::max<size_t>(part, 1)));
     TT_CHECK(p->ensure(p->cfb, sizeof(int2) * ((size_t)S.cols + 1)));

@@ -211,7 +211,7 @@ class BatchEngine {
     DevArray<BatchImage> img_;
     DevArray<CircusStack> stacks_;
     DevArray<float2> trig_, tab_, p3tw_;
-    DevArray<float> p3ck_, sino_, circ_, sig_, part_;
+    DevArray<float> p3ck_, p3tc_, sino_, circ_, sig_, part_;
     DevArray<int2> fb_;
     DevArray<unsigned> counter_;
     DevArray<long long> voff_;
@@ -397,6 +397,17 @@ int BatchEngine::build(cudaStream_t st) {
     for (const auto &kv : p3_at)
         B_CUDA(launch_p3_dft_tables(kv.first, p3tw_.p + kv.second.first,
                                     p3ck_.p + kv.second.second, st));
+    // the tensor-core P3's twiddle blocks, one set per distinct n
+    std::map<int, size_t> p3tc_at;
+    size_t p3tc_total = 0;
+    for (const auto &kv : p3_at) {
+        p3tc_at[kv.first] = p3tc_total;
+        p3tc_total += p3_tc_table_floats(kv.first);
+    }
+    B_CHECK(p3tc_.resize(std::max<size_t>(p3tc_total, 1)));
+    for (const auto &kv : p3_at)
+        B_CUDA(launch_p3_tc_tables(kv.first, p3tw_.p + kv.second.first,
+                                   p3tc_.p + p3tc_at[kv.first], st));
     B_CUDA(cudaStreamSynchronize(st));
     B_CHECK(sino_.resize((size_t)std::max<long long>(sino_total, 1)));
     B_CHECK(circ_.resize(std::max<size_t>(out_floats_, 1)));
@@ -413,6 +424,7 @@ int BatchEngine::build(cudaStream_t st) {
         part_at += (long long)c.mtiles * c.cols;
         c.tw = p3 ? p3tw_.p + p3_at[n_[i]].first : nullptr;
         c.ck = p3 ? p3ck_.p + p3_at[n_[i]].second : nullptr;
+        c.wtc = p3 ? p3tc_.p + p3tc_at[n_[i]] : nullptr;
     }
     B_CHECK(stacks_.upload(stacks, st));
     // z-score vectors: n_t x n_p per image, length = its angle count
@@ -467,6 +479,7 @@ int BatchEngine::build(cudaStream_t st) {
     for (int p = 0; p < n_p; p++)
         cargs_.kind[p] = shape_.pk[p];
     cargs_.need = pneed;
+    cargs_.tc_tables = 1;
     cargs_.stride = circus_warp_stride(n_max_);
     cargs_.fb_count = reinterpret_cast<unsigned *>(fb_.p);
     cargs_.fb_list = fb_.p + 1;

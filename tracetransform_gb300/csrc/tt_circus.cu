@@ -3,10 +3,12 @@
 //
 // P1-P3 over stacks of sinogram columns (every call without Hermite, and
 // the batched engine), three launches:
-//   p3_dft_kernel      P3: the real DFT of every column as a GEMM-shaped
-//                      direct sum F = W^T X with |F_k / N|^4 and the trapz
-//                      weights folded into the epilogue (partial sums per
-//                      64-frequency tile, added in tile order: deterministic)
+//   p3_dft_tc_kernel   P3: the real DFT of every column as a GEMM on the
+//                      tensor cores (tcgen05, TF32 split in three products,
+//                      the accumulator in tensor memory), F = W^T X with
+//                      |F_k / N|^4 and the trapz weights folded into the
+//                      epilogue (partial sums per 64-frequency tile, added in
+//                      tile order: deterministic)
 //   circus_p12_kernel  one warp per column: P1 = sum |x[p] - x[p-1]|, P2 = the
 //                      weighted median of the column weighted by itself by
 //                      selection (tt_select.cuh, no sort), P3's tile sums
@@ -244,16 +246,12 @@ __global__ void zscore_kernel(const float *__restrict__ in, int len,
 // cols), F = W^T X with W[p][2k] = cos(2 pi k p / n), W[p][2k+1] =
 // -sin(2 pi k p / n), k <= n/2; the epilogue folds |F_k / n|^4 and the trapz
 // weights ck[k] into one partial sum per (64-frequency tile, column), which
-// the per-column kernel adds in tile order (deterministic).  A CTA computes a
-// 128 x 128 tile of F (64 frequencies as re/im rows x 128 columns) with an
-// 8 x 8 register tile per thread, samples staged 16 at a time through shared
-// memory (next step's global loads in flight during the current step's
-// FMAs); W is generated from the n-entry twiddle table with an incremental
-// (k p) mod n index.  The O(n^2) DFT replaces the Bluestein FFT's two
-// power-of-two transforms in shared memory: at these lengths the FMA pipe
-// runs it faster than the FFT's barrier-bound butterflies, and its float
-// error (accumulated over n terms) stays far inside the 1e-4 tolerance.
-constexpr int kDftBM = 128, kDftBN = 128, kDftBK = 16, kFreqTile = kDftBM / 2;
+// the per-column kernel adds in tile order (deterministic).  W is generated
+// from the n-entry twiddle table with an incremental (k p) mod n index.  The
+// O(n^2) DFT replaces the Bluestein FFT's two power-of-two transforms in
+// shared memory: as a GEMM it runs on the tensor cores, and its error
+// (accumulated in FP32 over n terms) stays far inside the 1e-4 tolerance.
+constexpr int kFreqTile = 64; // frequencies per partial sum
 
 __device__ __forceinline__ const CircusStack &stack_at(const CircusStackArgs &a, int i) {
     return a.st ? a.st[i] : a.one;
@@ -272,108 +270,321 @@ __device__ __forceinline__ int stack_of(const CircusStack *st, int n_st, int v, 
     return lo;
 }
 
-__global__ void __launch_bounds__(256, 2) p3_dft_kernel(const CircusStackArgs a) {
-    __shared__ __align__(16) float Ws[kDftBK][kDftBM];
-    __shared__ __align__(16) float Xs[kDftBK][kDftBN];
-    __shared__ float Red[16][kDftBN];
+// ---- P3 DFT on the tensor cores (tcgen05, kind::tf32, three products) -------
+//
+// Per CTA, F^T = X^T W^T for 128 sinogram columns (M: the accumulator's
+// tensor memory lanes) x one 64-frequency tile as (re, im) pairs (N <= 128
+// tensor memory columns), over the columns' n samples in stages of 32.  TF32
+// keeps 10 mantissa bits, so each operand is split x = hi + lo (hi rounded to
+// TF32, lo = x - hi exact in FP32) and F sums hi.hi + hi.lo + lo.hi: ~2^-21
+// relative per product.  The tensor cores' FP32 accumulation rounds at every
+// MMA, and that rounding, not the split, bounds the error: hi.hi goes to
+// three accumulators in turn (stage s to accumulator s mod 3) and the small
+// cross terms to a fourth, so that each accumulator takes a third of the
+// big products' roundings; the epilogue adds the four in FP32.  All 256
+// threads stage the operands into shared memory in the canonical K-major
+// layout without swizzle, one block per 8-sample MMA slice: core matrices of
+// 8 rows x 16 bytes (4 samples), the slice's second 4 samples 128 bytes on
+// (LBO), the next 8 rows 256 bytes on (SBO) -- every descriptor stays inside
+// its slice's block -- into two stage buffers, each released by the commit
+// of the MMAs that read it; one thread issues a stage's 12 MMAs (4 slices x
+// 3 products).  The twiddle operand depends only on (n, frequency tile,
+// stage): with kPre its hi / lo blocks come precomputed in that layout
+// (p3_tc_tables_kernel) and one bulk asynchronous copy per stage brings them
+// in, completing on an mbarrier, so that the threads only split and store
+// the sinogram operand; without (the allocation-free entry point) the
+// threads gather the twiddles from the n-entry table one stage ahead.  The epilogue: warps 0-3 read their 32 lanes' accumulator rows
+// (one sinogram column per thread) and fold ck |F/n|^4 into the tile's
+// partial sum.  Every wait is bounded: a barrier that never completes (which
+// the commit protocol rules out) makes the tile's partial sums NaN instead
+// of hanging the GPU.
+constexpr int kTcCols = 128, kTcKT = 32, kTcThreads = 256, kTcN = 2 * kFreqTile;
+constexpr int kTcAcc = 4; // accumulators of kTcN columns: hi.hi x 3, cross terms
+constexpr int kTcAFloats = kTcCols * kTcKT, kTcBFloats = kTcN * kTcKT;
+constexpr size_t kTcBufFloats = 2 * (size_t)kTcAFloats + 2 * (size_t)kTcBFloats;
+constexpr size_t kTcSmem = 2 * kTcBufFloats * sizeof(float); // 128 KB
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+// x rounded to TF32 (10 mantissa bits); infinities and NaN unchanged
+__device__ __forceinline__ float tf32_hi(float x) {
+    const unsigned u = __float_as_uint(x);
+    return __uint_as_float((u & 0x7f800000u) == 0x7f800000u ? u : (u + 0x1000u) & 0xffffe000u);
+}
+// Shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
+// offsets in 16-byte units, the descriptor version bit, no swizzle.
+__device__ __forceinline__ unsigned long long umma_desc(unsigned addr, unsigned lbo,
+                                                        unsigned sbo) {
+    return (unsigned long long)((addr & 0x3ffffu) >> 4) |
+           ((unsigned long long)((lbo >> 4) & 0x3fffu) << 16) |
+           ((unsigned long long)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ void umma_tf32(unsigned d, unsigned long long a, unsigned long long b,
+                                          unsigned idesc, unsigned accumulate) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+                 "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(unsigned ta, float (&o)[32]) {
+    unsigned v[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, "
+                 "%8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, "
+                 "%22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                   "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                   "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+                   "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                   "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]),
+                   "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                 : "r"(ta));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++)
+        o[i] = __uint_as_float(v[i]);
+}
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+    for (int it = 0; it < (1 << 22); it++) {
+        unsigned ok;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (ok)
+            return true;
+    }
+    return false;
+}
+
+// The precomputed twiddle operand of n: for each (64-frequency tile mt,
+// stage of 32 samples), a hi block then a lo block of 128 component rows x 32
+// samples in the layout the kernel stages (p3_tc_table_floats(n) floats).
+__global__ void p3_tc_tables_kernel(int n, const float2 *__restrict__ tw, float *__restrict__ out) {
+    const int K = n / 2 + 1, stages = (n + kTcKT - 1) / kTcKT;
+    const long long total = (long long)((K + kFreqTile - 1) / kFreqTile) * stages * kTcBFloats;
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= total)
+        return;
+    const int blk = (int)(e / kTcBFloats), w = (int)(e % kTcBFloats);
+    const int mt = blk / stages, st = blk % stages;
+    const int row = w / kTcKT, k = w % kTcKT;
+    const int f = mt * kFreqTile + (row >> 1), p = st * kTcKT + k;
+    float v = 0.f;
+    if (f < K && p < n) {
+        const float2 t = tw[(int)(((long long)f * p) % n)];
+        v = (row & 1) ? t.y : t.x;
+    }
+    const float hi = tf32_hi(v);
+    const int off = (k >> 3) * (kTcN * 8) + (row >> 3) * 64 + ((k >> 2) & 1) * 32 + (row & 7) * 4 + (k & 3);
+    float *b = out + (size_t)blk * 2 * kTcBFloats;
+    b[off] = hi;
+    b[kTcBFloats + off] = v - hi;
+}
+
+// grid: one CTA per (64-frequency tile, 128 columns) over the stacks
+template <bool kPre>
+__global__ void __launch_bounds__(kTcThreads, 1) p3_dft_tc_kernel(const CircusStackArgs a) {
+    extern __shared__ __align__(1024) float tsm[];
+    __shared__ __align__(8) unsigned long long s_bar[2];
+    __shared__ __align__(8) unsigned long long s_load[2];
+    __shared__ unsigned s_tmem;
     const int tile = blockIdx.x;
     const CircusStack &S = stack_at(a, stack_of(a.st, a.n_st, tile, true));
-    const int n = S.n, cols = S.cols, K = n / 2 + 1;
     const int local = tile - S.tile_begin;
     const int mt = local % S.mtiles, ct = local / S.mtiles;
-    const int k0 = mt * kFreqTile, c0 = ct * kDftBN;
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const float2 *tw = S.tw;
-    const float *x = S.sino;
-    // twiddles: frequency kk of the tile, samples pw .. pw + 3 of each step
-    const int kk = tid & 63, pw = (tid >> 6) * 4;
-    const int kg = k0 + kk;
-    const bool kval = kg < K;
-    float acc[8][8];
-#pragma unroll
-    for (int i = 0; i < 8; i++)
-#pragma unroll
-        for (int j = 0; j < 8; j++)
-            acc[i][j] = 0.f;
-    float xr[8];
-    float2 wr[4];
-    auto load = [&](int p0) {
-        // (kg p) mod n for p = p0 + pw, then stepped by kg (kg < n, n < 46341)
-        unsigned idx = kval ? ((unsigned)kg * (unsigned)(p0 + pw)) % (unsigned)n : 0u;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int p = p0 + pw + j;
-            wr[j] = (kval && p < n) ? __ldg(tw + idx) : make_float2(0.f, 0.f);
-            idx += (unsigned)kg;
-            if (idx >= (unsigned)n)
-                idx -= (unsigned)n;
-        }
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const int e = tid + 256 * j;
-            const int col = e >> 4, p = p0 + (e & 15), gc = c0 + col;
-            xr[j] = (gc < cols && p < n) ? __ldg(x + (size_t)gc * n + p) : 0.f;
-        }
-    };
-    load(0);
-    for (int p0 = 0; p0 < n; p0 += kDftBK) {
-        __syncthreads(); // the previous step is done with Ws / Xs
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            Ws[pw + j][2 * kk] = wr[j].x;
-            Ws[pw + j][2 * kk + 1] = wr[j].y;
-        }
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const int e = tid + 256 * j;
-            Xs[e & 15][e >> 4] = xr[j];
-        }
-        __syncthreads();
-        if (p0 + kDftBK < n)
-            load(p0 + kDftBK);
-#pragma unroll
-        for (int q = 0; q < kDftBK; q++) {
-            const float4 a0 = *reinterpret_cast<const float4 *>(&Ws[q][ty * 4]);
-            const float4 a1 = *reinterpret_cast<const float4 *>(&Ws[q][64 + ty * 4]);
-            const float4 b0 = *reinterpret_cast<const float4 *>(&Xs[q][tx * 4]);
-            const float4 b1 = *reinterpret_cast<const float4 *>(&Xs[q][64 + tx * 4]);
-            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-            for (int i = 0; i < 8; i++)
-#pragma unroll
-                for (int j = 0; j < 8; j++)
-                    acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
-        }
+    const int n = S.n, cols = S.cols, K = n / 2 + 1;
+    const int k0 = mt * kFreqTile, c0 = ct * kTcCols;
+    const int nfreq = min(kFreqTile, K - k0);
+    const int N = (2 * nfreq + 15) & ~15;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(N >> 3) << 17) |
+                           ((unsigned)(kTcCols >> 4) << 24);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_addr(&s_tmem)),
+                     "r"((unsigned)(kTcAcc * kTcN))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    // epilogue: rows (2f, 2f + 1) of the register tile are (re, im) of one
-    // frequency; ck |F / n|^4 summed over the thread's 4 frequencies
-    const float invn = 1.f / (float)n;
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-        float part = 0.f;
-#pragma unroll
-        for (int f = 0; f < 4; f++) {
-            const int freq = k0 + (f < 2 ? 0 : 32) + ty * 2 + (f & 1);
-            if (freq < K) {
-                const float re = acc[2 * f][j] * invn, im = acc[2 * f + 1][j] * invn;
-                const float s2 = re * re + im * im;
-                part = fmaf(__ldg(S.ck + freq), s2 * s2, part);
-            }
-        }
-        Red[ty][j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4)] = part;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&s_bar[0])), "r"(1u)
+                     : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&s_bar[1])), "r"(1u)
+                     : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&s_load[0])), "r"(1u)
+                     : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&s_load[1])), "r"(1u)
+                     : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid < kDftBN) {
-        float sum = 0.f;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = s_tmem;
+    bool ok = true;
+
+    // staging roles: column / component row r = tid & 127, sample chunks
+    // (4 samples) h, h + 2, h + 4, h + 6 of a stage, h = tid / 128
+    const int r = tid & 127, h = tid >> 7;
+    const int gcol = c0 + r;
+    const float *xcol = S.sino + (size_t)min(gcol, cols - 1) * n;
+    const bool acol = gcol < cols;
+    const int bf = r >> 1, be = r & 1;
+    const bool brow = bf < nfreq;
+    const unsigned f = (unsigned)(k0 + bf) % (unsigned)n;
+    const unsigned f4 = (4u * f) % (unsigned)n, f32 = (32u * f) % (unsigned)n;
+    unsigned idx = (f4 * (unsigned)h) % (unsigned)n; // (f p) mod n at p = p0 + 4 h
+    const int stages = (n + kTcKT - 1) / kTcKT;
+    // the operands of a stage, loaded one stage ahead so that the global and
+    // table loads are in flight during the previous stage's store and MMAs
+    float va[16], vb[16];
+    auto fetch = [&](int p0) {
+        unsigned ib = idx;
 #pragma unroll
-        for (int t = 0; t < 16; t++)
-            sum += Red[t][tid];
-        const int gc = c0 + tid;
+        for (int u = 0; u < 4; u++) {
+            const int kq = h + 2 * u;
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int p = p0 + 4 * kq + e;
+                va[4 * u + e] = acol && p < n ? __ldg(xcol + p) : 0.f;
+                if (!kPre) {
+                    float w = 0.f;
+                    if (brow && p < n) {
+                        const float2 t = __ldg(S.tw + ib);
+                        w = be ? t.y : t.x;
+                    }
+                    vb[4 * u + e] = w;
+                }
+                ib += f;
+                if (ib >= (unsigned)n)
+                    ib -= (unsigned)n;
+            }
+            ib += f4; // skip the other half's 4 samples
+            if (ib >= (unsigned)n)
+                ib -= (unsigned)n;
+        }
+        idx += f32;
+        if (idx >= (unsigned)n)
+            idx -= (unsigned)n;
+    };
+    fetch(0);
+    for (int s = 0; s < stages; s++) {
+        const int b = s & 1;
+        float *Ahi = tsm + b * kTcBufFloats, *Alo = Ahi + kTcAFloats;
+        float *Bhi = Alo + kTcAFloats, *Blo = Bhi + kTcBFloats;
+        float ca[16], cb[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            ca[i] = va[i];
+            cb[i] = vb[i];
+        }
+        if (s + 1 < stages)
+            fetch((s + 1) * kTcKT);
+        if (s >= 2)
+            ok &= mbar_wait(smem_addr(&s_bar[b]), ((s - 2) >> 1) & 1);
+        if (kPre && tid == 0) { // the stage's twiddle blocks (hi, lo: contiguous here and there)
+            const float *src = S.wtc + ((size_t)mt * stages + s) * 2 * kTcBFloats;
+            unsigned long long state;
+            asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 %0, [%1], %2;"
+                         : "=l"(state)
+                         : "r"(smem_addr(&s_load[b])), "r"((unsigned)(2 * kTcBFloats * sizeof(float)))
+                         : "memory");
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                             smem_addr(Bhi)),
+                         "l"(src), "r"((unsigned)(2 * kTcBFloats * sizeof(float))),
+                         "r"(smem_addr(&s_load[b]))
+                         : "memory");
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int kq = h + 2 * u;
+            const int off = (kq >> 1) * (kTcCols * 8) + (r >> 3) * 64 + (kq & 1) * 32 + (r & 7) * 4;
+            const float4 ah = make_float4(tf32_hi(ca[4 * u]), tf32_hi(ca[4 * u + 1]),
+                                          tf32_hi(ca[4 * u + 2]), tf32_hi(ca[4 * u + 3]));
+            *reinterpret_cast<float4 *>(Ahi + off) = ah;
+            *reinterpret_cast<float4 *>(Alo + off) =
+                make_float4(ca[4 * u] - ah.x, ca[4 * u + 1] - ah.y, ca[4 * u + 2] - ah.z,
+                            ca[4 * u + 3] - ah.w);
+            if (!kPre) {
+                const float4 bh = make_float4(tf32_hi(cb[4 * u]), tf32_hi(cb[4 * u + 1]),
+                                              tf32_hi(cb[4 * u + 2]), tf32_hi(cb[4 * u + 3]));
+                *reinterpret_cast<float4 *>(Bhi + off) = bh;
+                *reinterpret_cast<float4 *>(Blo + off) =
+                    make_float4(cb[4 * u] - bh.x, cb[4 * u + 1] - bh.y, cb[4 * u + 2] - bh.z,
+                                cb[4 * u + 3] - bh.w);
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            if (kPre)
+                ok &= mbar_wait(smem_addr(&s_load[b]), (s >> 1) & 1);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const unsigned ahi = smem_addr(Ahi), alo = smem_addr(Alo);
+            const unsigned bhi = smem_addr(Bhi), blo = smem_addr(Blo);
+            const unsigned slice = kTcCols * 32; // bytes per 8-sample block (A and B: 128 rows)
+            const unsigned dbig = tmem + (unsigned)(s % 3) * kTcN, dsmall = tmem + 3u * kTcN;
+#pragma unroll
+            for (int j = 0; j < kTcKT / 8; j++) {
+                const unsigned long long dah = umma_desc(ahi + j * slice, 128, 256);
+                const unsigned long long dal = umma_desc(alo + j * slice, 128, 256);
+                const unsigned long long dbh = umma_desc(bhi + j * slice, 128, 256);
+                const unsigned long long dbl = umma_desc(blo + j * slice, 128, 256);
+                umma_tf32(dbig, dah, dbh, idesc, (s >= 3 || j > 0) ? 1u : 0u);
+                umma_tf32(dsmall, dah, dbl, idesc, (s > 0 || j > 0) ? 1u : 0u);
+                umma_tf32(dsmall, dal, dbh, idesc, 1u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_addr(&s_bar[b]))
+                         : "memory");
+        }
+    }
+    ok &= mbar_wait(smem_addr(&s_bar[(stages - 1) & 1]), ((stages - 1) >> 1) & 1);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    // epilogue: warp w < 4 holds columns c0 + 32 w + lane
+    if (warp < 4) {
+        const float invn = 1.f / (float)n;
+        float part = 0.f;
+        const unsigned row = tmem + ((unsigned)(32 * warp) << 16);
+        const int chunks = (2 * nfreq + 31) / 32;
+        for (int q = 0; q < chunks; q++) {
+            float v[32], t[32];
+            tmem_ld32(row + 32u * q, v);
+            for (int d = 1; d < 4; d++) {
+                if (d < 3 && d >= stages)
+                    continue; // an accumulator no stage wrote
+                tmem_ld32(row + (unsigned)d * kTcN + 32u * q, t);
+#pragma unroll
+                for (int i = 0; i < 32; i++)
+                    v[i] += t[i];
+            }
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                const int fl = 16 * q + i;
+                if (fl < nfreq) {
+                    const float re = v[2 * i] * invn, im = v[2 * i + 1] * invn;
+                    const float s2 = re * re + im * im;
+                    part = fmaf(__ldg(S.ck + k0 + fl), s2 * s2, part);
+                }
+            }
+        }
+        const int gc = c0 + 32 * warp + lane;
         if (gc < cols)
-            S.partial[(size_t)mt * cols + gc] = sum;
+            S.partial[(size_t)mt * cols + gc] = ok ? part : __int_as_float(0x7fc00000);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"((unsigned)(kTcAcc * kTcN))
+                     : "memory");
     }
 }
+
 
 // P1, P2 and the P3 total of one column per warp (8 columns per CTA).  P2 is
 // the weighted selection of tt_select.cuh (no sort) for columns of finite,
@@ -566,6 +777,18 @@ cudaError_t launch_p3_dft_tables(int n, float2 *tw, float *ck, cudaStream_t st) 
 
 int p3_freq_tiles(int n) { return (n / 2 + 1 + kFreqTile - 1) / kFreqTile; }
 
+size_t p3_tc_table_floats(int n) {
+    return (size_t)p3_freq_tiles(n) * ((n + kTcKT - 1) / kTcKT) * 2 * kTcBFloats;
+}
+
+cudaError_t launch_p3_tc_tables(int n, const float2 *tw, float *out, cudaStream_t st) {
+    const long long total = (long long)p3_tc_table_floats(n) / 2;
+    if (n <= 0 || total <= 0)
+        return cudaSuccess;
+    p3_tc_tables_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(n, tw, out);
+    return cudaGetLastError();
+}
+
 int circus_warp_stride(int n_max) { return (n_max + 3) & ~3; }
 
 size_t circus_warp_smem_bytes(int n_max) {
@@ -579,7 +802,14 @@ cudaError_t launch_circus_stacks(const CircusStackArgs &a, size_t smem, cudaStre
     if (e != cudaSuccess)
         return e;
     if ((a.need & (1u << 3)) && a.total_tiles > 0) {
-        p3_dft_kernel<<<a.total_tiles, 256, 0, st>>>(a);
+        const void *k = a.tc_tables ? (const void *)p3_dft_tc_kernel<true>
+                                    : (const void *)p3_dft_tc_kernel<false>;
+        if (opt_in_smem(k) < kTcSmem)
+            return cudaErrorInvalidValue;
+        if (a.tc_tables)
+            p3_dft_tc_kernel<true><<<a.total_tiles, kTcThreads, kTcSmem, st>>>(a);
+        else
+            p3_dft_tc_kernel<false><<<a.total_tiles, kTcThreads, kTcSmem, st>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess)
             return e;
     }

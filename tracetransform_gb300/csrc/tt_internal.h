@@ -72,6 +72,7 @@ struct CircusStack {
     float *partial;     // P3: mtiles x cols partial sums of ck |F_k / n|^4
     const float2 *tw;   // n twiddles (cos, -sin)(2 pi j / n)
     const float *ck;    // n / 2 + 1 trapz weights
+    const float *wtc;   // the tensor cores' twiddle blocks of n (p3_tc_table_floats)
     int n, angles, cols;
     int mtiles;         // frequency tiles of 64 (P3)
     int tile_begin;     // first P3 tile of this stack (flat over stacks)
@@ -92,10 +93,14 @@ struct CircusStackArgs {
     int fb_capacity;
     int sort_len_max;   // power of two >= the longest column (exact-sort fallback)
     int fb_grid;        // CTAs of the exact-sort fallback
+    int tc_tables;      // every stack has wtc (else the kernel gathers the twiddles)
 };
 
 // Device tables of the direct-DFT P3: tw (n), ck (n / 2 + 1), built on stream.
 cudaError_t launch_p3_dft_tables(int n, float2 *tw, float *ck, cudaStream_t st);
+// The tensor-core P3's precomputed twiddle blocks of n, from its twiddles.
+size_t p3_tc_table_floats(int n);
+cudaError_t launch_p3_tc_tables(int n, const float2 *tw, float *out, cudaStream_t st);
 // Longest column whose P3 the direct DFT computes (longer ones: the FFT kernel).
 constexpr int kP3DftMaxRows = 2048;
 // P3 frequency tiles of a column length n.
