@@ -302,7 +302,8 @@ constexpr int kTcCols = 128, kTcKT = 32, kTcThreads = 256, kTcN = 2 * kFreqTile;
 constexpr int kTcAcc = 4; // accumulators of kTcN columns: hi.hi x 3, cross terms
 constexpr int kTcAFloats = kTcCols * kTcKT, kTcBFloats = kTcN * kTcKT;
 constexpr size_t kTcBufFloats = 2 * (size_t)kTcAFloats + 2 * (size_t)kTcBFloats;
-constexpr size_t kTcSmem = 2 * kTcBufFloats * sizeof(float); // 128 KB
+constexpr int kTcRing = 3; // stage buffers
+constexpr size_t kTcSmem = kTcRing * kTcBufFloats * sizeof(float); // 192 KB
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) {
     return (unsigned)__cvta_generic_to_shared(p);
@@ -384,12 +385,19 @@ __global__ void p3_tc_tables_kernel(int n, const float2 *__restrict__ tw, float 
     b[kTcBFloats + off] = v - hi;
 }
 
-// grid: one CTA per (64-frequency tile, 128 columns) over the stacks
+// grid: one CTA per (64-frequency tile, 128 columns) over the stacks.
+// Warp-specialised: warps 0-7 produce the stages into a ring of kTcRing
+// buffers (each thread its 16 sinogram samples, hi / lo split and stored;
+// with kPre one thread also starts the bulk copy of the twiddle blocks) and
+// arrive on the slot's `full` barrier (256 arrivals plus the copy's bytes);
+// warp 8 waits on `full`, issues the slot's 12 MMAs and commits them to the
+// slot's `empty` barrier, which the producers wait on before refilling it.
+// No CTA barrier inside the stage loop: producers run up to kTcRing stages
+// ahead of the MMAs.  Warps 0-3 then read the accumulators.
 template <bool kPre>
-__global__ void __launch_bounds__(kTcThreads, 1) p3_dft_tc_kernel(const CircusStackArgs a) {
+__global__ void __launch_bounds__(kTcThreads + 32, 1) p3_dft_tc_kernel(const CircusStackArgs a) {
     extern __shared__ __align__(1024) float tsm[];
-    __shared__ __align__(8) unsigned long long s_bar[2];
-    __shared__ __align__(8) unsigned long long s_load[2];
+    __shared__ __align__(8) unsigned long long s_full[kTcRing], s_empty[kTcRing], s_done;
     __shared__ unsigned s_tmem;
     const int tile = blockIdx.x;
     const CircusStack &S = stack_at(a, stack_of(a.st, a.n_st, tile, true));
@@ -400,9 +408,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) p3_dft_tc_kernel(const CircusSt
     const int nfreq = min(kFreqTile, K - k0);
     const int N = (2 * nfreq + 15) & ~15;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const unsigned idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(N >> 3) << 17) |
-                           ((unsigned)(kTcCols >> 4) << 24);
-    if (warp == 0) {
+    const int stages = (n + kTcKT - 1) / kTcKT;
+    constexpr int kMmaWarp = kTcThreads / 32;
+    if (warp == kMmaWarp) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_addr(&s_tmem)),
                      "r"((unsigned)(kTcAcc * kTcN))
@@ -410,13 +418,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) p3_dft_tc_kernel(const CircusSt
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&s_bar[0])), "r"(1u)
-                     : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&s_bar[1])), "r"(1u)
-                     : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&s_load[0])), "r"(1u)
-                     : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&s_load[1])), "r"(1u)
+        for (int i = 0; i < kTcRing; i++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&s_full[i])),
+                         "r"((unsigned)kTcThreads)
+                         : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&s_empty[i])),
+                         "r"(1u)
+                         : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&s_done)), "r"(1u)
                      : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -425,159 +435,170 @@ __global__ void __launch_bounds__(kTcThreads, 1) p3_dft_tc_kernel(const CircusSt
     const unsigned tmem = s_tmem;
     bool ok = true;
 
-    // staging roles: column / component row r = tid & 127, sample chunks
-    // (4 samples) h, h + 2, h + 4, h + 6 of a stage, h = tid / 128
-    const int r = tid & 127, h = tid >> 7;
-    const int gcol = c0 + r;
-    const float *xcol = S.sino + (size_t)min(gcol, cols - 1) * n;
-    const bool acol = gcol < cols;
-    const int bf = r >> 1, be = r & 1;
-    const bool brow = bf < nfreq;
-    const unsigned f = (unsigned)(k0 + bf) % (unsigned)n;
-    const unsigned f4 = (4u * f) % (unsigned)n, f32 = (32u * f) % (unsigned)n;
-    unsigned idx = (f4 * (unsigned)h) % (unsigned)n; // (f p) mod n at p = p0 + 4 h
-    const int stages = (n + kTcKT - 1) / kTcKT;
-    // the operands of a stage, loaded one stage ahead so that the global and
-    // table loads are in flight during the previous stage's store and MMAs
-    float va[16], vb[16];
-    auto fetch = [&](int p0) {
-        unsigned ib = idx;
+    if (warp == kMmaWarp) {
+        if (lane == 0) {
+            const unsigned idesc = (1u << 4) | (2u << 7) | (2u << 10) |
+                                   ((unsigned)(N >> 3) << 17) | ((unsigned)(kTcCols >> 4) << 24);
+            const unsigned slice = kTcCols * 32; // bytes per 8-sample block (A and B: 128 rows)
+            for (int s = 0; s < stages; s++) {
+                const int b = s % kTcRing;
+                ok &= mbar_wait(smem_addr(&s_full[b]), (unsigned)(s / kTcRing) & 1u);
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                float *Ahi = tsm + b * kTcBufFloats, *Alo = Ahi + kTcAFloats;
+                float *Bhi = Alo + kTcAFloats, *Blo = Bhi + kTcBFloats;
+                const unsigned ahi = smem_addr(Ahi), alo = smem_addr(Alo);
+                const unsigned bhi = smem_addr(Bhi), blo = smem_addr(Blo);
+                const unsigned dbig = tmem + (unsigned)(s % 3) * kTcN, dsmall = tmem + 3u * kTcN;
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int kq = h + 2 * u;
-#pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const int p = p0 + 4 * kq + e;
-                va[4 * u + e] = acol && p < n ? __ldg(xcol + p) : 0.f;
-                if (!kPre) {
-                    float w = 0.f;
-                    if (brow && p < n) {
-                        const float2 t = __ldg(S.tw + ib);
-                        w = be ? t.y : t.x;
-                    }
-                    vb[4 * u + e] = w;
+                for (int j = 0; j < kTcKT / 8; j++) {
+                    const unsigned long long dah = umma_desc(ahi + j * slice, 128, 256);
+                    const unsigned long long dal = umma_desc(alo + j * slice, 128, 256);
+                    const unsigned long long dbh = umma_desc(bhi + j * slice, 128, 256);
+                    const unsigned long long dbl = umma_desc(blo + j * slice, 128, 256);
+                    umma_tf32(dbig, dah, dbh, idesc, (s >= 3 || j > 0) ? 1u : 0u);
+                    umma_tf32(dsmall, dah, dbl, idesc, (s > 0 || j > 0) ? 1u : 0u);
+                    umma_tf32(dsmall, dal, dbh, idesc, 1u);
                 }
-                ib += f;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_addr(&s_empty[b]))
+                             : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_addr(&s_done))
+                         : "memory");
+        }
+    } else {
+        // producers: column / component row r = tid & 127, sample chunks
+        // (4 samples) h, h + 2, h + 4, h + 6 of a stage, h = tid / 128
+        const int r = tid & 127, h = tid >> 7;
+        const int gcol = c0 + r;
+        const float *xcol = S.sino + (size_t)min(gcol, cols - 1) * n;
+        const bool acol = gcol < cols;
+        const int bf = r >> 1, be = r & 1;
+        const bool brow = bf < nfreq;
+        const unsigned f = (unsigned)(k0 + bf) % (unsigned)n;
+        const unsigned f4 = (4u * f) % (unsigned)n, f32 = (32u * f) % (unsigned)n;
+        unsigned idx = (f4 * (unsigned)h) % (unsigned)n; // (f p) mod n at p = p0 + 4 h
+        float va[16], vb[16];
+        auto fetch = [&](int p0) {
+            unsigned ib = idx;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int kq = h + 2 * u;
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int p = p0 + 4 * kq + e;
+                    va[4 * u + e] = acol && p < n ? __ldg(xcol + p) : 0.f;
+                    if (!kPre) {
+                        float w = 0.f;
+                        if (brow && p < n) {
+                            const float2 t = __ldg(S.tw + ib);
+                            w = be ? t.y : t.x;
+                        }
+                        vb[4 * u + e] = w;
+                    }
+                    ib += f;
+                    if (ib >= (unsigned)n)
+                        ib -= (unsigned)n;
+                }
+                ib += f4; // skip the other half's 4 samples
                 if (ib >= (unsigned)n)
                     ib -= (unsigned)n;
             }
-            ib += f4; // skip the other half's 4 samples
-            if (ib >= (unsigned)n)
-                ib -= (unsigned)n;
-        }
-        idx += f32;
-        if (idx >= (unsigned)n)
-            idx -= (unsigned)n;
-    };
-    fetch(0);
-    for (int s = 0; s < stages; s++) {
-        const int b = s & 1;
-        float *Ahi = tsm + b * kTcBufFloats, *Alo = Ahi + kTcAFloats;
-        float *Bhi = Alo + kTcAFloats, *Blo = Bhi + kTcBFloats;
-        float ca[16], cb[16];
-#pragma unroll
-        for (int i = 0; i < 16; i++) {
-            ca[i] = va[i];
-            cb[i] = vb[i];
-        }
-        if (s + 1 < stages)
-            fetch((s + 1) * kTcKT);
-        if (s >= 2)
-            ok &= mbar_wait(smem_addr(&s_bar[b]), ((s - 2) >> 1) & 1);
-        if (kPre && tid == 0) { // the stage's twiddle blocks (hi, lo: contiguous here and there)
-            const float *src = S.wtc + ((size_t)mt * stages + s) * 2 * kTcBFloats;
-            unsigned long long state;
-            asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 %0, [%1], %2;"
-                         : "=l"(state)
-                         : "r"(smem_addr(&s_load[b])), "r"((unsigned)(2 * kTcBFloats * sizeof(float)))
-                         : "memory");
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                             smem_addr(Bhi)),
-                         "l"(src), "r"((unsigned)(2 * kTcBFloats * sizeof(float))),
-                         "r"(smem_addr(&s_load[b]))
-                         : "memory");
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int kq = h + 2 * u;
-            const int off = (kq >> 1) * (kTcCols * 8) + (r >> 3) * 64 + (kq & 1) * 32 + (r & 7) * 4;
-            const float4 ah = make_float4(tf32_hi(ca[4 * u]), tf32_hi(ca[4 * u + 1]),
-                                          tf32_hi(ca[4 * u + 2]), tf32_hi(ca[4 * u + 3]));
-            *reinterpret_cast<float4 *>(Ahi + off) = ah;
-            *reinterpret_cast<float4 *>(Alo + off) =
-                make_float4(ca[4 * u] - ah.x, ca[4 * u + 1] - ah.y, ca[4 * u + 2] - ah.z,
-                            ca[4 * u + 3] - ah.w);
-            if (!kPre) {
-                const float4 bh = make_float4(tf32_hi(cb[4 * u]), tf32_hi(cb[4 * u + 1]),
-                                              tf32_hi(cb[4 * u + 2]), tf32_hi(cb[4 * u + 3]));
-                *reinterpret_cast<float4 *>(Bhi + off) = bh;
-                *reinterpret_cast<float4 *>(Blo + off) =
-                    make_float4(cb[4 * u] - bh.x, cb[4 * u + 1] - bh.y, cb[4 * u + 2] - bh.z,
-                                cb[4 * u + 3] - bh.w);
-            }
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            if (kPre)
-                ok &= mbar_wait(smem_addr(&s_load[b]), (s >> 1) & 1);
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const unsigned ahi = smem_addr(Ahi), alo = smem_addr(Alo);
-            const unsigned bhi = smem_addr(Bhi), blo = smem_addr(Blo);
-            const unsigned slice = kTcCols * 32; // bytes per 8-sample block (A and B: 128 rows)
-            const unsigned dbig = tmem + (unsigned)(s % 3) * kTcN, dsmall = tmem + 3u * kTcN;
-#pragma unroll
-            for (int j = 0; j < kTcKT / 8; j++) {
-                const unsigned long long dah = umma_desc(ahi + j * slice, 128, 256);
-                const unsigned long long dal = umma_desc(alo + j * slice, 128, 256);
-                const unsigned long long dbh = umma_desc(bhi + j * slice, 128, 256);
-                const unsigned long long dbl = umma_desc(blo + j * slice, 128, 256);
-                umma_tf32(dbig, dah, dbh, idesc, (s >= 3 || j > 0) ? 1u : 0u);
-                umma_tf32(dsmall, dah, dbl, idesc, (s > 0 || j > 0) ? 1u : 0u);
-                umma_tf32(dsmall, dal, dbh, idesc, 1u);
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_addr(&s_bar[b]))
-                         : "memory");
-        }
-    }
-    ok &= mbar_wait(smem_addr(&s_bar[(stages - 1) & 1]), ((stages - 1) >> 1) & 1);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-
-    // epilogue: warp w < 4 holds columns c0 + 32 w + lane
-    if (warp < 4) {
-        const float invn = 1.f / (float)n;
-        float part = 0.f;
-        const unsigned row = tmem + ((unsigned)(32 * warp) << 16);
-        const int chunks = (2 * nfreq + 31) / 32;
-        for (int q = 0; q < chunks; q++) {
-            float v[32], t[32];
-            tmem_ld32(row + 32u * q, v);
-            for (int d = 1; d < 4; d++) {
-                if (d < 3 && d >= stages)
-                    continue; // an accumulator no stage wrote
-                tmem_ld32(row + (unsigned)d * kTcN + 32u * q, t);
-#pragma unroll
-                for (int i = 0; i < 32; i++)
-                    v[i] += t[i];
-            }
+            idx += f32;
+            if (idx >= (unsigned)n)
+                idx -= (unsigned)n;
+        };
+        fetch(0);
+        for (int s = 0; s < stages; s++) {
+            const int b = s % kTcRing;
+            float *Ahi = tsm + b * kTcBufFloats, *Alo = Ahi + kTcAFloats;
+            float *Bhi = Alo + kTcAFloats, *Blo = Bhi + kTcBFloats;
+            float ca[16], cb[16];
 #pragma unroll
             for (int i = 0; i < 16; i++) {
-                const int fl = 16 * q + i;
-                if (fl < nfreq) {
-                    const float re = v[2 * i] * invn, im = v[2 * i + 1] * invn;
-                    const float s2 = re * re + im * im;
-                    part = fmaf(__ldg(S.ck + k0 + fl), s2 * s2, part);
+                ca[i] = va[i];
+                cb[i] = vb[i];
+            }
+            if (s + 1 < stages)
+                fetch((s + 1) * kTcKT);
+            if (s >= kTcRing)
+                ok &= mbar_wait(smem_addr(&s_empty[b]), (unsigned)(s / kTcRing - 1) & 1u);
+            if (kPre && tid == 0) { // the stage's twiddle blocks (hi, lo: contiguous here and there)
+                const unsigned bytes = (unsigned)(2 * kTcBFloats * sizeof(float));
+                asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(
+                                 smem_addr(&s_full[b])),
+                             "r"(bytes)
+                             : "memory");
+                const float *src = S.wtc + ((size_t)mt * stages + s) * 2 * kTcBFloats;
+                asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                                 smem_addr(Bhi)),
+                             "l"(src), "r"(bytes), "r"(smem_addr(&s_full[b]))
+                             : "memory");
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int kq = h + 2 * u;
+                const int off = (kq >> 1) * (kTcCols * 8) + (r >> 3) * 64 + (kq & 1) * 32 + (r & 7) * 4;
+                const float4 ah = make_float4(tf32_hi(ca[4 * u]), tf32_hi(ca[4 * u + 1]),
+                                              tf32_hi(ca[4 * u + 2]), tf32_hi(ca[4 * u + 3]));
+                *reinterpret_cast<float4 *>(Ahi + off) = ah;
+                *reinterpret_cast<float4 *>(Alo + off) =
+                    make_float4(ca[4 * u] - ah.x, ca[4 * u + 1] - ah.y, ca[4 * u + 2] - ah.z,
+                                ca[4 * u + 3] - ah.w);
+                if (!kPre) {
+                    const float4 bh = make_float4(tf32_hi(cb[4 * u]), tf32_hi(cb[4 * u + 1]),
+                                                  tf32_hi(cb[4 * u + 2]), tf32_hi(cb[4 * u + 3]));
+                    *reinterpret_cast<float4 *>(Bhi + off) = bh;
+                    *reinterpret_cast<float4 *>(Blo + off) =
+                        make_float4(cb[4 * u] - bh.x, cb[4 * u + 1] - bh.y, cb[4 * u + 2] - bh.z,
+                                    cb[4 * u + 3] - bh.w);
                 }
             }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            unsigned long long state;
+            asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 %0, [%1];"
+                         : "=l"(state)
+                         : "r"(smem_addr(&s_full[b]))
+                         : "memory");
         }
-        const int gc = c0 + 32 * warp + lane;
-        if (gc < cols)
-            S.partial[(size_t)mt * cols + gc] = ok ? part : __int_as_float(0x7fc00000);
+        // epilogue: warp w < 4 holds columns c0 + 32 w + lane
+        if (warp < 4) {
+            ok &= mbar_wait(smem_addr(&s_done), 0u);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const float invn = 1.f / (float)n;
+            float part = 0.f;
+            const unsigned row = tmem + ((unsigned)(32 * warp) << 16);
+            const int chunks = (2 * nfreq + 31) / 32;
+            for (int q = 0; q < chunks; q++) {
+                float v[32], t[32];
+                tmem_ld32(row + 32u * q, v);
+                for (int d = 1; d < 4; d++) {
+                    if (d < 3 && d >= stages)
+                        continue; // an accumulator no stage wrote
+                    tmem_ld32(row + (unsigned)d * kTcN + 32u * q, t);
+#pragma unroll
+                    for (int i = 0; i < 32; i++)
+                        v[i] += t[i];
+                }
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    const int fl = 16 * q + i;
+                    if (fl < nfreq) {
+                        const float re = v[2 * i] * invn, im = v[2 * i + 1] * invn;
+                        const float s2 = re * re + im * im;
+                        part = fmaf(__ldg(S.ck + k0 + fl), s2 * s2, part);
+                    }
+                }
+            }
+            const int gc = c0 + 32 * warp + lane;
+            if (gc < cols)
+                S.partial[(size_t)mt * cols + gc] = ok ? part : __int_as_float(0x7fc00000);
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) {
+    if (warp == kMmaWarp) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                      "r"((unsigned)(kTcAcc * kTcN))
@@ -807,9 +828,9 @@ cudaError_t launch_circus_stacks(const CircusStackArgs &a, size_t smem, cudaStre
         if (opt_in_smem(k) < kTcSmem)
             return cudaErrorInvalidValue;
         if (a.tc_tables)
-            p3_dft_tc_kernel<true><<<a.total_tiles, kTcThreads, kTcSmem, st>>>(a);
+            p3_dft_tc_kernel<true><<<a.total_tiles, kTcThreads + 32, kTcSmem, st>>>(a);
         else
-            p3_dft_tc_kernel<false><<<a.total_tiles, kTcThreads, kTcSmem, st>>>(a);
+            p3_dft_tc_kernel<false><<<a.total_tiles, kTcThreads + 32, kTcSmem, st>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess)
             return e;
     }
