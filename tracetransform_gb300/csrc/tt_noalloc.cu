@@ -21,7 +21,7 @@
 //
 // The array's device address is looked up once per device (the first call
 // made with that device current); with CUDA's lazy module loading that first
-// call is also where the driver loads this module and allocates the array,
+// call is also where the CUDA driver loads this module and allocates the array,
 // so make it before any region that must not allocate (or run with
 // CUDA_MODULE_LOADING=EAGER).  The cached address does not survive
 // cudaDeviceReset.
