@@ -183,6 +183,29 @@ def test_circus_vs_oracle(oracle_lib):
     assert_accounted(rep, "circus")
 
 
+@pytest.mark.parametrize("rows,cols,ns", [(1, 5, 1), (2, 7, 2), (3, 130, 1), (17, 129, 3),
+                                          (130, 257, 2), (1449, 40, 2), (2048, 131, 1)])
+def test_p_stage_tensor_core_edges(oracle_lib, engine, rows, cols, ns):
+    """P1-P3 of sinogram stacks through tt_circus_device -- P3 on the tensor
+    cores with the precomputed twiddle blocks -- at its edges: the shortest
+    columns (one to three frequencies: the smallest MMA width), column counts
+    that leave partial 128-column tiles, and the longest columns the DFT path
+    takes (2048 rows), against the oracle's P-stage, every entry accounted."""
+    import torch
+    rng = np.random.default_rng(rows * 1000 + cols)
+    t = np.linspace(-1, 1, rows)
+    sino = (np.exp(-(t[None, :, None] / rng.uniform(0.2, 0.6, (ns, 1, cols))) ** 2) *
+            rng.uniform(1, 50, (ns, 1, cols)) + rng.uniform(0, 0.5, (ns, rows, cols)))
+    sino = sino.astype(np.float32)
+    dev = torch.from_numpy(np.ascontiguousarray(sino.transpose(0, 2, 1))).cuda()
+    got = engine.circus(dev, [(k, -1, -1) for k in (1, 2, 3)])
+    torch.cuda.synchronize()
+    got = got.cpu().numpy()
+    rep = account_circus(sino, P123, got)
+    record(f"p_stage_edges_{rows}x{cols}x{ns}", rep)
+    assert_accounted(rep, f"P-stage {rows} x {cols} x {ns}")
+
+
 def test_zscore_bit_exact(oracle_lib):
     rng = np.random.default_rng(3)
     for n in (2, 7, 360, 720):
