@@ -38,6 +38,25 @@ def test_nos_orthonormal_columns_full_size(oracle_lib):
     assert np.abs(got - want).max() < 1e-4
 
 
+@pytest.mark.parametrize("rows,cols", [(4300, 40), (4500, 33), (4200, 130)])
+def test_nos_tall_blocked_q(oracle_lib, rows, cols):
+    """Aligned columns longer than 4096 rows: Q [P; 0] by blocks of 32
+    reflectors (a partial last block -- one reflector at 33 columns -- and a
+    partial 128-column tile at 130) against the oracle's double Jacobi."""
+    rng = np.random.default_rng(rows + cols)
+    r = np.arange(rows, dtype=np.float64)[:, None]
+    mu = rng.uniform(0.3, 0.7, cols) * rows
+    sig = rng.uniform(0.05, 0.2, cols) * rows
+    sino = (rng.uniform(50, 200, cols) * np.exp(-0.5 * ((r - mu) / sig) ** 2)
+            + rng.uniform(0, 4, (rows, cols))).astype(np.float32)
+    got, c = tt.nearest_orthonormal_sinogram(sino)
+    want, wc = oracle_lib.nos(sino)
+    assert got.shape == want.shape and got.shape[0] > 4096 and c == wc
+    g = got.astype(np.float64)
+    assert np.abs(g.T @ g - np.eye(cols)).max() < 1e-4
+    np.testing.assert_allclose(got, want, rtol=0, atol=2e-5)
+
+
 def test_nos_needs_rows(oracle_lib):
     sino = _sino(oracle_lib, 12, 12, 1)  # 360 angles, N = 17: m < cols
     with pytest.raises(TTError):

@@ -808,19 +808,22 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
     TT_CHECK(p->ensure(p->nos_a, sizeof(float2) * a_elems));
     TT_CHECK(p->ensure(p->nos_desc, sizeof(NosDesc) * n_sino));
     TT_CHECK(p->ensure(p->nos, sizeof(float) * a_elems));
-    if (max_m > tt::nos_max_rows() || tt::nos_apply_smem(max_m) > 227 * 1024)
+    if (max_m > tt::nos_max_rows())
         return fail(TT_ERR_UNSUPPORTED,
                     "nearest orthonormal sinogram of %d aligned rows exceeds %d", max_m,
                     tt::nos_max_rows());
     if (cols > 1024)
         return fail(TT_ERR_UNSUPPORTED, "orthonormal circus of %d angles exceeds 1024", cols);
     // scratch: 5 double-float + 3 int vectors of n, 3 float n x n matrices,
-    // 2 float vectors, the sweep loop's state
+    // 2 float vectors, the sweep loop's state, then (256-byte aligned) the
+    // blocked Q application's
     const size_t nv = ncol, nm = (size_t)cols * cols * n_sino;
-    TT_CHECK(p->ensure(p->nos_work, sizeof(float2) * 5 * nv + sizeof(int) * 3 * nv +
-                                        sizeof(float) * (3 * nm + 2 * nv) +
-                                        sizeof(unsigned) * n_sino + sizeof(float) * n_sino +
-                                        sizeof(unsigned) * 2 + 64));
+    const size_t head = sizeof(float2) * 5 * nv + sizeof(int) * 3 * nv +
+                        sizeof(float) * (3 * nm + 2 * nv) + sizeof(unsigned) * n_sino +
+                        sizeof(float) * n_sino + sizeof(unsigned) * 2;
+    const size_t wy_at = (head + 255) & ~size_t(255);
+    TT_CHECK(p->ensure(p->nos_work,
+                       wy_at + sizeof(float) * tt::nos_assemble_floats(cols, n_sino, max_m)));
     tt::NosWork w;
     {
         char *q = (char *)p->nos_work.p;
@@ -838,6 +841,7 @@ tt_status run_nos(tt_plan *p, const float *d_sino, int rows, int cols, int n_sin
         w.off_bits = (unsigned *)(w.perm + nv);
         w.tiny = (float *)(w.off_bits + n_sino);
         w.sweep_state = (unsigned *)(w.tiny + n_sino);
+        w.wy = (float *)((char *)p->nos_work.p + wy_at);
     }
     TT_CUDA(cudaMemcpyAsync(p->nos_desc.p, desc.data(), sizeof(NosDesc) * n_sino,
                             cudaMemcpyHostToDevice, st));

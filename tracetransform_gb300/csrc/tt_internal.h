@@ -195,6 +195,8 @@ struct NosWork {
     unsigned *off_bits;         // n_sino: largest rotated |cos| of a sweep (float bits)
     float *tiny;                // n_sino: squared column norm below which a direction is null
     unsigned *sweep_state;      // 2: the last sweep's largest cos (float bits), sweeps done
+    float *wy;                  // nos_assemble_floats(): the blocked Q application's T
+                                // factors, partial products and T W
 };
 cudaError_t launch_nos_offsets(const float *sino, int rows, int cols, int n_sino, int center,
                                int *offsets, cudaStream_t st);
@@ -211,7 +213,10 @@ int nos_max_rows(); // aligned rows the QR kernels hold in registers
 // zeroed before the loop, counts them).
 cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, int max_sweeps,
                              cudaGraphConditionalHandle loop, cudaStream_t st);
-size_t nos_apply_smem(int max_m);
+// Scratch floats (NosWork.wy) of launch_nos_assemble.
+size_t nos_assemble_floats(int n, int n_sino, int max_m);
+// The nearest orthonormal sinograms from the converged sweeps:
+// Q [V U^T; 0] by blocks of reflectors, into out.
 cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int n_sino,
                                 int max_m, const NosWork &w, float *out, cudaStream_t st);
 

@@ -537,10 +537,13 @@ constexpr float kJacTol = 1e-6f, kJacDone = 1e-4f;
 // columns of V are multiplied by J once per round, in row chunks staged
 // through shared memory.  Columns sit in shared memory zero-padded to a
 // multiple of 128 rows, so a lane moves 4 consecutive rows per 128-bit
-// access and no row needs a bounds test.  Blocks of 16 keep the grid of 8
-// sinograms of 360 angles within one CTA per SM.
-constexpr int kBJ = 16, kBCols = 2 * kBJ, kBThreads = 32 * kBJ;
-constexpr int kVRows = 256; // rows of V per chunk: 64 groups of 4 rows x 8 groups of 4 columns
+// access and no row needs a bounds test.  Blocks of 12 (measured at 8
+// sinograms of 1449 x 360 and 5795 x 720: 11 % and 29 % faster sweeps than
+// blocks of 16, whose inner rounds are longer; blocks of 8 took one sweep
+// more) give a round of 8 x 360-angle sinograms 120 CTAs.
+constexpr int kBJ = 12, kBCols = 2 * kBJ, kBThreads = 32 * kBJ;
+constexpr int kVRows = 256; // rows of V per chunk: 64 groups of 4 rows x kBCols / 4 of 4 columns
+static_assert(kBJ % 2 == 0 && kBCols <= 32, "whole pairs per block; a J row per lane");
 static_assert(kBThreads == (kVRows / 4) * (kBCols / 4), "one 4 x 4 tile of V J per thread");
 
 __device__ __forceinline__ void round_robin(int players, int round, int k, int &p, int &q) {
@@ -750,13 +753,15 @@ rt_block_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int n
     float wmax = 0.f;
     // J <- J G on columns p, q (row `lane` of each)
     auto j_rotate = [&](int p, int q, float c, float sn) {
+        if (kBCols < 32 && lane >= kBCols)
+            return;
         const float a = Jt[p][lane], b = Jt[q][lane];
         Jt[p][lane] = c * a - sn * b;
         Jt[q][lane] = sn * a + c * b;
     };
     float4 x[K4], y[K4];
     if (intra) {
-        // pairs within each block: warps 0..7 block bp, 8..15 block bq
+        // pairs within each block: warps 0 .. kBJ / 2 - 1 block bp, the rest block bq
         const int half = warp / (kBJ / 2);
         for (int ir = 0; ir < kBJ - 1; ir++) {
             int p, q;
@@ -819,8 +824,9 @@ rt_block_round_kernel(float *__restrict__ X, float *__restrict__ V, int n, int n
         Jr[e / kBCols][e % kBCols] = Jt[e % kBCols][e / kBCols];
 
     // V block <- V block J, kVRows rows per pass: thread t computes rows
-    // 4 (t / 8) .. + 3 and columns 4 (t % 8) .. + 3 of each pass
-    const int cg = (threadIdx.x % 8) * 4, rg = (threadIdx.x / 8) * 4;
+    // 4 (t / G) .. + 3 and columns 4 (t % G) .. + 3 of each pass, G = kBCols / 4
+    constexpr int kCG = kBCols / 4;
+    const int cg = (threadIdx.x % kCG) * 4, rg = (threadIdx.x / kCG) * 4;
     auto vj_tile = [&](const float *vb, int ld, float (&acc)[4][4]) {
 #pragma unroll
         for (int u = 0; u < 4; u++)
@@ -949,82 +955,13 @@ rt_gemm_kernel(const float *__restrict__ A, int ai, int ak, const float *__restr
     }
 }
 
+// Y = Q [P; 0] = H_0 H_1 ... H_{n-1} [P; 0], out[:, perm[j]] = Y[:, j]:
+// one reflector at a time with Y in registers while the aligned columns fit
+// (m <= 16 kQThreads), by blocks of reflectors above.
 constexpr int kQThreads = 256, kQCols = 4; // columns of Y per CTA
 constexpr int kNosMaxCols = 1024;              // angles the orthonormal circus takes
 
-// Y = Q [P; 0] = H_0 H_1 ... H_{n-1} [P; 0] for kQCols columns of P per CTA
-// (shared memory: kQCols x m floats), then out[:, perm[j]] = Y[:, j].
-// grid (ceil(n / kQCols), n_sino).
-__global__ void __launch_bounds__(kQThreads)
-nos_apply_q_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc,
-                   const float2 *__restrict__ tau, const float2 *__restrict__ scale,
-                   const int *__restrict__ perm, const float *__restrict__ P, int n,
-                   float *__restrict__ out) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    float *y = reinterpret_cast<float *>(smraw);
-    __shared__ float red[kQThreads / 32][kQCols];
-    const int s = blockIdx.y, j0 = blockIdx.x * kQCols;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const NosDesc d = desc[s];
-    const int m = d.m, nc = min(kQCols, n - j0);
-    const size_t nn = (size_t)n * n;
-    for (int c = 0; c < kQCols; c++)
-        for (int i = threadIdx.x; i < m; i += kQThreads)
-            y[c * m + i] = (c < nc && i < n) ? P[s * nn + i + (size_t)(j0 + c) * n] : 0.f;
-    const float2 *As = A + d.a_off;
-    const float2 *ts = tau + (size_t)s * n, *sc = scale + (size_t)s * n;
-    const int *pm = perm + (size_t)s * n;
-    for (int k = n - 1; k >= 0; k--) {
-        const float t = ts[k].x + ts[k].y;
-        if (t == 0.f)
-            continue; // uniform
-        // reflector k: v = (1, x[k+1:] scale[k]), x the stored pivot column
-        const float2 *v = As + (size_t)pm[k] * m;
-        const float vs = sc[k].x + sc[k].y;
-        __syncthreads();
-        float w[kQCols];
-#pragma unroll
-        for (int c = 0; c < kQCols; c++)
-            w[c] = 0.f;
-        for (int i = k + 1 + threadIdx.x; i < m; i += kQThreads) {
-            const float vi = (v[i].x + v[i].y) * vs;
-#pragma unroll
-            for (int c = 0; c < kQCols; c++)
-                w[c] = fmaf(vi, y[c * m + i], w[c]);
-        }
-#pragma unroll
-        for (int c = 0; c < kQCols; c++) {
-            w[c] = warp_sum(w[c]);
-            if (lane == 0)
-                red[warp][c] = w[c];
-        }
-        __syncthreads();
-#pragma unroll
-        for (int c = 0; c < kQCols; c++) {
-            float tot = y[c * m + k];
-            for (int u = 0; u < kQThreads / 32; u++)
-                tot += red[u][c];
-            w[c] = t * tot;
-        }
-        __syncthreads(); // everyone has read y[.., k] and red
-        for (int i = k + 1 + threadIdx.x; i < m; i += kQThreads) {
-            const float vi = (v[i].x + v[i].y) * vs;
-#pragma unroll
-            for (int c = 0; c < kQCols; c++)
-                y[c * m + i] = fmaf(-w[c], vi, y[c * m + i]);
-        }
-        if (threadIdx.x < kQCols)
-            y[threadIdx.x * m + k] -= w[threadIdx.x];
-    }
-    __syncthreads();
-    for (int c = 0; c < nc; c++) {
-        float *o = out + d.out_off + (size_t)pm[j0 + c] * m;
-        for (int i = threadIdx.x; i < m; i += kQThreads)
-            o[i] = y[c * m + i];
-    }
-}
-
-// The same product with Y held in registers, for m <= K kQThreads: thread t
+// The product with Y held in registers, for m <= K kQThreads: thread t
 // owns rows t + kQThreads u (u < K) of the kQCols columns, so applying a
 // reflector needs one block reduction (double-buffered: one barrier) and no
 // other exchange; the next reflector's column is loaded while the current
@@ -1126,6 +1063,361 @@ nos_apply_q_reg_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__
             if (i < m)
                 o[i] = y[c][u];
         }
+    }
+}
+
+// Y = Q [P; 0] = H_0 H_1 ... H_{n-1} [P; 0] by blocks of kWyB reflectors in
+// compact WY form (the LAPACK larft / larfb scheme): the product of reflectors
+// k0 .. k0 + b - 1 is I - V T V^T with V = [v_k0 .. v_k0+b-1] (v_k: 1 at row
+// k, the scaled stored pivot column below it, 0 above) and T upper
+// triangular, T[i, i] = tau_i, T[0:i, i] = -tau_i T[0:i, 0:i] V[:, 0:i]^T v_i.
+// The blocks apply last to first, each as Y <- Y - V (T (V^T Y)) over rows
+// k0.. (V is zero above): V^T Y by row chunks into partial sums, T times
+// their sum, then the rank-b update -- float GEMM tiles instead of one
+// latency-bound pass over Y per reflector.  Y lives in the output: its
+// column j is out[:, perm[j]].
+constexpr int kWyB = 32;          // reflectors per block
+constexpr int kWyThreads = 256;   // threads of every WY kernel
+constexpr int kWyCols = 128;      // columns of Y per CTA of the GEMM passes
+constexpr int kWyVLd = 36;        // V tile row stride (float4 rows, conflict-free fill)
+constexpr int kWyYLd = 132;       // Y / W tile row stride
+constexpr int kWyGramRows = 128;  // rows per pass of the T kernel
+
+// out[:, perm[j]] = [P[:, j]; 0].  grid (n, n_sino).
+__global__ void __launch_bounds__(kWyThreads)
+wy_init_kernel(const float *__restrict__ P, const NosDesc *__restrict__ desc,
+               const int *__restrict__ perm, int n, float *__restrict__ out) {
+    const int j = blockIdx.x, s = blockIdx.y;
+    const NosDesc d = desc[s];
+    float *o = out + d.out_off + (size_t)perm[(size_t)s * n + j] * d.m;
+    const float *p = P + (size_t)s * n * n + (size_t)j * n;
+    for (int i = threadIdx.x; i < d.m; i += kWyThreads)
+        o[i] = i < n ? p[i] : 0.f;
+}
+
+// Per-block reflector data in shared memory: stored column, float scale and
+// tau (0 past n, which makes those columns of V and T zero).
+struct WyRefl {
+    int pm[kWyB];
+    float vs[kWyB], t[kWyB];
+};
+__device__ __forceinline__ void wy_load_refl(WyRefl &R, const float2 *tau, const float2 *scale,
+                                             const int *perm, int n, int s, int k0) {
+    if (threadIdx.x < kWyB) {
+        const int k = k0 + threadIdx.x;
+        const bool ok = k < n;
+        const size_t o = (size_t)s * n + k;
+        R.pm[threadIdx.x] = ok ? perm[o] : 0;
+        R.vs[threadIdx.x] = ok ? scale[o].x + scale[o].y : 0.f;
+        R.t[threadIdx.x] = ok ? tau[o].x + tau[o].y : 0.f;
+    }
+}
+// v_{k0 + r}[row] for a row inside the matrix (row < m).
+__device__ __forceinline__ float wy_v(const float2 *As, int m, const WyRefl &R, int n, int k0,
+                                      int r, int row) {
+    const int k = k0 + r;
+    if (k >= n || row < k)
+        return 0.f;
+    if (row == k)
+        return 1.f;
+    const float2 x = As[(size_t)R.pm[r] * m + row];
+    return (x.x + x.y) * R.vs[r];
+}
+
+// T of every block: the Gram matrix G = V^T V over rows k0..m-1 (kWyGramRows
+// rows of V staged per pass; thread t accumulates G[t / 32 + 8 q][t % 32]),
+// then the recurrence on one warp.  grid (blocks, n_sino); T row-major,
+// 32 x 32 per (sinogram, block).
+__global__ void __launch_bounds__(kWyThreads)
+wy_t_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc,
+            const float2 *__restrict__ tau, const float2 *__restrict__ scale,
+            const int *__restrict__ perm, int n, float *__restrict__ T) {
+    __shared__ float Vs[kWyGramRows][kWyB + 1];
+    __shared__ float Gs[kWyB][kWyB + 1];
+    __shared__ float Ts[kWyB][kWyB + 1];
+    __shared__ WyRefl R;
+    const int jb = blockIdx.x, s = blockIdx.y, k0 = jb * kWyB;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const NosDesc d = desc[s];
+    const int m = d.m;
+    const float2 *As = A + d.a_off;
+    wy_load_refl(R, tau, scale, perm, n, s, k0);
+    __syncthreads(); // R in place
+    constexpr int kPer = kWyGramRows * kWyB / kWyThreads;
+    float vr[kPer]; // the next pass, fetched while the current one is reduced
+    auto fetch = [&](int row0) {
+#pragma unroll
+        for (int q = 0; q < kPer; q++) {
+            const int e = threadIdx.x + kWyThreads * q;
+            const int i = e % kWyGramRows, r = e / kWyGramRows, row = row0 + i;
+            vr[q] = row < m ? wy_v(As, m, R, n, k0, r, row) : 0.f;
+        }
+    };
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    if (k0 < m)
+        fetch(k0);
+    for (int row0 = k0; row0 < m; row0 += kWyGramRows) {
+        __syncthreads(); // the previous pass is read
+#pragma unroll
+        for (int q = 0; q < kPer; q++) {
+            const int e = threadIdx.x + kWyThreads * q;
+            Vs[e % kWyGramRows][e / kWyGramRows] = vr[q];
+        }
+        __syncthreads();
+        if (row0 + kWyGramRows < m)
+            fetch(row0 + kWyGramRows);
+#pragma unroll 4
+        for (int i = 0; i < kWyGramRows; i++) {
+            const float b = Vs[i][lane];
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                acc[q] = fmaf(Vs[i][warp + 8 * q], b, acc[q]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+        Gs[warp + 8 * q][lane] = acc[q];
+    __syncthreads();
+    if (warp == 0) {
+        for (int c = 0; c < kWyB; c++)
+            Ts[lane][c] = 0.f;
+        __syncwarp();
+        for (int i = 0; i < kWyB; i++) {
+            float v = 0.f;
+            if (lane < i) {
+                for (int c = lane; c < i; c++)
+                    v = fmaf(Ts[lane][c], Gs[c][i], v);
+                v *= -R.t[i];
+            }
+            __syncwarp();
+            if (lane < i)
+                Ts[lane][i] = v;
+            else if (lane == i)
+                Ts[i][i] = R.t[i];
+            __syncwarp();
+        }
+        float *o = T + ((size_t)s * gridDim.x + jb) * kWyB * kWyB;
+        for (int r = 0; r < kWyB; r++)
+            o[r * kWyB + lane] = Ts[r][lane];
+    }
+}
+
+// Column offsets of the CTA's kWyCols columns of Y in out (-1 past n).
+__device__ __forceinline__ void wy_load_cols(long long *cols, const NosDesc &d, const int *perm,
+                                             int n, int s, int j0) {
+    if (threadIdx.x < kWyCols) {
+        const int j = j0 + threadIdx.x;
+        cols[threadIdx.x] = j < n ? d.out_off + (long long)perm[(size_t)s * n + j] * d.m : -1;
+    }
+}
+
+// Partial W = V^T Y over rows [k0 + c R, k0 + (c + 1) R) of each sinogram
+// (R = 32 ns rows; none past m): part[s][c][r][j], 32 x kWyCols per CTA,
+// thread (warp, lane) owning reflectors 4 warp .. + 3 and columns 4 lane ..
+// + 3.  Rows are staged 32 at a time; the fills map a warp to 8 rows x 4
+// columns, which makes their shared-memory stores conflict-free.
+// grid (ceil(n / kWyCols), nchunk, n_sino).
+__global__ void __launch_bounds__(kWyThreads)
+wy_vty_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc,
+              const float2 *__restrict__ tau, const float2 *__restrict__ scale,
+              const int *__restrict__ perm, int n, int k0, int ns,
+              const float *__restrict__ out, float *__restrict__ part) {
+    __shared__ __align__(16) float Vs[32 * kWyVLd];
+    __shared__ __align__(16) float Ys[32 * kWyYLd];
+    __shared__ long long cols[kWyCols];
+    __shared__ WyRefl R;
+    const int j0 = blockIdx.x * kWyCols, c = blockIdx.y, s = blockIdx.z;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const NosDesc d = desc[s];
+    const int m = d.m;
+    const float2 *As = A + d.a_off;
+    const int rb = k0 + c * 32 * ns, re = min(rb + 32 * ns, m);
+    wy_load_refl(R, tau, scale, perm, n, s, k0);
+    wy_load_cols(cols, d, perm, n, s, j0);
+    __syncthreads(); // R and cols in place
+    constexpr int kPV = 32 * kWyB / kWyThreads, kPY = 32 * kWyCols / kWyThreads;
+    float vr[kPV], yr[kPY]; // the next 32 rows, fetched during the current ones
+    auto fetch = [&](int row0) {
+#pragma unroll
+        for (int q = 0; q < kPV; q++) {
+            const int e = threadIdx.x + kWyThreads * q;
+            const int i = (e >> 8) * 8 + (e & 7), r = (e >> 3) & 31, row = row0 + i;
+            vr[q] = row < re ? wy_v(As, m, R, n, k0, r, row) : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < kPY; q++) {
+            const int e = threadIdx.x + kWyThreads * q;
+            const int i = (e >> 10) * 8 + (e & 7), col = (e >> 3) & 127, row = row0 + i;
+            const long long o = cols[col];
+            yr[q] = o >= 0 && row < re ? out[o + row] : 0.f;
+        }
+    };
+    float acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int v = 0; v < 4; v++)
+            acc[u][v] = 0.f;
+    if (rb < re)
+        fetch(rb);
+    for (int row0 = rb; row0 < re; row0 += 32) {
+        __syncthreads(); // the previous tiles are read
+#pragma unroll
+        for (int q = 0; q < kPV; q++) {
+            const int e = threadIdx.x + kWyThreads * q;
+            Vs[((e >> 8) * 8 + (e & 7)) * kWyVLd + ((e >> 3) & 31)] = vr[q];
+        }
+#pragma unroll
+        for (int q = 0; q < kPY; q++) {
+            const int e = threadIdx.x + kWyThreads * q;
+            Ys[((e >> 10) * 8 + (e & 7)) * kWyYLd + ((e >> 3) & 127)] = yr[q];
+        }
+        __syncthreads();
+        if (row0 + 32 < re)
+            fetch(row0 + 32);
+#pragma unroll 8
+        for (int i = 0; i < 32; i++) {
+            const float4 a = *reinterpret_cast<const float4 *>(&Vs[i * kWyVLd + 4 * warp]);
+            const float4 y = *reinterpret_cast<const float4 *>(&Ys[i * kWyYLd + 4 * lane]);
+            const float av[4] = {a.x, a.y, a.z, a.w}, yv[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++)
+                    acc[u][v] = fmaf(av[u], yv[v], acc[u][v]);
+        }
+    }
+    float *p = part + ((size_t)s * gridDim.y + c) * kWyB * n;
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            const int j = j0 + 4 * lane + v;
+            if (j < n)
+                p[(size_t)(4 * warp + u) * n + j] = acc[u][v];
+        }
+}
+
+// W2 = T (sum of the nchunk partials), 32 x n per sinogram.  grid
+// (ceil(n / 32), n_sino).
+__global__ void __launch_bounds__(kWyThreads)
+wy_w2_kernel(const float *__restrict__ T, const float *__restrict__ part, int nchunk, int n,
+             int jb, int nbk, float *__restrict__ W2) {
+    __shared__ float Ws[kWyB][33];
+    __shared__ float Tt[kWyB][kWyB + 1];
+    const int j0 = blockIdx.x * 32, s = blockIdx.y;
+    const float *Tb = T + ((size_t)s * nbk + jb) * kWyB * kWyB;
+    for (int e = threadIdx.x; e < kWyB * 32; e += kWyThreads) {
+        const int r = e >> 5, jj = e & 31, j = j0 + jj;
+        // four independent sums, so that the chunks' loads overlap
+        float s4[4] = {0.f, 0.f, 0.f, 0.f};
+        if (j < n) {
+            const float *q = part + ((size_t)s * nchunk * kWyB + r) * n + j;
+            const size_t step = (size_t)kWyB * n;
+            int c = 0;
+#pragma unroll 2
+            for (; c + 4 <= nchunk; c += 4)
+#pragma unroll
+                for (int h = 0; h < 4; h++)
+                    s4[h] += q[(c + h) * step];
+            for (; c < nchunk; c++)
+                s4[0] += q[c * step];
+        }
+        Ws[r][jj] = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+        Tt[r][jj] = Tb[r * kWyB + jj];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kWyB * 32; e += kWyThreads) {
+        const int r = e >> 5, jj = e & 31, j = j0 + jj;
+        float v = 0.f;
+        for (int c = r; c < kWyB; c++)
+            v = fmaf(Tt[r][c], Ws[c][jj], v);
+        if (j < n)
+            W2[((size_t)s * kWyB + r) * n + j] = v;
+    }
+}
+
+// Y[rows, cols] -= V[rows, :] W2[:, cols] over rows [k0 + c R, .. + R)
+// (none past m): W2's 32 x kWyCols tile staged once, V 32 rows at a time;
+// lane = row, warp w = columns 16 w .. + 15, so each column's 32 rows are
+// one coalesced read-modify-write.  grid (ceil(n / kWyCols), nchunk, n_sino).
+__global__ void __launch_bounds__(kWyThreads)
+wy_update_kernel(const float2 *__restrict__ A, const NosDesc *__restrict__ desc,
+                 const float2 *__restrict__ tau, const float2 *__restrict__ scale,
+                 const int *__restrict__ perm, int n, int k0, int ns,
+                 const float *__restrict__ W2, float *__restrict__ out) {
+    __shared__ __align__(16) float Ws[kWyB * kWyYLd];
+    __shared__ float Vs[32 * 33];
+    __shared__ long long cols[kWyCols];
+    __shared__ WyRefl R;
+    const int j0 = blockIdx.x * kWyCols, c = blockIdx.y, s = blockIdx.z;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const NosDesc d = desc[s];
+    const int m = d.m;
+    const int rb = k0 + c * 32 * ns, re = min(rb + 32 * ns, m);
+    if (rb >= re)
+        return; // uniform: no rows of this sinogram here
+    const float2 *As = A + d.a_off;
+    wy_load_refl(R, tau, scale, perm, n, s, k0);
+    wy_load_cols(cols, d, perm, n, s, j0);
+    for (int e = threadIdx.x; e < kWyB * kWyCols; e += kWyThreads) {
+        const int r = e >> 7, q = e & 127, j = j0 + q;
+        Ws[r * kWyYLd + q] = j < n ? W2[((size_t)s * kWyB + r) * n + j] : 0.f;
+    }
+    const int cw = 16 * warp;
+    constexpr int kPV = 32 * kWyB / kWyThreads;
+    float vr[kPV]; // the next 32 rows of V, fetched during the current ones
+    auto fetch = [&](int row0) {
+#pragma unroll
+        for (int q = 0; q < kPV; q++) {
+            const int e = threadIdx.x + kWyThreads * q;
+            const int i = e & 31, r = e >> 5, row = row0 + i;
+            vr[q] = row < re ? wy_v(As, m, R, n, k0, r, row) : 0.f;
+        }
+    };
+    __syncthreads(); // R, cols and Ws in place
+    fetch(rb);
+    for (int row0 = rb; row0 < re; row0 += 32) {
+        __syncthreads(); // the previous V tile is read
+#pragma unroll
+        for (int q = 0; q < kPV; q++) {
+            const int e = threadIdx.x + kWyThreads * q;
+            Vs[(e & 31) * 33 + (e >> 5)] = vr[q];
+        }
+        __syncthreads();
+        if (row0 + 32 < re)
+            fetch(row0 + 32);
+        const int row = row0 + lane;
+        float yo[16]; // the rows' current values, loaded ahead of the FMAs
+#pragma unroll
+        for (int v = 0; v < 16; v++) {
+            const long long o = cols[cw + v];
+            yo[v] = o >= 0 && row < re ? out[o + row] : 0.f;
+        }
+        float acc[16];
+#pragma unroll
+        for (int v = 0; v < 16; v++)
+            acc[v] = 0.f;
+#pragma unroll 4
+        for (int r = 0; r < kWyB; r++) {
+            const float a = Vs[lane * 33 + r];
+            const float4 *w = reinterpret_cast<const float4 *>(&Ws[r * kWyYLd + cw]);
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const float4 x = w[h];
+                acc[4 * h] = fmaf(a, x.x, acc[4 * h]);
+                acc[4 * h + 1] = fmaf(a, x.y, acc[4 * h + 1]);
+                acc[4 * h + 2] = fmaf(a, x.z, acc[4 * h + 2]);
+                acc[4 * h + 3] = fmaf(a, x.w, acc[4 * h + 3]);
+            }
+        }
+        if (row < re)
+#pragma unroll
+            for (int v = 0; v < 16; v++) {
+                const long long o = cols[cw + v];
+                if (o >= 0)
+                    out[o + row] = yo[v] - acc[v];
+            }
     }
 }
 
@@ -1256,7 +1548,43 @@ cudaError_t launch_nos_sweep(int n, int n_sino, const NosWork &w, int max_sweeps
     return cudaGetLastError();
 }
 
-size_t nos_apply_smem(int max_m) { return sizeof(float) * (size_t)kQCols * max_m; }
+// Shape of the blocked Q application: row chunks of 32 ns rows, ns halved
+// from 8 until the GEMM passes have at least 3 CTAs per SM (or ns is 1).
+struct WyShape {
+    int nbk, tiles, ns, nchunk0;
+    size_t t_floats, part_floats, w2_floats;
+};
+static WyShape wy_shape(int n, int n_sino, int max_m) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    WyShape w;
+    w.nbk = (n + kWyB - 1) / kWyB;
+    w.tiles = (n + kWyCols - 1) / kWyCols;
+    w.ns = 8;
+    auto chunks = [&](int ns) { return (max_m + 32 * ns - 1) / (32 * ns); };
+    while (w.ns > 1 && (long long)w.tiles * chunks(w.ns) * n_sino < 3LL * std::max(sms, 1))
+        w.ns /= 2;
+    w.nchunk0 = chunks(w.ns);
+    w.t_floats = (size_t)n_sino * w.nbk * kWyB * kWyB;
+    w.part_floats = (size_t)n_sino * w.nchunk0 * kWyB * n;
+    w.w2_floats = (size_t)n_sino * kWyB * n;
+    return w;
+}
+
+// The blocked application takes over from the register kernel where the
+// aligned columns no longer fit its registers (measured on 8 sinograms of
+// 5795 x 720: the whole assembly 9.5 ms against 32.4 ms with a shared-memory
+// form of the one-reflector-at-a-time kernel; on 1843 x 360 the register
+// kernel is the faster, 1.04 against 1.33 ms).
+static bool wy_path(int n, int max_m) { return n > kNosMaxCols || max_m > 16 * kQThreads; }
+
+size_t nos_assemble_floats(int n, int n_sino, int max_m) {
+    if (!wy_path(n, max_m))
+        return 0;
+    const WyShape w = wy_shape(n, n_sino, max_m);
+    return w.t_floats + w.part_floats + w.w2_floats;
+}
 
 cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int n_sino,
                                 int max_m, const NosWork &w, float *out, cudaStream_t st) {
@@ -1272,24 +1600,33 @@ cudaError_t launch_nos_assemble(const float2 *A, const NosDesc *desc, int n, int
     rt_gemm_kernel<<<gt, 256, 0, st>>>(w.P, n, 1, w.P, 1, n, nullptr, 1.f, 0.f, n, w.X);
     rt_gemm_kernel<<<gt, 256, 0, st>>>(w.P, 1, n, w.X, 1, n, w.P, -0.5f, 1.5f, n, w.V);
     const dim3 gq((n + kQCols - 1) / kQCols, n_sino);
-    if (n <= kNosMaxCols && max_m <= 8 * kQThreads) {
+    if (!wy_path(n, max_m) && max_m <= 8 * kQThreads) {
         nos_apply_q_reg_kernel<8><<<gq, kQThreads, 0, st>>>(A, desc, w.tau, w.scale, w.perm,
                                                              w.V, n, out);
         return cudaGetLastError();
     }
-    if (n <= kNosMaxCols && max_m <= 16 * kQThreads) {
+    if (!wy_path(n, max_m)) {
         nos_apply_q_reg_kernel<16><<<gq, kQThreads, 0, st>>>(A, desc, w.tau, w.scale, w.perm,
                                                               w.V, n, out);
         return cudaGetLastError();
     }
-    const size_t limit = opt_in_smem((const void *)nos_apply_q_kernel);
-    if (limit == 0)
-        return cudaErrorInvalidValue;
-    const size_t smem = nos_apply_smem(max_m);
-    if (smem > limit)
-        return cudaErrorInvalidValue;
-    nos_apply_q_kernel<<<dim3((n + kQCols - 1) / kQCols, n_sino), kQThreads, smem, st>>>(
-        A, desc, w.tau, w.scale, w.perm, w.V, n, out);
+    // Y = Q [P; 0] in the output, block by block (last block first)
+    const WyShape sh = wy_shape(n, n_sino, max_m);
+    float *T = w.wy, *part = T + sh.t_floats, *W2 = part + sh.part_floats;
+    wy_init_kernel<<<dim3(n, n_sino), kWyThreads, 0, st>>>(w.V, desc, w.perm, n, out);
+    wy_t_kernel<<<dim3(sh.nbk, n_sino), kWyThreads, 0, st>>>(A, desc, w.tau, w.scale, w.perm,
+                                                              n, T);
+    for (int jb = sh.nbk - 1; jb >= 0; jb--) {
+        const int k0 = jb * kWyB;
+        const int nch = (max_m - k0 + 32 * sh.ns - 1) / (32 * sh.ns);
+        const dim3 g(sh.tiles, nch, n_sino);
+        wy_vty_kernel<<<g, kWyThreads, 0, st>>>(A, desc, w.tau, w.scale, w.perm, n, k0, sh.ns,
+                                                 out, part);
+        wy_w2_kernel<<<dim3((n + 31) / 32, n_sino), kWyThreads, 0, st>>>(T, part, nch, n, jb,
+                                                                         sh.nbk, W2);
+        wy_update_kernel<<<g, kWyThreads, 0, st>>>(A, desc, w.tau, w.scale, w.perm, n, k0,
+                                                    sh.ns, W2, out);
+    }
     return cudaGetLastError();
 }
 
