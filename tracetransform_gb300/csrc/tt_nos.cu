@@ -1501,6 +1501,8 @@ cudaError_t launch_nos_factor(float2 *A, const NosDesc *desc, int n, int n_sino,
         qr_steps<16, 128>(A, desc, n, n_sino, w, st);
     else if (max_m <= 16 * kQrThreads)
         qr_steps<16, kQrThreads>(A, desc, n, n_sino, w, st);
+    else if (max_m <= 24 * kQrThreads)
+        qr_steps<24, kQrThreads>(A, desc, n, n_sino, w, st);
     else
         qr_steps<32, kQrThreads>(A, desc, n, n_sino, w, st);
     const long long nn = (long long)n * n;
