@@ -207,7 +207,9 @@ tt_status tt_circus_device(tt_plan *plan, const float *d_sino, int rows, int col
  * weighted medians); the Jacobi sweeps loop on the device (a conditional
  * graph node whose stop rule runs after each sweep).  *sweeps (may be NULL)
  * receives the number of sweeps -- asking for it adds a synchronisation at
- * the end. */
+ * the end.  TT_ERR_UNSUPPORTED for more than 1024 angles, for more than 8192
+ * aligned rows (rows plus the spread of the weighted-median offsets), or when
+ * the aligned rows are fewer than the angles. */
 tt_status tt_circus_orthonormal_device(tt_plan *plan, const float *d_sino, int rows, int cols,
                                        int n_sino, const tt_pfunctional *pfuncs, int n_p,
                                        float *d_out, int32_t *centers, int32_t *sweeps,
