@@ -23,14 +23,16 @@
 //                 and recomputed when cancellation sets in)
 //   Jacobi        one-sided Jacobi on X = R^T in float (R^T of a pivoted QR is
 //                 graded, so float rotations keep relative accuracy), block-
-//                 cyclic: round-robin rounds of 16-column block pairs, each
+//                 cyclic: round-robin rounds of 12-column block pairs, each
 //                 pair rotated in one CTA's shared memory with V updated once
 //                 per round through the accumulated rotation;
 //                 X V = U_X S, so polar(R) = V U_X^T
 //   assemble      P = V U_X^T (float) with one Newton-Schulz step to clean
 //                 its orthogonality, then polar(A P) = Q [P; 0] applied
 //                 reflector by reflector to groups of columns held in
-//                 registers, and the column permutation undone
+//                 registers (up to 4096 aligned rows) or by blocks of 32
+//                 reflectors in compact-WY form (above), straight into the
+//                 result columns, which undoes the column permutation
 //
 // Against the oracle's double one-sided Jacobi on the aligned matrix the
 // result agrees to ~3e-5 absolute (entries up to ~0.7) for condition numbers
